@@ -1,0 +1,200 @@
+/* infernal_gb300.h -- C ABI of the GB300 query-dependent-banded (QDB) CM scanners.
+ *
+ * This library replaces the CPU scanning DP of Infernal's search pipeline:
+ *
+ *   FastCYKScan()      src/cm_dpsearch.c:90     (declared src/infernal.h:2710)
+ *   FastIInsideScan()  src/cm_dpsearch.c:1106   (declared src/infernal.h:2712)
+ *   FastFInsideScan()  src/cm_dpsearch.c:1731   (declared src/infernal.h:2713)
+ *   RefTrCYKScan()     src/cm_dpsearch_trunc.c:79   (declared src/infernal.h:2722)
+ *   RefITrInsideScan() src/cm_dpsearch_trunc.c:741  (declared src/infernal.h:2724)
+ *
+ * Every entry point keeps the reference scanner's argument meaning, return
+ * codes and error text convention (status code + message in errbuf); the
+ * only differences are that the model is passed as a flat, already
+ * configured parameter block (cmgb_model_desc, uploaded once into a
+ * cmgb_model) instead of a CM_t, the rolling scan matrix lives on the GPU
+ * (cmgb_ctx) instead of a CM_SCAN_MX, and hits are appended to a
+ * cmgb_hitlist instead of a CM_TOPHITS.  An Infernal build binds the
+ * reference names to these calls with a ~100 line adapter that reads the
+ * CM_t fields listed below.
+ *
+ * All pointers are plain host pointers, all sizes plain integers; nothing in
+ * this header depends on CUDA, PyTorch or Easel headers.
+ */
+#ifndef INFERNAL_GB300_H
+#define INFERNAL_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Return codes: the Easel status codes the reference scanners return. */
+#define CMGB_OK          0   /* eslOK        */
+#define CMGB_EMEM        5   /* eslEMEM      */
+#define CMGB_EINCOMPAT  10   /* eslEINCOMPAT */
+#define CMGB_EINVAL     11   /* eslEINVAL    */
+#define CMGB_ERANGE     16   /* eslERANGE    */
+#define CMGB_ENODEV     30   /* no usable sm_103 GPU / CUDA runtime error */
+#define CMGB_ERRBUFSIZE 128  /* eslERRBUFSIZE */
+
+/* State types, unique state ids (src/infernal.h:193-243). */
+#define CMGB_D_st   0
+#define CMGB_MP_st  1
+#define CMGB_ML_st  2
+#define CMGB_MR_st  3
+#define CMGB_IL_st  4
+#define CMGB_IR_st  5
+#define CMGB_S_st   6
+#define CMGB_E_st   7
+#define CMGB_B_st   8
+#define CMGB_EL_st  9
+#define CMGB_BEGL_S 3
+
+/* Band sets (SMX_NOQDB / SMX_QDB1_TIGHT / SMX_QDB2_LOOSE, src/infernal.h). */
+#define CMGB_NOQDB      0
+#define CMGB_QDB1_TIGHT 1
+#define CMGB_QDB2_LOOSE 2
+
+/* Model flags (subset of cm->flags / cm->search_opts that the scanners read). */
+#define CMGB_LOCAL_BEGIN  (1 << 0)   /* CMH_LOCAL_BEGIN */
+#define CMGB_LOCAL_END    (1 << 1)   /* CMH_LOCAL_END   */
+#define CMGB_NOTGREEDY    (1 << 2)   /* CM_SEARCH_CMNOTGREEDY: optimal (gamma) hit resolution */
+
+/* Score sentinels (src/infernal.h:148-158). */
+#define CMGB_IMPOSSIBLE (-1e36f)
+#define CMGB_INFTY      987654321
+#define CMGB_LOGSUM_TBL 23000
+
+/* Truncated-pass indices (PLI_PASS_*, src/infernal.h:2097-2104). */
+#define CMGB_PASS_STD_ANY         0
+#define CMGB_PASS_5P_ONLY_FORCE   2
+#define CMGB_PASS_3P_ONLY_FORCE   3
+#define CMGB_PASS_5P_AND_3P_FORCE 4
+
+/* Truncation modes of a hit (TRMODE_*, src/infernal.h). */
+#define CMGB_TRMODE_J 3
+#define CMGB_TRMODE_L 2
+#define CMGB_TRMODE_R 1
+#define CMGB_TRMODE_T 0
+
+/* Flat view of a configured CM_t: exactly the fields the scanners read.
+ * Per-state tables are indexed [v] for v in 0..M-1; tsc/itsc have a fixed
+ * stride of 6 (MAXCONNECT) and oesc/ioesc a fixed stride of Kp*Kp (the
+ * reference allocates Kp for singlet emitters and Kp*Kp for pair emitters;
+ * only that prefix of each row is read). */
+typedef struct {
+  int          M;          /* cm->M */
+  int          W;          /* cm->W, maximum hit length */
+  int          K, Kp;      /* cm->abc->K, cm->abc->Kp (4 and 18 for RNA) */
+  int          flags;      /* CMGB_LOCAL_BEGIN | CMGB_LOCAL_END | CMGB_NOTGREEDY */
+  const int8_t *sttype;    /* cm->sttype[v] */
+  const int8_t *stid;      /* cm->stid[v]   */
+  const int   *cfirst;     /* cm->cfirst[v] */
+  const int   *cnum;       /* cm->cnum[v]   */
+  const int   *dmin1, *dmax1, *dmin2, *dmax2;  /* cm->qdbinfo bands */
+  const float *tsc;        /* [M*6]     cm->tsc      */
+  const float *oesc;       /* [M*Kp*Kp] cm->oesc     */
+  const float *endsc;      /* [M]       cm->endsc    */
+  const float *beginsc;    /* [M]       cm->beginsc  */
+  float        el_selfsc;  /* cm->el_selfsc */
+  const int   *itsc;       /* [M*6]     cm->itsc     */
+  const int   *ioesc;      /* [M*Kp*Kp] cm->ioesc    */
+  const int   *iendsc;     /* [M]       cm->iendsc   */
+  const int   *ibeginsc;   /* [M]       cm->ibeginsc */
+  int          iel_selfsc; /* cm->iel_selfsc */
+  const float *null;       /* [K] cm->null, background for NULL3 */
+  float        null3_omega;/* cm->null3_omega */
+  /* Truncated scanning (cm->trp, cm->lmesc/rmesc, cm->emap); may be NULL
+   * when the truncated scanners are not used. */
+  const float *lmesc, *rmesc;     /* [M*Kp] marginal left/right emission scores */
+  const int   *ilmesc, *irmesc;   /* [M*Kp] integer versions */
+  const float *tr_g_pty;   /* [3*M] trp->g_ptyAA[pty_idx][v] (global begins) */
+  const float *tr_l_pty;   /* [3*M] trp->l_ptyAA[pty_idx][v] (local begins)  */
+  const int   *tr_ig_pty;  /* [3*M] trp->ig_ptyAA */
+  const int   *tr_il_pty;  /* [3*M] trp->il_ptyAA */
+  const int   *ndidx;      /* [M]     cm->ndidx[v] */
+  const int   *emap_lpos;  /* [nodes] cm->emap->lpos */
+  const int   *emap_rpos;  /* [nodes] cm->emap->rpos */
+  int          clen;       /* cm->clen */
+} cmgb_model_desc;
+
+/* One hit (the fields of CM_HIT that the scanners set, src/infernal.h:2424). */
+typedef struct {
+  int64_t start, stop;   /* 1-based sequence coordinates, start <= stop */
+  int     root;          /* root state of the hit (0 or a local-begin state) */
+  int     mode;          /* CMGB_TRMODE_* */
+  float   score;         /* bit score (NULL3-corrected when requested) */
+} cmgb_hit;
+
+typedef struct cmgb_model_s   cmgb_model;
+typedef struct cmgb_ctx_s     cmgb_ctx;
+typedef struct cmgb_hitlist_s cmgb_hitlist;
+
+/* ---- logsum tables (init_ilogsum / FLogsumInit, src/logsum.c:74, 138) ---- */
+/* Fills the host copies once; must be called before the first scan. */
+void cmgb_logsum_init(void);
+
+/* ---- device contexts: per-thread scan matrix + stream (the GPU analogue of
+ * the per-worker CM_SCAN_MX clone, src/cmsearch.c:2555) ---- */
+int  cmgb_ctx_create(int device, cmgb_ctx **ret_ctx, char *errbuf);
+void cmgb_ctx_destroy(cmgb_ctx *ctx);
+/* Kernel launch shape override (0 keeps the tuned default). */
+int  cmgb_ctx_set_shape(cmgb_ctx *ctx, int tile_rows, int window_len, int ctas_per_sm);
+/* Device time of the last scan's kernels in milliseconds (CUDA events). */
+float cmgb_ctx_last_kernel_ms(const cmgb_ctx *ctx);
+/* Number of this library's kernels launched by the last scan. */
+int  cmgb_ctx_last_launches(const cmgb_ctx *ctx);
+
+/* ---- models: configured CM parameters uploaded to one device ---- */
+int  cmgb_model_create(cmgb_ctx *ctx, const cmgb_model_desc *desc, cmgb_model **ret_model, char *errbuf);
+void cmgb_model_destroy(cmgb_model *model);
+
+/* ---- hit lists (the CM_TOPHITS subset the scanners append to) ---- */
+cmgb_hitlist *cmgb_hitlist_create(void);
+void     cmgb_hitlist_destroy(cmgb_hitlist *hl);
+int64_t  cmgb_hitlist_count(const cmgb_hitlist *hl);
+int      cmgb_hitlist_get(const cmgb_hitlist *hl, int64_t idx, cmgb_hit *ret_hit);
+void     cmgb_hitlist_clear(cmgb_hitlist *hl);
+
+/* ---- scanners ----
+ * dsq is the Easel digitized sequence: dsq[1..L] residues (0..Kp-1), with
+ * sentinels in dsq[0] and dsq[L+1]; only dsq[i0..j0] is read.
+ * hitlist may be NULL (no hit reporting, as in the reference).
+ * ret_vsc may be NULL; otherwise it must hold M floats and receives the best
+ * score of every state (the reference allocates it for the caller; here the
+ * caller owns it).  ret_envi/ret_envj/ret_sc may be NULL. */
+
+/* Replaces FastCYKScan() (src/cm_dpsearch.c:90-681). */
+int cmgb_FastCYKScan(cmgb_ctx *ctx, cmgb_model *model, char *errbuf, int qdbidx,
+                     const uint8_t *dsq, int64_t i0, int64_t j0, float cutoff,
+                     cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
+                     int64_t *ret_envi, int64_t *ret_envj, float *ret_vsc, float *ret_sc);
+
+/* Replaces FastIInsideScan() (src/cm_dpsearch.c:1106-1693). */
+int cmgb_FastIInsideScan(cmgb_ctx *ctx, cmgb_model *model, char *errbuf, int qdbidx,
+                         const uint8_t *dsq, int64_t i0, int64_t j0, float cutoff,
+                         cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
+                         int64_t *ret_envi, int64_t *ret_envj, float *ret_vsc, float *ret_sc);
+
+/* Same scans with the residues already resident in device memory:
+ * d_dsq points at a device copy of dsq[0..j0+1] (same indexing as dsq). */
+int cmgb_FastCYKScan_dev(cmgb_ctx *ctx, cmgb_model *model, char *errbuf, int qdbidx,
+                         const uint8_t *d_dsq, int64_t i0, int64_t j0, float cutoff,
+                         cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
+                         int64_t *ret_envi, int64_t *ret_envj, float *ret_vsc, float *ret_sc);
+int cmgb_FastIInsideScan_dev(cmgb_ctx *ctx, cmgb_model *model, char *errbuf, int qdbidx,
+                             const uint8_t *d_dsq, int64_t i0, int64_t j0, float cutoff,
+                             cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
+                             int64_t *ret_envi, int64_t *ret_envj, float *ret_vsc, float *ret_sc);
+
+/* DP cell count of one scan of [i0,j0] with band set qdbidx: the
+ * algorithmic work unit, sum over j and non-E states of the band width
+ * (the count cm_CountSearchDPCalcs() approximates, src/cm_dpsearch.c:3099). */
+int64_t cmgb_count_cells(const cmgb_model_desc *desc, int qdbidx, int64_t L);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* INFERNAL_GB300_H */
