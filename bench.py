@@ -1,0 +1,343 @@
+"""Benchmark of the plain GPU QDB scan (CYK filter + Inside on survivors).
+
+Workload (one "step"): a seeded synthetic target of --mb megabases at 40% GC
+with CM-emitted sequences embedded on random strands, scanned on BOTH strands
+with the clen-305 Plant_SRP CM (939 states, 4 bifurcations; the stand-in for
+the synthetic clen-300 multibranch CM of the single-large-CM configuration):
+  1. FastCYKScan, QDB1 bands (beta 1e-7), NULL3, greedy, filter cutoff
+  2. survivor hits padded by W-1 and merged into windows
+     (pli_cyk_seq_filter, src/cm_pipeline.c:3566-3601)
+  3. FastIInsideScan, QDB2 bands (beta 1e-15), NULL3, greedy, on each window.
+The default 10 steps x 10 Mb cover the configuration's 100 Mb target.
+
+Metric: residues scanned per second (both strands counted) and GCUPS (DP
+cells per second).  `value` uses residues already resident in device memory
+(the *_dev entry points); `e2e` calls the host-buffer C ABI (host->device
+copy of the residues and device->host hit lists inside every call).
+
+`--impl reference` times the reference's scanner on the host cores instead:
+the reference's own FastCYKScan/FastIInsideScan compiled from source
+(oracle/_ref) where that library exists, otherwise the C restatement of them
+(oracle/cm_scan_oracle.c), one process per core, on a bounded sample of the
+same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CYK_CUT = 10.0      # CYK filter threshold in bits (stand-in for the F6 E-value cutoff)
+INS_CUT = 15.0      # final Inside threshold in bits
+
+
+def _env_int(k, d):
+    try:
+        return int(os.environ.get(k, d))
+    except ValueError:
+        return d
+
+
+def make_step_input(model_glob, step, mb, seed=20261203):
+    from infernal_gb300 import emit
+    rng = np.random.default_rng([seed, step])
+    L = int(mb * 1_000_000)
+    nhits = max(1, int(round(20 * mb / 10)))     # 200 hits per 100 Mb
+    ins = [emit.sample(model_glob, rng) for _ in range(nhits)]
+    dsq, spans = emit.make_target(rng, L, 0.40, ins)
+    return dsq, emit.revcomp_dsq(dsq)
+
+
+def windows_from_hits(hits, W, L):
+    """Pads survivors by W-1 and merges overlaps (src/cm_pipeline.c:3566-3601)."""
+    ws = []
+    for h in sorted(hits, key=lambda h: h[0]):
+        a, b = max(1, h[1] - (W - 1)), min(L, h[0] + (W - 1))
+        if ws and a <= ws[-1][1] + 1:
+            ws[-1][1] = max(ws[-1][1], b)
+        else:
+            ws.append([a, b])
+    return ws
+
+
+# ----------------------------------------------------------------------------
+def run_ours(args, rank, world):
+    import torch
+    from infernal_gb300 import cmfile, lib as L
+    mpath = os.path.join(ROOT, "tests", "golden", "Plant_SRP.model.npz")
+    m = cmfile.load_npz(mpath)
+    torch.cuda.set_device(0 if world == 1 else _env_int("LOCAL_RANK", 0))
+    dev = torch.cuda.current_device()
+    sc = L.Scanner(dev)
+    keep = []
+    desc = cmfile.make_desc(m, keep=keep)
+    lib = sc.lib
+    import ctypes
+
+    nsteps = args.warmup + args.steps
+    inputs = [make_step_input(m, rank * 100000 + s, args.mb) for s in range(nsteps)]
+    Lres = len(inputs[0][0]) - 2
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def step(strands, dev_ptrs):
+        """One pass; returns (hits, cells, kernel_ms, launches)."""
+        cells = 0
+        kms = 0.0
+        launches = 0
+        nh = 0
+        for k, dsq in enumerate(strands):
+            ptr = dev_ptrs[k] if dev_ptrs else None
+            r = sc.scan(m, dsq, 1, Lres, algo="cyk", qdbidx=1, cutoff=CYK_CUT, env_cutoff=CYK_CUT,
+                        device_ptr=ptr)
+            kms += r.kernel_ms; launches += sc.last_launches()
+            cells += lib.cmgb_count_cells(ctypes.byref(desc), 1, Lres)
+            for a, b in windows_from_hits(r.hits, m.W, Lres):
+                r2 = sc.scan(m, dsq, a, b, algo="inside", qdbidx=2, cutoff=INS_CUT, env_cutoff=INS_CUT,
+                             device_ptr=ptr)
+                kms += r2.kernel_ms; launches += sc.last_launches()
+                cells += lib.cmgb_count_cells(ctypes.byref(desc), 2, b - a + 1)
+                nh += len(r2.hits)
+        return nh, cells, kms, launches
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def timed(use_dev):
+        dev_inputs = []
+        if use_dev:
+            for s in range(nsteps):
+                dev_inputs.append([torch.from_numpy(x).to("cuda") for x in inputs[s]])
+        torch.cuda.synchronize()
+        for s in range(args.warmup):
+            step(inputs[s], [t.data_ptr() for t in dev_inputs[s]] if use_dev else None)
+        tot, cells, kms, launches, nh = 0.0, 0, 0.0, 0, 0
+        for s in range(args.warmup, nsteps):
+            flush.fill_(float(s))                  # evict L2 between timed steps
+            barrier()
+            t0 = time.perf_counter()
+            h, c, k, l = step(inputs[s], [t.data_ptr() for t in dev_inputs[s]] if use_dev else None)
+            barrier()
+            tot += time.perf_counter() - t0
+            cells += c; kms += k; launches += l; nh += h
+        del dev_inputs
+        return tot, cells, kms, launches, nh
+
+    clk = start_clock_sampler(rank)
+    t_dev, cells, kms, launches, nh = timed(True)
+    clocks = stop_clock_sampler(clk)
+    t_e2e, _, _, _, _ = timed(False)
+    if world > 1:
+        tt = torch.tensor([t_dev, t_e2e], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_dev, t_e2e = float(tt[0]), float(tt[1])
+    res_per_rank = 2 * Lres * args.steps
+    total_res = res_per_rank * world
+    value = total_res / t_dev / 1e6
+    e2e = total_res / t_e2e / 1e6
+    out = {
+        "metric": "Mres/s scanned (both strands), plain GPU QDB-CYK + Inside scan",
+        "value": round(value, 3), "unit": "Mres/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1000 * t_dev / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (CYK) + int32 (Inside)", "data": "synthetic",
+        "config": {"workload": f"Plant_SRP CM stand-in (M={m.M}, clen={m.clen}, W={m.W}, 4 B), "
+                               f"{args.mb} Mb x 2 strands per step, GC 0.40, {max(1, round(2 * args.mb))} emitted hits per step; "
+                               f"CYK QDB1 cutoff {CYK_CUT} bits -> Inside QDB2 cutoff {INS_CUT} bits, NULL3, greedy",
+                   "residues_per_step": 2 * Lres, "l2": "flushed between timed steps (256 MB write)",
+                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+        "gcups": round(cells * world / t_dev / 1e9, 2),
+        "kernel_gcups": round(cells / (kms / 1e3) / 1e9, 2) if kms > 0 else None,
+        "kernel_ms_per_step": round(kms / args.steps, 3),
+        "e2e": {"value": round(e2e, 3), "unit": "Mres/s", "h2d_bytes_per_step": 2 * (Lres + 2),
+                "d2h_bytes_per_step": None},
+        "gpu_launches": launches,
+        "hits_per_step": nh / args.steps,
+        "clocks": clocks,
+    }
+    out["roofline"] = roofline_block(cells, kms, Lres, args)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(m, inputs[args.warmup][0], threads=1, seconds=args.cpu_seconds)
+    sc.close()
+    return out
+
+
+def roofline_block(cells, kms, Lres, args):
+    """The scan kernel is not bandwidth bound: its algorithmic DRAM traffic is
+    the residues (1 byte each) and the hit records; the DP state stays in
+    shared memory / L2.  Reported against the measured HBM copy peak."""
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            peaks = json.load(fh)
+    except OSError:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    alg_bytes = 2 * (Lres + 2) * args.steps
+    ach = alg_bytes / (kms / 1e3) / 1e9 if kms > 0 else 0.0
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "qdb_scan_cyk_traffic.json")
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get("dram_bytes_per_residue")
+            if traffic is not None:
+                traffic = traffic * 2 * (Lres + 2)
+        except Exception:
+            traffic = None
+    return {"bound": "hbm", "achieved": round(ach, 4), "peak": peak, "unit": "GB/s",
+            "frac": round(ach / peak, 8), "traffic": traffic,
+            "note": "algorithmic bytes = residues only; the DP is bound by shared-memory/ALU issue, see cell rate"}
+
+
+def cpu_baseline(m, dsq, threads=1, seconds=10.0):
+    """Times the CPU scanner (reference build if present, else the oracle port)
+    on a prefix of one strand, sized to about `seconds` of work."""
+    import oracle
+    use_ref = os.path.exists(oracle.REF_SO)
+    n = 2000
+    t0 = time.perf_counter()
+    oracle.scan(m, dsq, 1, n, algo="cyk", qdbidx=1, cutoff=CYK_CUT, env_cutoff=CYK_CUT, reference=use_ref)
+    dt = time.perf_counter() - t0
+    n2 = int(min(len(dsq) - 2, max(n, n * seconds / max(dt, 1e-3))))
+    t0 = time.perf_counter()
+    oracle.scan(m, dsq, 1, n2, algo="cyk", qdbidx=1, cutoff=CYK_CUT, env_cutoff=CYK_CUT, reference=use_ref)
+    dt = time.perf_counter() - t0
+    return {"value": round(n2 / dt / 1e6, 6), "unit": "Mres/s", "cores": threads,
+            "kind": "reference" if use_ref else "port",
+            "sample": f"FastCYKScan QDB1 over the first {n2} residues of one strand of the step-{0} target"}
+
+
+def _ref_worker(argv):
+    mb, idx, nres, use_ref = argv
+    import oracle
+    from infernal_gb300 import cmfile
+    m = cmfile.load_npz(os.path.join(ROOT, "tests", "golden", "Plant_SRP.model.npz"))
+    dsq, _ = make_step_input(m, 1000 + idx, min(mb, 0.1))
+    t0 = time.perf_counter()
+    oracle.scan(m, dsq, 1, nres, algo="cyk", qdbidx=1, cutoff=CYK_CUT, env_cutoff=CYK_CUT, reference=use_ref)
+    return nres, time.perf_counter() - t0
+
+
+def run_reference(args, rank, world):
+    """CPU reference arm: all host cores, one process per core."""
+    import multiprocessing as mp
+    import oracle
+    from infernal_gb300 import cmfile
+    oracle.build_oracle()
+    use_ref = os.path.exists(oracle.REF_SO)
+    ncpu = len(os.sched_getaffinity(0))
+    m = cmfile.load_npz(os.path.join(ROOT, "tests", "golden", "Plant_SRP.model.npz"))
+    # size the per-process sample from a short single-process probe
+    dsq, _ = make_step_input(m, 999, 0.01)
+    t0 = time.perf_counter()
+    oracle.scan(m, dsq, 1, 1500, algo="cyk", qdbidx=1, cutoff=CYK_CUT, reference=use_ref)
+    rate = 1500 / (time.perf_counter() - t0)
+    per_step_s = max(2.0, args.ref_step_seconds)
+    nres = int(max(1500, min(90000, rate * per_step_s)))
+    ctx = mp.get_context("spawn")
+    times = []
+    with ctx.Pool(ncpu) as pool:
+        for s in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            res = pool.map(_ref_worker, [(args.mb, s * ncpu + k, nres, use_ref) for k in range(ncpu)])
+            dt = time.perf_counter() - t0
+            if s >= args.warmup:
+                times.append((sum(r[0] for r in res), dt))
+    tot_res = sum(t[0] for t in times)
+    tot_t = sum(t[1] for t in times)
+    v = tot_res / tot_t / 1e6
+    return {
+        "impl": "reference", "metric": "Mres/s scanned (both strands), plain GPU QDB-CYK + Inside scan",
+        "value": round(v, 6), "unit": "Mres/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1000 * tot_t / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (CYK)", "data": "synthetic",
+        "config": {"workload": "same model and target distribution as the GPU arm; CYK QDB1 filter scan per core",
+                   "parallelism": f"{ncpu} host processes"},
+        "cpu_baseline": {"value": round(v, 6), "unit": "Mres/s", "cores": ncpu, "kind": "reference" if use_ref else "port",
+                         "sample": f"{nres} residues per process per step, {ncpu} processes"},
+        "e2e": {"value": round(v, 6), "unit": "Mres/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+_clk = {}
+
+
+def start_clock_sampler(rank):
+    if rank != 0:
+        return None
+    os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
+    path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+    try:
+        fh = open(path, "w")
+        p = subprocess.Popen(["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,"
+                              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                              "--format=csv,noheader,nounits", "-lms", "200"], stdout=fh, stderr=subprocess.DEVNULL)
+        return (p, fh, path)
+    except Exception:
+        return None
+
+
+def stop_clock_sampler(h):
+    if not h:
+        return None
+    p, fh, path = h
+    p.terminate()
+    p.wait()
+    fh.close()
+    sm, mx, reasons = [], 0, set()
+    for ln in open(path):
+        f = [x.strip() for x in ln.split(",")]
+        if len(f) < 8 or f[0] != str(os.environ.get("CUDA_VISIBLE_DEVICES", "0")).split(",")[0] and len(f) < 8:
+            continue
+        try:
+            sm.append(float(f[1])); mx = max(mx, float(f[2]))
+        except ValueError:
+            continue
+        for name, val in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"), f[4:8]):
+            if val.lower().startswith("active"):
+                reasons.add(name)
+    if not sm:
+        return None
+    return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--mb", type=float, default=10.0, help="megabases of target per step (scanned on both strands)")
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--ref-step-seconds", type=float, default=8.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = _env_int("WORLD_SIZE", 1)
+    rank = _env_int("RANK", 0)
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        print(json.dumps(run_reference(args, rank, world)))
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    out = run_ours(args, rank, world)
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

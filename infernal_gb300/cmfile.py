@@ -174,6 +174,7 @@ class CMModel:
     dmin2: np.ndarray = None
     dmax2: np.ndarray = None
     t: np.ndarray = None          # [M, 6] float32 probabilities
+    t_global: np.ndarray = None   # [M, 6] transitions before local configuration
     e: np.ndarray = None          # [M, K*K] float32 probabilities
     null: np.ndarray = None       # [K] float32
     begin: np.ndarray = None
@@ -301,6 +302,7 @@ def read_cm(path: str, which: int = 0) -> CMModel:
         m.stid[v] = _STID[(int(m.ndtype[nd]), st)]
         v += 1
     _renormalize(m)
+    m.t_global = m.t.copy()
     return m
 
 
@@ -591,7 +593,7 @@ def make_desc(m: CMModel, flags_extra: int = 0, keep: Optional[list] = None) -> 
 # ---- flat (npz) serialisation of a configured model --------------------------
 _ARRAYS = ("sttype", "stid", "ndidx", "cfirst", "cnum", "plast", "pnum", "ndtype", "nodemap",
            "dmin1", "dmax1", "dmin2", "dmax2", "null", "tsc", "itsc", "oesc", "ioesc",
-           "endsc", "beginsc", "iendsc", "ibeginsc", "lmesc", "rmesc", "ilmesc", "irmesc")
+           "endsc", "beginsc", "iendsc", "ibeginsc", "lmesc", "rmesc", "ilmesc", "irmesc", "t_global", "e")
 _SCALARS = ("M", "nodes", "clen", "W", "K", "Kp", "flags", "iel_selfsc")
 _F32 = ("el_selfsc", "null3_omega", "pbegin", "pend")
 
@@ -613,7 +615,7 @@ def load_npz(path: str) -> CMModel:
     m = CMModel(name=str(z["name"]), M=int(z["M"]), nodes=int(z["nodes"]), clen=int(z["clen"]),
                 W=int(z["W"]))
     for a in _ARRAYS:
-        setattr(m, a, z[a])
+        setattr(m, a, z[a] if a in z else None)
     for s in _SCALARS:
         setattr(m, s, int(z[s]))
     for s in _F32:

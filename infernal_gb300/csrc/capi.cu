@@ -1,0 +1,425 @@
+// capi.cu -- C ABI of the GB300 QDB scanners (declared in include/infernal_gb300.h).
+//
+// Device memory per context: the per-CTA carry rows and BEGL history rings
+// (the scan matrix of src/cm_mx.c:5686, kept as rolling tiles), the residue
+// staging buffer, the candidate-cell buffer and a small control block.
+// Models hold the uploaded score tables and one execution plan per band set.
+#ifdef CMGB_HOST_EMULATION
+#include "cmgb_emu.h"
+#endif
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/infernal_gb300.h"
+#include "hits.h"
+#include "scan_kernel.cuh"
+#include "scan_plan.h"
+
+using namespace cmgb;
+
+#define ERRF(code, ...) do { if (errbuf) snprintf(errbuf, CMGB_ERRBUFSIZE, __VA_ARGS__); return (code); } while (0)
+#define CUDA_TRY(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) ERRF(CMGB_ENODEV, "CUDA error %s at %s:%d", cudaGetErrorString(e_), __FILE__, __LINE__); } while (0)
+
+#ifdef CMGB_HOST_EMULATION
+static const int kThreads = CMGB_EMU_THREADS;
+template <bool INS>
+static void launch_qdb(int grid, int nt, size_t smem, cudaStream_t, const KParams &kp)
+{
+  std::vector<std::vector<float>> sm(grid, std::vector<float>(smem / 4 + 16));
+  std::vector<std::barrier<> *> bars;
+  for (int b = 0; b < grid; b++) bars.push_back(new std::barrier<>(nt));
+  std::vector<std::thread> th;
+  for (int b = 0; b < grid; b++)
+    for (int t = 0; t < nt; t++)
+      th.emplace_back([&, b, t] { cmgb_emu_bar = bars[b]; qdb_scan_body<INS>(kp, sm[b].data(), t, nt, b); });
+  for (auto &x : th) x.join();
+  for (auto *b : bars) delete b;
+}
+#else
+static const int kThreads = 256;
+template <bool INS>
+static void launch_qdb(int grid, int nt, size_t smem, cudaStream_t s, const KParams &kp)
+{
+  qdb_scan_kernel<INS><<<grid, nt, smem, s>>>(kp);
+}
+#endif
+static const int kCandCap = 1 << 22;
+
+struct Control {            // device control block, zeroed/initialised per scan
+  int queue;
+  int ncand;
+  int err;
+  int pad;
+  long long env[2];
+  unsigned best;
+  unsigned pad2[3];
+};
+
+struct cmgb_hitlist_s { std::vector<cmgb_hit> h; };
+
+struct DevPlan {
+  bool built = false;
+  int T = 0;
+  ScanPlan plan;
+  StateInfo *d_states = nullptr;
+};
+
+struct cmgb_model_s {
+  cmgb_ctx *ctx = nullptr;
+  int M = 0, W = 0, K = 0, Kp = 0, flags = 0;
+  std::vector<float> null;
+  float null3_omega = 0.f;
+  // host copy of the description arrays (the plan builder re-reads them)
+  std::vector<int8_t> sttype, stid;
+  std::vector<int> cfirst, cnum, dmin1, dmax1, dmin2, dmax2, itsc, iendsc, ibeginsc;
+  std::vector<float> tsc, endsc, beginsc;
+  float el_selfsc = 0.f; int iel_selfsc = 0;
+  cmgb_model_desc desc;      // points into the vectors above
+  float *d_oesc = nullptr;
+  int *d_ioesc = nullptr;
+  DevPlan plans[3][2];       // [qdbidx][0: T as requested]
+};
+
+struct cmgb_ctx_s {
+  int device = 0;
+  int nsm = 0;
+  int max_smem_optin = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  float last_ms = 0.f;
+  int last_launches = 0;
+  int tile_rows = 16, window_len = 0, ctas_per_sm = 0;
+  // scratch
+  float *d_carry = nullptr; size_t carry_bytes = 0;
+  float *d_ring = nullptr; size_t ring_bytes = 0;
+  unsigned char *d_dsq = nullptr; size_t dsq_bytes = 0;
+  Cand *d_cand = nullptr;
+  Control *d_ctl = nullptr;
+  unsigned *d_vsc = nullptr; int vsc_len = 0;
+  int *d_ilog = nullptr;
+  Control *h_ctl = nullptr;       // pinned
+  std::vector<CandHost> h_cand;
+};
+
+static int grow(void **p, size_t *cur, size_t need, char *errbuf)
+{
+  if (need <= *cur) return CMGB_OK;
+  if (*p) cudaFree(*p);
+  *p = nullptr; *cur = 0;
+  size_t n = need + need / 4;
+  if (cudaMalloc(p, n) != cudaSuccess) { *p = nullptr; ERRF(CMGB_EMEM, "out of device memory (%zu bytes)", n); }
+  *cur = n;
+  return CMGB_OK;
+}
+
+extern "C" void cmgb_logsum_init(void) { logsum_tables(nullptr, nullptr); }
+
+extern "C" int cmgb_ctx_create(int device, cmgb_ctx **ret, char *errbuf)
+{
+  *ret = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device)
+    ERRF(CMGB_ENODEV, "no CUDA device %d available", device);
+  CUDA_TRY(cudaSetDevice(device));
+  cudaDeviceProp prop;
+  CUDA_TRY(cudaGetDeviceProperties(&prop, device));
+  if (prop.major < 10) ERRF(CMGB_ENODEV, "device %d is sm_%d%d; this library is built for sm_103a", device, prop.major, prop.minor);
+  std::unique_ptr<cmgb_ctx> c(new cmgb_ctx);
+  c->device = device;
+  c->nsm = prop.multiProcessorCount;
+  c->max_smem_optin = (int) prop.sharedMemPerBlockOptin;
+  CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  CUDA_TRY(cudaEventCreate(&c->ev0));
+  CUDA_TRY(cudaEventCreate(&c->ev1));
+  CUDA_TRY(cudaMalloc(&c->d_cand, sizeof(Cand) * (size_t) kCandCap));
+  CUDA_TRY(cudaMalloc(&c->d_ctl, sizeof(Control)));
+  CUDA_TRY(cudaMallocHost(&c->h_ctl, sizeof(Control)));
+  const int *ilog;
+  logsum_tables(nullptr, &ilog);
+  CUDA_TRY(cudaMalloc(&c->d_ilog, sizeof(int) * 23000));
+  CUDA_TRY(cudaMemcpy(c->d_ilog, ilog, sizeof(int) * 23000, cudaMemcpyHostToDevice));
+  *ret = c.release();
+  return CMGB_OK;
+}
+
+extern "C" void cmgb_ctx_destroy(cmgb_ctx *c)
+{
+  if (!c) return;
+  cudaSetDevice(c->device);
+  cudaFree(c->d_carry); cudaFree(c->d_ring); cudaFree(c->d_dsq); cudaFree(c->d_cand);
+  cudaFree(c->d_ctl); cudaFree(c->d_vsc); cudaFree(c->d_ilog);
+  cudaFreeHost(c->h_ctl);
+  cudaEventDestroy(c->ev0); cudaEventDestroy(c->ev1);
+  cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+extern "C" int cmgb_ctx_set_shape(cmgb_ctx *c, int tile_rows, int window_len, int ctas_per_sm)
+{
+  if (!c) return CMGB_EINVAL;
+  if (tile_rows < 0 || tile_rows > 64 || window_len < 0 || ctas_per_sm < 0 || ctas_per_sm > 8) return CMGB_EINVAL;
+  c->tile_rows = tile_rows ? tile_rows : 16;
+  c->window_len = window_len;
+  c->ctas_per_sm = ctas_per_sm;
+  return CMGB_OK;
+}
+extern "C" float cmgb_ctx_last_kernel_ms(const cmgb_ctx *c) { return c ? c->last_ms : 0.f; }
+extern "C" int cmgb_ctx_last_launches(const cmgb_ctx *c) { return c ? c->last_launches : 0; }
+
+extern "C" int cmgb_model_create(cmgb_ctx *c, const cmgb_model_desc *d, cmgb_model **ret, char *errbuf)
+{
+  *ret = nullptr;
+  if (!c || !d) ERRF(CMGB_EINVAL, "cmgb_model_create: NULL argument");
+  if (d->M < 2 || d->W < 1 || d->K != 4 || d->Kp != 18) ERRF(CMGB_EINCOMPAT, "cmgb_model_create: unsupported model shape (M=%d W=%d K=%d Kp=%d)", d->M, d->W, d->K, d->Kp);
+  const int M = d->M, KK = d->Kp * d->Kp;
+  std::unique_ptr<cmgb_model> m(new cmgb_model);
+  m->ctx = c; m->M = M; m->W = d->W; m->K = d->K; m->Kp = d->Kp; m->flags = d->flags;
+  m->null.assign(d->null, d->null + d->K);
+  m->null3_omega = d->null3_omega;
+  m->sttype.assign(d->sttype, d->sttype + M); m->stid.assign(d->stid, d->stid + M);
+  m->cfirst.assign(d->cfirst, d->cfirst + M); m->cnum.assign(d->cnum, d->cnum + M);
+  m->dmin1.assign(d->dmin1, d->dmin1 + M); m->dmax1.assign(d->dmax1, d->dmax1 + M);
+  m->dmin2.assign(d->dmin2, d->dmin2 + M); m->dmax2.assign(d->dmax2, d->dmax2 + M);
+  m->tsc.assign(d->tsc, d->tsc + 6 * M); m->itsc.assign(d->itsc, d->itsc + 6 * M);
+  m->endsc.assign(d->endsc, d->endsc + M); m->beginsc.assign(d->beginsc, d->beginsc + M);
+  m->iendsc.assign(d->iendsc, d->iendsc + M); m->ibeginsc.assign(d->ibeginsc, d->ibeginsc + M);
+  m->el_selfsc = d->el_selfsc; m->iel_selfsc = d->iel_selfsc;
+  std::memset(&m->desc, 0, sizeof(m->desc));
+  cmgb_model_desc &D = m->desc;
+  D.M = M; D.W = d->W; D.K = d->K; D.Kp = d->Kp; D.flags = d->flags;
+  D.sttype = m->sttype.data(); D.stid = m->stid.data(); D.cfirst = m->cfirst.data(); D.cnum = m->cnum.data();
+  D.dmin1 = m->dmin1.data(); D.dmax1 = m->dmax1.data(); D.dmin2 = m->dmin2.data(); D.dmax2 = m->dmax2.data();
+  D.tsc = m->tsc.data(); D.itsc = m->itsc.data(); D.endsc = m->endsc.data(); D.beginsc = m->beginsc.data();
+  D.iendsc = m->iendsc.data(); D.ibeginsc = m->ibeginsc.data();
+  D.el_selfsc = d->el_selfsc; D.iel_selfsc = d->iel_selfsc;
+  D.null = m->null.data(); D.null3_omega = d->null3_omega;
+  if (cudaSetDevice(c->device) != cudaSuccess) ERRF(CMGB_ENODEV, "cudaSetDevice failed");
+  if (cudaMalloc(&m->d_oesc, sizeof(float) * (size_t) M * KK) != cudaSuccess ||
+      cudaMalloc(&m->d_ioesc, sizeof(int) * (size_t) M * KK) != cudaSuccess)
+    ERRF(CMGB_EMEM, "out of device memory for emission tables");
+  CUDA_TRY(cudaMemcpy(m->d_oesc, d->oesc, sizeof(float) * (size_t) M * KK, cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(m->d_ioesc, d->ioesc, sizeof(int) * (size_t) M * KK, cudaMemcpyHostToDevice));
+  *ret = m.release();
+  return CMGB_OK;
+}
+
+extern "C" void cmgb_model_destroy(cmgb_model *m)
+{
+  if (!m) return;
+  cudaSetDevice(m->ctx->device);
+  cudaFree(m->d_oesc); cudaFree(m->d_ioesc);
+  for (auto &row : m->plans) for (auto &p : row) cudaFree(p.d_states);
+  delete m;
+}
+
+extern "C" cmgb_hitlist *cmgb_hitlist_create(void) { return new cmgb_hitlist; }
+extern "C" void cmgb_hitlist_destroy(cmgb_hitlist *hl) { delete hl; }
+extern "C" int64_t cmgb_hitlist_count(const cmgb_hitlist *hl) { return hl ? (int64_t) hl->h.size() : 0; }
+extern "C" int cmgb_hitlist_get(const cmgb_hitlist *hl, int64_t i, cmgb_hit *h)
+{
+  if (!hl || !h || i < 0 || i >= (int64_t) hl->h.size()) return CMGB_EINVAL;
+  *h = hl->h[i];
+  return CMGB_OK;
+}
+extern "C" void cmgb_hitlist_clear(cmgb_hitlist *hl) { if (hl) hl->h.clear(); }
+
+// Builds (once) the plan of band set qdbidx for the context's tile size,
+// shrinking the tile until its shared memory fits the device.
+static int get_plan(cmgb_model *m, int qdbidx, DevPlan **ret, char *errbuf)
+{
+  cmgb_ctx *c = m->ctx;
+  DevPlan &dp = m->plans[qdbidx][0];
+  if (dp.built && dp.T == c->tile_rows) { *ret = &dp; return CMGB_OK; }
+  if (dp.d_states) { cudaFree(dp.d_states); dp.d_states = nullptr; }
+  PlanOut po;
+  int T = c->tile_rows;
+  for (;;) {
+    po = PlanOut();
+    if (!build_plan(&m->desc, qdbidx, T, kThreads, &po)) ERRF(CMGB_EINCOMPAT, "%s", po.err.c_str());
+    if (po.plan.smem_bytes + 64 <= c->max_smem_optin) break;
+    if (T <= 2) ERRF(CMGB_ERANGE, "model needs %d bytes of shared memory per CTA even with 2-row tiles", po.plan.smem_bytes);
+    T = T > 8 ? T - 4 : T - 2;
+  }
+  CUDA_TRY(cudaMalloc(&dp.d_states, sizeof(StateInfo) * m->M));
+  CUDA_TRY(cudaMemcpy(dp.d_states, po.states.data(), sizeof(StateInfo) * m->M, cudaMemcpyHostToDevice));
+  dp.plan = po.plan;
+  dp.T = c->tile_rows;
+  dp.built = true;
+  *ret = &dp;
+  return CMGB_OK;
+}
+
+// Common driver of the standard scanners.  dev_dsq: device residues indexed
+// by sequence coordinate (may be shifted); host_dsq: host residues (for
+// NULL3), may be NULL when do_null3 is FALSE or the device copy suffices.
+static int scan_std(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, bool ins,
+                    const uint8_t *host_dsq, const uint8_t *dev_dsq_in, int64_t i0, int64_t j0,
+                    float cutoff, cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
+                    int64_t *ret_envi, int64_t *ret_envj, float *ret_vsc, float *ret_sc)
+{
+  const char *fn = ins ? "FastIInsideScan" : "FastCYKScan";
+  if (!c || !m) ERRF(CMGB_EINVAL, "%s, NULL context or model", fn);
+  if (j0 < i0) ERRF(CMGB_EINCOMPAT, "%s, i0: %lld j0: %lld", fn, (long long) i0, (long long) j0);
+  if (i0 < 1) ERRF(CMGB_EINCOMPAT, "%s, i0 must be >= 1", fn);
+  if (host_dsq == nullptr && dev_dsq_in == nullptr) ERRF(CMGB_EINCOMPAT, "%s, dsq is NULL", fn);
+  if (qdbidx < 0 || qdbidx > 2) ERRF(CMGB_EINCOMPAT, "%s, qdbidx is invalid", fn);
+  int st;
+  CUDA_TRY(cudaSetDevice(c->device));
+  DevPlan *dp;
+  if ((st = get_plan(m, qdbidx, &dp, errbuf)) != CMGB_OK) return st;
+  const ScanPlan &P = dp->plan;
+  const int64_t L = j0 - i0 + 1;
+  const int W = m->W;
+
+  // residues: device copy of dsq[lo .. j0+1]
+  const unsigned char *d_dsq;
+  int64_t lo = i0 - W - 1; if (lo < 0) lo = 0;
+  if (dev_dsq_in) d_dsq = dev_dsq_in;
+  else {
+    size_t need = (size_t) (j0 + 2 - lo);
+    if ((st = grow((void **) &c->d_dsq, &c->dsq_bytes, need, errbuf)) != CMGB_OK) return st;
+    CUDA_TRY(cudaMemcpyAsync(c->d_dsq, host_dsq + lo, need, cudaMemcpyHostToDevice, c->stream));
+    d_dsq = c->d_dsq - lo;
+  }
+
+  // launch shape
+  int cps = c->ctas_per_sm;
+  if (cps == 0) cps = (2 * (P.smem_bytes + 1024) <= 228 * 1024) ? 2 : 1;
+  int grid_max = c->nsm * cps;
+  int64_t win = c->window_len;
+  if (win <= 0) {
+    win = (L + grid_max - 1) / grid_max;
+    int64_t minwin = 8LL * W;
+    if (win < minwin) win = minwin;
+  }
+  win = ((win + P.T - 1) / P.T) * P.T;
+  int64_t nwin = (L + win - 1) / win;
+  if (nwin > INT_MAX) ERRF(CMGB_ERANGE, "%s, too many windows", fn);
+  int grid = (int) std::min<int64_t>(nwin, grid_max);
+
+  size_t carry_need = sizeof(float) * 2 * (size_t) P.carry_elems * grid;
+  size_t ring_need = sizeof(float) * (size_t) P.ring_elems * grid;
+  if ((st = grow((void **) &c->d_carry, &c->carry_bytes, carry_need, errbuf)) != CMGB_OK) return st;
+  if ((st = grow((void **) &c->d_ring, &c->ring_bytes, ring_need, errbuf)) != CMGB_OK) return st;
+  if (ret_vsc && c->vsc_len < m->M) {
+    cudaFree(c->d_vsc); c->d_vsc = nullptr;
+    if (cudaMalloc(&c->d_vsc, sizeof(unsigned) * m->M) != cudaSuccess) ERRF(CMGB_EMEM, "out of device memory");
+    c->vsc_len = m->M;
+  }
+  Control *h = c->h_ctl;
+  std::memset(h, 0, sizeof(Control));
+  h->env[0] = LLONG_MAX; h->env[1] = -1;
+  CUDA_TRY(cudaMemcpyAsync(c->d_ctl, h, sizeof(Control), cudaMemcpyHostToDevice, c->stream));
+  if (ret_vsc) CUDA_TRY(cudaMemsetAsync(c->d_vsc, 0, sizeof(unsigned) * m->M, c->stream));
+
+  KParams kp;
+  std::memset(&kp, 0, sizeof(kp));
+  kp.st = dp->d_states; kp.plan = P;
+  kp.oesc = m->d_oesc; kp.ioesc = m->d_ioesc; kp.ilog = c->d_ilog;
+  kp.dsq = d_dsq; kp.i0 = i0; kp.j0 = j0; kp.win_len = win; kp.nwin = (int) nwin;
+  kp.queue = &c->d_ctl->queue; kp.carry = c->d_carry; kp.ring = c->d_ring;
+  kp.cand = c->d_cand; kp.ncand = &c->d_ctl->ncand; kp.cand_cap = kCandCap;
+  const bool greedy = !(m->flags & CMGB_NOTGREEDY);
+  kp.cand_cut = cutoff; kp.cand_pos = (hitlist && !greedy) ? 1 : 0;
+  if (!hitlist) { kp.cand_cut = 3.0e38f; kp.cand_pos = 0; }
+  kp.env_cut = env_cutoff; kp.env = c->d_ctl->env;
+  kp.vsc = ret_vsc ? c->d_vsc : nullptr; kp.best = &c->d_ctl->best; kp.err = &c->d_ctl->err;
+
+  const size_t smem = (size_t) P.smem_bytes;
+#ifndef CMGB_HOST_EMULATION
+  if (ins) CUDA_TRY(cudaFuncSetAttribute(qdb_scan_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+  else     CUDA_TRY(cudaFuncSetAttribute(qdb_scan_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+#endif
+  CUDA_TRY(cudaEventRecord(c->ev0, c->stream));
+  if (ins) launch_qdb<true>(grid, kThreads, smem, c->stream, kp);
+  else     launch_qdb<false>(grid, kThreads, smem, c->stream, kp);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaEventRecord(c->ev1, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(h, c->d_ctl, sizeof(Control), cudaMemcpyDeviceToHost, c->stream));
+  std::vector<unsigned> vscu;
+  if (ret_vsc) { vscu.resize(m->M); CUDA_TRY(cudaMemcpyAsync(vscu.data(), c->d_vsc, sizeof(unsigned) * m->M, cudaMemcpyDeviceToHost, c->stream)); }
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  CUDA_TRY(cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1));
+  c->last_launches = 1;
+  if (h->err) ERRF(CMGB_ERANGE, "%s, more than %d candidate hit cells; raise the cutoff", fn, kCandCap);
+
+  auto u2f = [](unsigned u) { if (u == 0) return CMGB_IMPOSSIBLE; unsigned b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u; float f; std::memcpy(&f, &b, 4); return f; };
+  const float best = u2f(h->best);
+  if (ret_sc) *ret_sc = best;
+  if (ret_envi) *ret_envi = (h->env[1] < 0) ? -1 : h->env[0];
+  if (ret_envj) *ret_envj = (h->env[1] < 0) ? -1 : h->env[1];
+  if (ret_vsc) { for (int v = 0; v < m->M; v++) ret_vsc[v] = u2f(vscu[v]); ret_vsc[0] = best; }
+
+  if (hitlist) {
+    const int n = h->ncand;
+    c->h_cand.resize(n);
+    if (n > 0) CUDA_TRY(cudaMemcpy(c->h_cand.data(), c->d_cand, sizeof(Cand) * n, cudaMemcpyDeviceToHost));
+    std::vector<uint8_t> res_copy;
+    const uint8_t *hd = host_dsq;
+    if (do_null3 && n > 0 && hd == nullptr) {
+      // device-resident residues: fetch [i0, j0] for the composition counts
+      res_copy.resize((size_t) (j0 + 2));
+      CUDA_TRY(cudaMemcpy(res_copy.data() + i0, dev_dsq_in + i0, (size_t) L, cudaMemcpyDeviceToHost));
+      hd = res_copy.data();
+    }
+    ResolveArgs ra;
+    ra.null = m->null.data(); ra.K = m->K; ra.null3_omega = m->null3_omega; ra.do_null3 = do_null3;
+    ra.greedy = greedy ? 1 : 0; ra.cutoff = cutoff; ra.i0 = i0; ra.j0 = j0; ra.dsq = hd;
+    resolve_hits(c->h_cand, ra, hitlist->h);
+  }
+  return CMGB_OK;
+}
+
+extern "C" int cmgb_FastCYKScan(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, const uint8_t *dsq, int64_t i0, int64_t j0,
+                                float cutoff, cmgb_hitlist *hl, int do_null3, float env_cutoff, int64_t *envi, int64_t *envj,
+                                float *vsc, float *sc)
+{
+  if (dsq == nullptr) ERRF(CMGB_EINCOMPAT, "FastCYKScan, dsq is NULL");
+  return scan_std(c, m, errbuf, qdbidx, false, dsq, nullptr, i0, j0, cutoff, hl, do_null3, env_cutoff, envi, envj, vsc, sc);
+}
+extern "C" int cmgb_FastIInsideScan(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, const uint8_t *dsq, int64_t i0, int64_t j0,
+                                    float cutoff, cmgb_hitlist *hl, int do_null3, float env_cutoff, int64_t *envi, int64_t *envj,
+                                    float *vsc, float *sc)
+{
+  if (dsq == nullptr) ERRF(CMGB_EINCOMPAT, "FastIInsideScan, dsq is NULL");
+  return scan_std(c, m, errbuf, qdbidx, true, dsq, nullptr, i0, j0, cutoff, hl, do_null3, env_cutoff, envi, envj, vsc, sc);
+}
+extern "C" int cmgb_FastCYKScan_dev(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, const uint8_t *d_dsq, int64_t i0, int64_t j0,
+                                    float cutoff, cmgb_hitlist *hl, int do_null3, float env_cutoff, int64_t *envi, int64_t *envj,
+                                    float *vsc, float *sc)
+{
+  if (d_dsq == nullptr) ERRF(CMGB_EINCOMPAT, "FastCYKScan, dsq is NULL");
+  return scan_std(c, m, errbuf, qdbidx, false, nullptr, d_dsq, i0, j0, cutoff, hl, do_null3, env_cutoff, envi, envj, vsc, sc);
+}
+extern "C" int cmgb_FastIInsideScan_dev(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, const uint8_t *d_dsq, int64_t i0, int64_t j0,
+                                        float cutoff, cmgb_hitlist *hl, int do_null3, float env_cutoff, int64_t *envi, int64_t *envj,
+                                        float *vsc, float *sc)
+{
+  if (d_dsq == nullptr) ERRF(CMGB_EINCOMPAT, "FastIInsideScan, dsq is NULL");
+  return scan_std(c, m, errbuf, qdbidx, true, nullptr, d_dsq, i0, j0, cutoff, hl, do_null3, env_cutoff, envi, envj, vsc, sc);
+}
+
+extern "C" int64_t cmgb_count_cells(const cmgb_model_desc *m, int qdbidx, int64_t L)
+{
+  const int *dmin = qdbidx == 1 ? m->dmin1 : qdbidx == 2 ? m->dmin2 : nullptr;
+  const int *dmax = qdbidx == 1 ? m->dmax1 : qdbidx == 2 ? m->dmax2 : nullptr;
+  const int Wl = (int) (m->W > L ? L : m->W);
+  int64_t cells = 0;
+  for (int v = 0; v < m->M; v++) {
+    if (m->sttype[v] == CMGB_E_st) continue;
+    int lo = m->sttype[v] == CMGB_MP_st ? 2 : 1;
+    if (dmin) lo = std::max(dmin[v], lo);
+    const int dn = std::min(lo, m->W), dx = dmax ? std::min(dmax[v], m->W) : m->W;
+    for (int64_t jp = 1; jp <= L && jp < Wl; jp++) { int hi = std::min((int) jp, dx); if (hi >= dn) cells += hi - dn + 1; }
+    if (L >= Wl) { int hi = std::min(Wl, dx); if (hi >= dn) cells += (int64_t) (hi - dn + 1) * (L - Wl + 1); }
+  }
+  return cells;
+}

@@ -1,0 +1,98 @@
+// scan_plan.h -- per-(model, band set) execution plan of the tiled QDB scan.
+//
+// The GPU scan advances each sequence window in tiles of T end positions j.
+// Inside a tile the states are swept from v = M-1 down to 0 (children before
+// parents, the order of the reference's `for (v = cm->M-1; ...)` loop,
+// src/cm_dpsearch.c:233), and every state's T x band cells are computed at
+// once from its children's tiles, which sit in shared memory.  A state's tile
+// buffer holds rows r = 0..T: row 0 is the state's last row of the previous
+// tile (the "carry", kept in global memory between tiles), rows 1..T are
+// j = t .. t+T-1.  Each buffer covers the padded d-range [lo, hi]: the
+// state's own band plus every cell any parent reads; cells outside the
+// state's band hold the values the reference's scan matrix holds there
+// (its d = 0 initialisation, src/cm_mx.c:6039-6082, or IMPOSSIBLE), so the
+// recurrences read children without per-cell band tests.
+//
+// This header is shared by the host planner (scan_plan.cpp) and the kernels.
+#pragma once
+#include <stdint.h>
+
+#define CMGB_MAXC 6
+
+// Per-state descriptor consumed by the kernels (one per state, indexed v).
+struct StateInfo {
+  int8_t  type;      // CMGB_*_st
+  int8_t  kind;      // SK_* below
+  int8_t  cnum;      // children (non-B); 0 for E
+  int8_t  sd;        // StateDelta
+  int8_t  right;     // reads children at row r-1 (MP, MR, IR)
+  int8_t  emit;      // 0 none, 1 left, 2 right, 3 pair
+  int8_t  has_begin; // local begin into this state
+  int8_t  has_end;   // local end (init_sc not IMPOSSIBLE)
+  int8_t  has_iend;  // integer version of has_end
+  int8_t  pad_[7];
+  int     lo, hi;    // padded d range of the buffer
+  int     dn, dxW;   // own band for j >= W (dx shrinks to jp for small jp)
+  int     buf;       // shared-memory element offset of row 0 (E: constant row)
+  int     stride;    // elements per row (0 for E: every row is the d=0 init row)
+  int     carry;     // element offset of [lo,hi] in the per-CTA carry arrays (-1: none)
+  int     ring;      // BEGL_S: element offset of its history ring in the per-CTA ring area
+  int     child[CMGB_MAXC];  // child state indices (non-B); B: child[0] = BEGL, child[1] = BEGR
+  int     cbuf[CMGB_MAXC];   // child's buf, stride and lo (copied so a phase needs no pointer chase)
+  int     cstr[CMGB_MAXC];
+  int     clo[CMGB_MAXC];
+  float   tsc[CMGB_MAXC];
+  int     itsc[CMGB_MAXC];
+  float   beginsc, endsc, init0;   // init0: value of the d = 0 cell
+  int     ibeginsc, iendsc, iinit0;
+  int     oesc_off;  // element offset of this state's emission row in the oesc/ioesc tables
+  // B states: k range terms (src/cm_dpsearch.c:258-269)
+  int     dn_y, dx_y, dn_w, dx_w, banded;
+};
+
+enum {
+  SK_E = 0,      // end state: constant row, never computed
+  SK_GEN = 1,    // generic: all cells independent
+  SK_IL = 2,     // insert-left: self-loop on the current row (serial in d)
+  SK_IR = 3,     // insert-right: self-loop on the previous row (serial along diagonals)
+  SK_B = 4,      // bifurcation
+  SK_BEGL = 5,   // BEGL_S: written to the global history ring
+  SK_ROOT = 6    // state 0
+};
+
+// Whole-plan parameters (device copy lives in global memory).
+struct ScanPlan {
+  int M, W, T;            // states, model W, tile rows
+  int Kp;
+  int nthreads;
+  int smem_elems;         // tile-buffer arena size (elements of 4 bytes)
+  int const_row;          // element offset of the shared constant E row
+  int const_row_len;      // W + 2
+  int acc_off;            // element offset of the root accumulator [T][W+1]
+  int bestr_off;          // element offset of the bestr array [T][W+1] (ints)
+  int res_off;            // element offset of the staged residues (bytes packed)
+  int res_len;            // number of staged residues per tile (W + T + 2)
+  int smem_bytes;         // total dynamic shared memory
+  int carry_elems;        // per-CTA carry size (one parity)
+  int ring_elems;         // per-CTA BEGL ring size
+  int ring_rows;          // R
+  int root_dn, root_dxW;
+  float el_selfsc;
+  int iel_selfsc;
+  int local_begin;
+};
+
+#ifndef CMGB_NO_HOST_PLAN
+#include <string>
+#include <vector>
+#include "../../include/infernal_gb300.h"
+namespace cmgb {
+struct PlanOut {
+  ScanPlan plan;
+  std::vector<StateInfo> states;
+  std::string err;
+};
+// Builds the plan of band set qdbidx with T-row tiles; false + err on failure.
+bool build_plan(const cmgb_model_desc *m, int qdbidx, int T, int nthreads, PlanOut *out);
+}  // namespace cmgb
+#endif

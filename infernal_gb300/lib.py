@@ -1,0 +1,192 @@
+"""ctypes bindings of the C ABI in include/infernal_gb300.h.
+
+This is the Python mirror of the reference scanner interface
+(``FastCYKScan``/``FastIInsideScan``, src/cm_dpsearch.c:90 and :1106): the
+same argument meaning and the same error behaviour (a non-zero Easel status
+code is raised as :class:`ScanError` carrying the errbuf text).
+
+The shared library is the in-tree build ``infernal_gb300/_lib/libinfernal_gb300.so``
+(``python -c "import __graft_entry__ as g; g.build()"``).  There is no CPU
+fallback: if the library or a GPU is missing, :func:`load` raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+from typing import List, Optional
+
+import numpy as np
+
+from . import cmfile
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libinfernal_gb300.so")
+
+P, I, I64, F = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_float
+CMGB_NOTGREEDY = 1 << 2
+
+# every symbol the header declares (checked by the CPU tests)
+EXPORTS = [
+    "cmgb_logsum_init", "cmgb_ctx_create", "cmgb_ctx_destroy", "cmgb_ctx_set_shape",
+    "cmgb_ctx_last_kernel_ms", "cmgb_ctx_last_launches", "cmgb_model_create", "cmgb_model_destroy",
+    "cmgb_hitlist_create", "cmgb_hitlist_destroy", "cmgb_hitlist_count", "cmgb_hitlist_get",
+    "cmgb_hitlist_clear", "cmgb_FastCYKScan", "cmgb_FastIInsideScan", "cmgb_FastCYKScan_dev",
+    "cmgb_FastIInsideScan_dev", "cmgb_count_cells",
+]
+
+_SCAN_ARGS = [P, P, ctypes.c_char_p, I, P, I64, I64, F, P, I, F, P, P, P, P]
+
+
+class Hit(ctypes.Structure):
+    _fields_ = [("start", I64), ("stop", I64), ("root", I), ("mode", I), ("score", F)]
+
+
+class ScanError(RuntimeError):
+    """A scanner returned a non-zero status; .status is the Easel code."""
+
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"status {status}: {msg}")
+        self.status = status
+
+
+_libs = {}
+
+
+def bind(path: str) -> ctypes.CDLL:
+    """Loads a library exporting the C ABI and declares its prototypes."""
+    if path in _libs:
+        return _libs[path]
+    lib = ctypes.CDLL(path)
+    lib.cmgb_logsum_init.argtypes = []
+    lib.cmgb_ctx_create.argtypes = [I, ctypes.POINTER(P), ctypes.c_char_p]
+    lib.cmgb_ctx_create.restype = I
+    lib.cmgb_ctx_destroy.argtypes = [P]
+    lib.cmgb_ctx_set_shape.argtypes = [P, I, I, I]
+    lib.cmgb_ctx_set_shape.restype = I
+    lib.cmgb_ctx_last_kernel_ms.argtypes = [P]
+    lib.cmgb_ctx_last_kernel_ms.restype = F
+    lib.cmgb_ctx_last_launches.argtypes = [P]
+    lib.cmgb_ctx_last_launches.restype = I
+    lib.cmgb_model_create.argtypes = [P, P, ctypes.POINTER(P), ctypes.c_char_p]
+    lib.cmgb_model_create.restype = I
+    lib.cmgb_model_destroy.argtypes = [P]
+    lib.cmgb_hitlist_create.argtypes = []
+    lib.cmgb_hitlist_create.restype = P
+    lib.cmgb_hitlist_destroy.argtypes = [P]
+    lib.cmgb_hitlist_count.argtypes = [P]
+    lib.cmgb_hitlist_count.restype = I64
+    lib.cmgb_hitlist_get.argtypes = [P, I64, ctypes.POINTER(Hit)]
+    lib.cmgb_hitlist_get.restype = I
+    lib.cmgb_hitlist_clear.argtypes = [P]
+    for name in ("cmgb_FastCYKScan", "cmgb_FastIInsideScan", "cmgb_FastCYKScan_dev", "cmgb_FastIInsideScan_dev"):
+        f = getattr(lib, name)
+        f.argtypes = _SCAN_ARGS
+        f.restype = I
+    lib.cmgb_count_cells.argtypes = [P, I, I64]
+    lib.cmgb_count_cells.restype = I64
+    lib.cmgb_logsum_init()
+    _libs[path] = lib
+    return lib
+
+
+def load(path: Optional[str] = None) -> ctypes.CDLL:
+    """Loads the built GPU library; raises if it has not been built."""
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with __graft_entry__.build()")
+    return bind(path)
+
+
+@dataclass
+class ScanResult:
+    hits: List[tuple]          # (start, stop, root, mode, score)
+    envi: int
+    envj: int
+    sc: float
+    vsc: Optional[np.ndarray]
+    kernel_ms: float
+
+
+class Scanner:
+    """One device context (the GB300 analogue of a worker's CM_SCAN_MX)."""
+
+    def __init__(self, device: int = 0, lib: Optional[ctypes.CDLL] = None):
+        self.lib = lib or load()
+        self._ctx = P()
+        err = ctypes.create_string_buffer(256)
+        st = self.lib.cmgb_ctx_create(device, ctypes.byref(self._ctx), err)
+        if st != 0:
+            raise ScanError(st, err.value.decode())
+        self._models = {}
+
+    def close(self):
+        for mh, _ in self._models.values():
+            self.lib.cmgb_model_destroy(mh)
+        self._models = {}
+        if self._ctx:
+            self.lib.cmgb_ctx_destroy(self._ctx)
+            self._ctx = P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_shape(self, tile_rows: int = 0, window_len: int = 0, ctas_per_sm: int = 0):
+        st = self.lib.cmgb_ctx_set_shape(self._ctx, tile_rows, window_len, ctas_per_sm)
+        if st != 0:
+            raise ScanError(st, "invalid launch shape")
+
+    def model(self, m: cmfile.CMModel, flags_extra: int = 0):
+        key = (id(m), flags_extra)
+        if key not in self._models:
+            keep: list = []
+            desc = cmfile.make_desc(m, flags_extra=flags_extra, keep=keep)
+            h = P()
+            err = ctypes.create_string_buffer(256)
+            st = self.lib.cmgb_model_create(self._ctx, ctypes.byref(desc), ctypes.byref(h), err)
+            if st != 0:
+                raise ScanError(st, err.value.decode())
+            self._models[key] = (h, (desc, keep, m))
+        return self._models[key][0]
+
+    def scan(self, m: cmfile.CMModel, dsq, i0: int, j0: int, algo: str = "cyk", qdbidx: int = 1,
+             cutoff: float = 0.0, do_null3: bool = True, env_cutoff: float = 0.0, want_hits: bool = True,
+             want_vsc: bool = False, notgreedy: bool = False, device_ptr: Optional[int] = None) -> ScanResult:
+        """Runs cmgb_FastCYKScan (algo="cyk") or cmgb_FastIInsideScan (algo="inside").
+        dsq: numpy uint8 Easel digital sequence (dsq[0], dsq[L+1] sentinels);
+        device_ptr: optional device address of the same array (the *_dev entry points)."""
+        mh = self.model(m, CMGB_NOTGREEDY if notgreedy else 0)
+        fn = {"cyk": "cmgb_FastCYKScan", "inside": "cmgb_FastIInsideScan"}[algo]
+        if device_ptr is not None:
+            fn += "_dev"
+            dptr = device_ptr
+        else:
+            dsq = np.ascontiguousarray(dsq, dtype=np.uint8)
+            dptr = dsq.ctypes.data
+        hl = self.lib.cmgb_hitlist_create() if want_hits else None
+        envi, envj, sc = I64(), I64(), F()
+        vsc = np.zeros(m.M, np.float32) if want_vsc else None
+        err = ctypes.create_string_buffer(256)
+        try:
+            st = getattr(self.lib, fn)(self._ctx, mh, err, qdbidx, dptr, i0, j0, cutoff, hl,
+                                       int(do_null3), env_cutoff, ctypes.byref(envi), ctypes.byref(envj),
+                                       vsc.ctypes.data if vsc is not None else None, ctypes.byref(sc))
+            if st != 0:
+                raise ScanError(st, err.value.decode())
+            hits = []
+            if hl:
+                h = Hit()
+                for k in range(self.lib.cmgb_hitlist_count(hl)):
+                    self.lib.cmgb_hitlist_get(hl, k, ctypes.byref(h))
+                    hits.append((h.start, h.stop, h.root, h.mode, h.score))
+        finally:
+            if hl:
+                self.lib.cmgb_hitlist_destroy(hl)
+        return ScanResult(hits, envi.value, envj.value, sc.value, vsc,
+                          float(self.lib.cmgb_ctx_last_kernel_ms(self._ctx)))
+
+    def last_launches(self) -> int:
+        return int(self.lib.cmgb_ctx_last_launches(self._ctx))

@@ -1,0 +1,102 @@
+"""Parity oracle for the GB300 scanners -- TEST INFRASTRUCTURE ONLY.
+
+Two checkers live here:
+  * the CPU restatement ``cm_scan_oracle.c`` (built on any machine into
+    ``oracle/_build/liboracle.so``), and
+  * the reference's own scanner sources compiled from the reference tree
+    (``oracle/_ref/libinfernal_ref.so``, built by ``build_ref.sh`` where the
+    reference tree exists), used to pin the restatement through golden vectors.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this package; the product (infernal_gb300/) never does.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+ORACLE_SO = os.path.join(BUILD, "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libinfernal_ref.so")
+
+P, I, I64, F = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_float
+ALGOS = {"cyk": 0, "inside": 1, "finside": 2}
+REF_ALGOS = {"cyk": 0, "refcyk": 1, "inside": 2, "refinside": 3, "finside": 4, "reffinside": 5,
+             "trcyk": 6, "trinside": 7}
+
+
+def build_oracle(force: bool = False) -> str:
+    """Compiles the C restatement (gcc, no FMA contraction so that every float
+    operation rounds as in the reference's C source)."""
+    src = os.path.join(HERE, "cm_scan_oracle.c")
+    if force or not os.path.exists(ORACLE_SO) or os.path.getmtime(ORACLE_SO) < os.path.getmtime(src):
+        os.makedirs(BUILD, exist_ok=True)
+        tmp = ORACLE_SO + f".tmp{os.getpid()}"
+        subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-o", tmp, src, "-lm"])
+        os.replace(tmp, ORACLE_SO)
+    return ORACLE_SO
+
+
+def build_ref(ref_root: str = "/root/reference") -> Optional[str]:
+    """Builds oracle/_ref from the reference tree when it exists here."""
+    if not os.path.isdir(os.path.join(ref_root, "src")):
+        return None
+    subprocess.check_call([os.path.join(HERE, "build_ref.sh"), ref_root], stdout=subprocess.DEVNULL)
+    return REF_SO
+
+
+class _Hit(ctypes.Structure):
+    _fields_ = [("start", I64), ("stop", I64), ("root", I), ("mode", I), ("score", F)]
+
+
+_lib = {}
+
+
+def _load(path):
+    if path not in _lib:
+        lib = ctypes.CDLL(path)
+        if hasattr(lib, "oracle_scan"):
+            lib.oracle_scan.argtypes = [P, I, I, P, I64, I64, F, I, F, I, P, I64, P, P, P, P, P, P]
+            lib.oracle_scan.restype = I
+        if hasattr(lib, "refh_scan"):
+            lib.refh_scan.argtypes = [P, I, I, I, P, I64, I64, F, I, F, I, I, P, I64, P, P, P, P, P, P, P]
+            lib.refh_scan.restype = I
+        _lib[path] = lib
+    return _lib[path]
+
+
+def scan(m, dsq, i0, j0, algo="cyk", qdbidx=1, cutoff=0.0, do_null3=True, env_cutoff=0.0,
+         want_hits=True, notgreedy=False, reference=False, pass_idx=0, max_hits=200000):
+    """Runs the restatement (reference=False) or the reference's own scanner
+    (reference=True) and returns (hits, envi, envj, sc, vsc)."""
+    from infernal_gb300 import cmfile
+    keep: list = []
+    desc = cmfile.make_desc(m, flags_extra=(4 if notgreedy else 0), keep=keep)
+    if getattr(m, "_tr", None) is not None:
+        m._tr.fill(desc, keep)
+    dsq = np.ascontiguousarray(dsq, dtype=np.uint8)
+    hits = (_Hit * max_hits)()
+    nh, ei, ej, sc, mode = I64(), I64(), I64(), F(), I()
+    vsc = np.zeros(m.M, np.float32)
+    err = ctypes.create_string_buffer(256)
+    if reference:
+        lib = _load(REF_SO)
+        st = lib.refh_scan(ctypes.byref(desc), m.nodes, REF_ALGOS[algo], qdbidx, dsq.ctypes.data, i0, j0,
+                           cutoff, int(do_null3), env_cutoff, pass_idx, int(want_hits), ctypes.cast(hits, P),
+                           max_hits, ctypes.byref(nh), ctypes.byref(ei), ctypes.byref(ej), vsc.ctypes.data,
+                           ctypes.byref(sc), ctypes.byref(mode), err)
+    else:
+        lib = _load(build_oracle())
+        st = lib.oracle_scan(ctypes.byref(desc), ALGOS[algo], qdbidx, dsq.ctypes.data, i0, j0, cutoff,
+                             int(do_null3), env_cutoff, int(want_hits), ctypes.cast(hits, P), max_hits,
+                             ctypes.byref(nh), ctypes.byref(ei), ctypes.byref(ej), vsc.ctypes.data,
+                             ctypes.byref(sc), err)
+    if st != 0:
+        raise RuntimeError(f"oracle status {st}: {err.value.decode()}")
+    H = [(hits[k].start, hits[k].stop, hits[k].root, hits[k].mode, hits[k].score) for k in range(min(nh.value, max_hits))]
+    return H, ei.value, ej.value, sc.value, vsc

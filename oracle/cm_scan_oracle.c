@@ -144,7 +144,107 @@ static void remove_overlaps(hitvec *in, hitvec *out)
 }
 
 /* ---------------- the standard scanners ---------------- */
-typedef union { float f; int i; } cell;
+/* Per-scan state shared by the three typed DP cores below. */
+typedef struct {
+  const cmgb_model_desc *m;
+  const uint8_t *dsq;
+  int64_t i0, j0, L;
+  int M, Wm, W, WP, Kp, K, nbegl;
+  const int *dmin, *dmax;
+  int *dn, *dxW, *beglidx;
+  float cutoff, env_cutoff;
+  int want_hits, gamma_mode;
+  double (*act)[8];
+  float *vsc, vsc_root;
+  float *bestf; int *bestr;
+  float *gmx; int64_t *gback; float *gsave; int *gr;
+  hitvec tmp, fin;
+  int64_t envi, envj;
+} scanctx;
+
+/* per-j hit bookkeeping: ReportHitsGreedily (src/cm_mx.c:7547) or
+ * UpdateGammaHitMx (src/cm_mx.c:7440) */
+static void report_j(scanctx *c, int64_t j, int64_t jp, int dn0, int dx0)
+{
+  const int W = c->W;
+  if (!c->want_hits) return;
+  if (c->gamma_mode) {
+    c->gmx[jp] = c->gmx[jp - 1]; c->gback[jp] = -1; c->gsave[jp] = IMP; c->gr[jp] = -1;
+    for (int d = MAXF(1, dn0); d <= dx0; d++) {
+      int64_t ip = jp - d + 1;
+      float hs = c->bestf[d], cum = c->gmx[ip - 1] + hs;
+      if (cum > c->gmx[jp] && NOT_IMP(hs)) {
+        int rep = 1;
+        if (c->act) {
+          float c3 = null3_correction(c->m, c->act[jp % (W + 1)], c->act[(ip - 1) % (W + 1)], d);
+          hs -= c3; cum -= c3; rep = cum > c->gmx[jp];
+        }
+        if (rep) { c->gmx[jp] = cum; c->gback[jp] = j - d + 1; c->gsave[jp] = hs; c->gr[jp] = c->bestr[d]; }
+      }
+    }
+  } else {
+    float best = IMP;
+    for (int d = MAXF(1, dn0); d <= dx0; d++) {
+      float hs = c->bestf[d];
+      if (hs > best && hs >= c->cutoff && NOT_IMP(hs)) {
+        int rep = 1;
+        if (c->act) {
+          int64_t ip = jp - d + 1;
+          hs -= null3_correction(c->m, c->act[jp % (W + 1)], c->act[(ip - 1) % (W + 1)], d);
+          rep = (hs > best && hs >= c->cutoff);
+        }
+        if (rep) { hv_push(&c->tmp, j - d + 1, j, c->bestr[d], CMGB_TRMODE_J, hs); best = hs; }
+      }
+    }
+  }
+}
+
+/* The typed DP core is written once in cm_scan_oracle_core.h and instantiated
+ * for CYK (float max), integer Inside (ILogsum) and float Inside (FLogsum). */
+#define CORE_NAME core_cyk
+#define SCT float
+#define IMPV IMP
+#define COMB(a, b) MAXF((a), (b))
+#define ROOTFIRST(x) MAXF(IMP, (x))
+#define SCOREF(x) (x)
+#define ENVF(x) (x)
+#define TSC(v, o) m->tsc[(v) * MAXC + (o)]
+#define ESC(v) (m->oesc + (size_t) (v) * Kp * Kp)
+#define BEGINSC(y) m->beginsc[y]
+#define HAS_BEGIN(y) NOT_IMP(m->beginsc[y])
+#define ENDSC(v) m->endsc[v]
+#define INIT_SC(v, d) (NOT_IMP(m->endsc[v]) ? (float) (m->el_selfsc * (d)) + m->endsc[v] : IMP)
+#include "cm_scan_oracle_core.h"
+
+#define CORE_NAME core_finside
+#define SCT float
+#define IMPV IMP
+#define COMB(a, b) flogsum((a), (b))
+#define ROOTFIRST(x) MAXF(IMP, (x))
+#define SCOREF(x) (x)
+#define ENVF(x) (x)
+#define TSC(v, o) m->tsc[(v) * MAXC + (o)]
+#define ESC(v) (m->oesc + (size_t) (v) * Kp * Kp)
+#define BEGINSC(y) m->beginsc[y]
+#define HAS_BEGIN(y) NOT_IMP(m->beginsc[y])
+#define ENDSC(v) m->endsc[v]
+#define INIT_SC(v, d) (NOT_IMP(m->endsc[v]) ? (float) (m->el_selfsc * (d)) + m->endsc[v] : IMP)
+#include "cm_scan_oracle_core.h"
+
+#define CORE_NAME core_iinside
+#define SCT int
+#define IMPV (-INFTY)
+#define COMB(a, b) ilogsum((a), (b))
+#define ROOTFIRST(x) (((x) > -INFTY) ? (x) : -INFTY)
+#define SCOREF(x) scorify(x)
+#define ENVF(x) ((float) (x))
+#define TSC(v, o) m->itsc[(v) * MAXC + (o)]
+#define ESC(v) (m->ioesc + (size_t) (v) * Kp * Kp)
+#define BEGINSC(y) m->ibeginsc[y]
+#define HAS_BEGIN(y) (m->ibeginsc[y] != -INFTY)
+#define ENDSC(v) m->iendsc[v]
+#define INIT_SC(v, d) ((m->iendsc[v] != -INFTY) ? m->iel_selfsc * (d) + m->iendsc[v] : -INFTY)
+#include "cm_scan_oracle_core.h"
 
 /* One scan of dsq[i0..j0].  algo: ORC_CYK (FastCYKScan), ORC_IINS
  * (FastIInsideScan) or ORC_FINS (FastFInsideScan).  Hits go to hits_out
@@ -159,253 +259,73 @@ int oracle_scan(const cmgb_model_desc *m, int algo, int qdbidx,
   init_tables();
   if (j0 < i0) { if (errbuf) snprintf(errbuf, CMGB_ERRBUFSIZE, "oracle: j0 < i0"); return CMGB_EINCOMPAT; }
   if (dsq == NULL) { if (errbuf) snprintf(errbuf, CMGB_ERRBUFSIZE, "oracle: dsq is NULL"); return CMGB_EINCOMPAT; }
-  const int M = m->M, Wm = m->W, Kp = m->Kp, K = m->K;
-  const int isint = (algo == ORC_IINS);
-  const int64_t L = j0 - i0 + 1;
-  const int W = (int) (Wm > L ? L : Wm);     /* local W (src/cm_dpsearch.c:157-158) */
-  const int *dmin = NULL, *dmax = NULL;
-  if (qdbidx == CMGB_QDB1_TIGHT) { dmin = m->dmin1; dmax = m->dmax1; }
-  else if (qdbidx == CMGB_QDB2_LOOSE) { dmin = m->dmin2; dmax = m->dmax2; }
+  scanctx c;
+  memset(&c, 0, sizeof(c));
+  c.m = m; c.dsq = dsq; c.i0 = i0; c.j0 = j0; c.L = j0 - i0 + 1;
+  c.M = m->M; c.Wm = m->W; c.Kp = m->Kp; c.K = m->K;
+  c.W = (int) (c.Wm > c.L ? c.L : c.Wm);     /* local W (src/cm_dpsearch.c:157-158) */
+  c.WP = c.Wm + 1;
+  if (qdbidx == CMGB_QDB1_TIGHT) { c.dmin = m->dmin1; c.dmax = m->dmax1; }
+  else if (qdbidx == CMGB_QDB2_LOOSE) { c.dmin = m->dmin2; c.dmax = m->dmax2; }
   else if (qdbidx != CMGB_NOQDB) { if (errbuf) snprintf(errbuf, CMGB_ERRBUFSIZE, "oracle: bad qdbidx"); return CMGB_EINCOMPAT; }
-
+  for (int v = 0; v < m->M; v++)
+    if (m->sttype[v] != CMGB_E_st && m->sttype[v] != CMGB_B_st && v > 0 && m->stid[v] != CMGB_BEGL_S && (m->cnum[v] < 2 || m->cnum[v] > 6)) {
+      if (errbuf) snprintf(errbuf, CMGB_ERRBUFSIZE, "oracle: state %d has %d children", v, m->cnum[v]);
+      return CMGB_EINCOMPAT;
+    }
   /* bands (src/cm_mx.c:5725-5738) */
-  int *dn = malloc(sizeof(int) * M), *dxW = malloc(sizeof(int) * M);
-  for (int v = 0; v < M; v++) {
+  c.dn = malloc(sizeof(int) * c.M); c.dxW = malloc(sizeof(int) * c.M);
+  for (int v = 0; v < c.M; v++) {
     int lo = m->sttype[v] == CMGB_MP_st ? 2 : 1;
-    if (dmin) lo = MAXF(dmin[v], lo);
-    dn[v]  = MINF(lo, Wm);
-    dxW[v] = dmax ? MINF(dmax[v], Wm) : Wm;
+    if (c.dmin) lo = MAXF(c.dmin[v], lo);
+    c.dn[v]  = MINF(lo, c.Wm);
+    c.dxW[v] = c.dmax ? MINF(c.dmax[v], c.Wm) : c.Wm;
   }
-  /* matrices: alpha[2][M][W+1], begl[W+1][M][W+1] (only BEGL rows used) */
-  const int WP = Wm + 1;
-  cell *alpha = malloc(sizeof(cell) * 2 * (size_t) M * WP);
-  int nbegl = 0;
-  int *beglidx = malloc(sizeof(int) * M);
-  for (int v = 0; v < M; v++) beglidx[v] = (m->stid[v] == CMGB_BEGL_S) ? nbegl++ : -1;
-  cell *begl = malloc(sizeof(cell) * (size_t) (W + 1) * (nbegl ? nbegl : 1) * WP);
-  cell impv; if (isint) impv.i = -INFTY; else impv.f = IMP;
-  for (size_t k = 0; k < 2 * (size_t) M * WP; k++) alpha[k] = impv;
-  for (size_t k = 0; k < (size_t) (W + 1) * (nbegl ? nbegl : 1) * WP; k++) begl[k] = impv;
-#define A(r, v, d)  alpha[((size_t) (r) * M + (v)) * WP + (d)]
-#define BG(r, b, d) begl[((size_t) (r) * (nbegl ? nbegl : 1) + (b)) * WP + (d)]
-  /* d = 0 initialisation (src/cm_mx.c:6039-6138) */
-  for (int v = M - 1; v >= 0; v--) {
-    int t = m->sttype[v], y = m->cfirst[v];
-    cell c = impv;
-    if (m->stid[v] == CMGB_BEGL_S || t == CMGB_S_st || t == CMGB_D_st) {
-      if (isint) {
-        int s = m->iendsc[v];
-        for (int o = 0; o < m->cnum[v]; o++) { int cand = A(0, y + o, 0).i + m->itsc[v * MAXC + o]; s = s > cand ? s : cand; }
-        c.i = s > -INFTY ? s : -INFTY;
-      } else {
-        float s = m->endsc[v];
-        for (int o = 0; o < m->cnum[v]; o++) s = MAXF(s, A(0, y + o, 0).f + m->tsc[v * MAXC + o]);
-        c.f = MAXF(s, IMP);
-      }
-    } else if (t == CMGB_E_st) {
-      if (isint) c.i = 0; else c.f = 0.f;
-    } else if (t == CMGB_B_st) {
-      int w = m->cfirst[v], yy = m->cnum[v];
-      if (isint) c.i = BG(0, beglidx[w], 0).i + A(0, yy, 0).i;
-      else       c.f = BG(0, beglidx[w], 0).f + A(0, yy, 0).f;
-    }
-    if (m->stid[v] == CMGB_BEGL_S) { for (int r = 0; r <= W; r++) BG(r, beglidx[v], 0) = c; }
-    else { A(0, v, 0) = c; A(1, v, 0) = c; }
+  c.beglidx = malloc(sizeof(int) * c.M);
+  for (int v = 0; v < c.M; v++) c.beglidx[v] = (m->stid[v] == CMGB_BEGL_S) ? c.nbegl++ : -1;
+  c.cutoff = cutoff; c.env_cutoff = env_cutoff; c.want_hits = want_hits;
+  c.vsc = malloc(sizeof(float) * c.M);
+  for (int v = 0; v < c.M; v++) c.vsc[v] = IMP;
+  c.vsc_root = IMP;
+  c.bestf = malloc(sizeof(float) * c.WP); c.bestr = malloc(sizeof(int) * c.WP);
+  c.act = do_null3 ? calloc((size_t) c.W + 1, sizeof(double[8])) : NULL;
+  c.gamma_mode = want_hits && (m->flags & CMGB_NOTGREEDY);
+  if (c.gamma_mode) {
+    c.gmx = malloc(sizeof(float) * (c.L + 1)); c.gback = malloc(sizeof(int64_t) * (c.L + 1));
+    c.gsave = malloc(sizeof(float) * (c.L + 1)); c.gr = malloc(sizeof(int) * (c.L + 1));
+    c.gmx[0] = 0.f; c.gback[0] = -1;
   }
-  /* init scores (src/cm.c:4100-4185) */
-  cell *init = malloc(sizeof(cell) * (size_t) M * WP);
-  for (int v = 0; v < M; v++)
-    for (int d = 0; d <= Wm; d++) {
-      if (isint) init[(size_t) v * WP + d].i = (m->iendsc[v] != -INFTY) ? m->iel_selfsc * d + m->iendsc[v] : -INFTY;
-      else { float el = m->el_selfsc * d; init[(size_t) v * WP + d].f = NOT_IMP(m->endsc[v]) ? el + m->endsc[v] : IMP; }
-    }
-#define INIT(v, d) init[(size_t) (v) * WP + (d)]
+  c.envi = j0 + 1; c.envj = i0 - 1;
 
-  float *vsc = malloc(sizeof(float) * M);
-  for (int v = 0; v < M; v++) vsc[v] = IMP;
-  float vsc_root = IMP;
-  cell *bestsc = malloc(sizeof(cell) * WP);
-  int *bestr = malloc(sizeof(int) * WP);
-  float *bestf = malloc(sizeof(float) * WP);
-  double (*act)[8] = do_null3 ? calloc((size_t) W + 1, sizeof(double[8])) : NULL;
-  int gamma_mode = want_hits && (m->flags & CMGB_NOTGREEDY);
-  float *gmx = NULL; int64_t *gback = NULL; float *gsave = NULL; int *gr = NULL;
-  if (gamma_mode) {
-    gmx = malloc(sizeof(float) * (L + 1)); gback = malloc(sizeof(int64_t) * (L + 1));
-    gsave = malloc(sizeof(float) * (L + 1)); gr = malloc(sizeof(int) * (L + 1));
-    gmx[0] = 0.f; gback[0] = -1;
-  }
-  hitvec tmp = {0}, fin = {0};
-  int64_t envi = j0 + 1, envj = i0 - 1;
+  if (algo == ORC_IINS) core_iinside(&c);
+  else if (algo == ORC_FINS) core_finside(&c);
+  else core_cyk(&c);
 
-  for (int64_t j = i0; j <= j0; j++) {
-    const int64_t jp = j - i0 + 1;
-    const int cur = (int) (j % 2), prv = (int) ((j - 1) % 2);
-    const int jrow = (int) (j % (W + 1));
-    int jr = jp >= W ? W : (int) jp;  /* band row */
-    if (act) {
-      memcpy(act[jp % (W + 1)], act[(jp - 1) % (W + 1)], sizeof(double[8]));
-      count_residue(act[jp % (W + 1)], dsq[j], K);
-    }
-    for (int v = M - 1; v > 0; v--) {
-      const int t = m->sttype[v];
-      if (t == CMGB_E_st) continue;
-      const int sd = st_delta(t), cnum = m->cnum[v], y0 = m->cfirst[v];
-      const int dnv = dn[v], dxv = MINF(jr, dxW[v]);
-      const int jpy = st_right(t) ? prv : cur;
-      const int isbegl = (m->stid[v] == CMGB_BEGL_S);
-      const float *tsc = m->tsc + v * MAXC; const int *itsc = m->itsc + v * MAXC;
-      const float *esc = m->oesc + (size_t) v * Kp * Kp; const int *iesc = m->ioesc + (size_t) v * Kp * Kp;
-      for (int d = dnv; d <= dxv; d++) {
-        cell sc;
-        const int dp = d - sd;
-        if (t == CMGB_B_st) {
-          int w = m->cfirst[v], yy = m->cnum[v], kmin, kmax;
-          if (dmin) {
-            int dny = MINF(dmin[yy], Wm), dxy = MINF(dmax[yy], Wm), dnw = MINF(dmin[w], Wm), dxw = MINF(dmax[w], Wm);
-            kmin = MAXF(0, MAXF(dny, d - dxw)); kmax = MINF(dxy, d - dnw);
-          } else { kmin = 0; kmax = d; }
-          sc = INIT(v, dp);
-          for (int k = kmin; k <= kmax; k++) {
-            int br = (int) ((j - k) % (W + 1));
-            if (isint) sc.i = ilogsum(sc.i, BG(br, beglidx[w], d - k).i + A(cur, yy, k).i);
-            else if (algo == ORC_FINS) sc.f = flogsum(sc.f, BG(br, beglidx[w], d - k).f + A(cur, yy, k).f);
-            else sc.f = MAXF(sc.f, BG(br, beglidx[w], d - k).f + A(cur, yy, k).f);
-          }
-        } else if (isbegl) {
-          sc = INIT(v, dp);
-          for (int o = 0; o < cnum; o++) {
-            if (isint) sc.i = ilogsum(sc.i, A(jpy, y0 + o, dp).i + itsc[o]);
-            else if (algo == ORC_FINS) sc.f = flogsum(sc.f, A(jpy, y0 + o, dp).f + tsc[o]);
-            else sc.f = MAXF(sc.f, A(jpy, y0 + o, dp).f + tsc[o]);
-          }
-        } else {
-          /* the Fast scanners' fold order per child count (src/cm_dpsearch.c:307-519) */
-          static const int order[7][7] = {
-            {0}, {0}, {1, -1, 0}, {2, 1, -1, 0}, {3, 2, -1, 1, 0}, {4, 3, -1, 1, 2, 0}, {5, -1, 4, 3, 2, 1, 0} };
-          if (cnum < 2 || cnum > 6) { if (errbuf) snprintf(errbuf, CMGB_ERRBUFSIZE, "oracle: state %d has %d children", v, cnum); return CMGB_EINCOMPAT; }
-          const int *ord = order[cnum];
-          for (int q = 0; q <= cnum; q++) {
-            cell term;
-            if (ord[q] < 0) term = INIT(v, dp);
-            else if (isint) term.i = A(jpy, y0 + ord[q], dp).i + itsc[ord[q]];
-            else term.f = A(jpy, y0 + ord[q], dp).f + tsc[ord[q]];
-            if (q == 0) sc = term;
-            else if (isint) sc.i = ilogsum(sc.i, term.i);
-            else if (algo == ORC_FINS) sc.f = flogsum(sc.f, term.f);
-            else sc.f = MAXF(sc.f, term.f);
-          }
-          /* emission */
-          int64_t i = j - d + 1;
-          int e = -1;
-          if (t == CMGB_MP_st) e = dsq[i] * Kp + dsq[j];
-          else if (st_left(t)) e = dsq[i];
-          else if (st_right(t)) e = dsq[j];
-          if (e >= 0) { if (isint) sc.i += iesc[e]; else sc.f += esc[e]; }
-        }
-        if (isbegl) BG(jrow, beglidx[v], d) = sc; else A(cur, v, d) = sc;
-        float sf = isint ? scorify(sc.i) : sc.f;
-        vsc[v] = MAXF(vsc[v], sf);
-      }
-    }
-    /* root and local begins (src/cm_dpsearch.c:562-616) */
-    const int dn0 = dn[0], dx0 = MINF(jr, dxW[0]);
-    for (int d = 0; d <= W; d++) { bestr[d] = -1; bestf[d] = IMP; }
-    for (int d = dn0; d <= dx0; d++) {
-      bestr[d] = 0;
-      int y = m->cfirst[0];
-      cell r;
-      if (isint) {
-        int s = A(cur, y, d).i + m->itsc[0]; r.i = s > -INFTY ? s : -INFTY;
-        for (int o = 1; o < m->cnum[0]; o++) r.i = ilogsum(r.i, A(cur, y + o, d).i + m->itsc[o]);
-      } else {
-        r.f = MAXF(IMP, A(cur, y, d).f + m->tsc[0]);
-        for (int o = 1; o < m->cnum[0]; o++) {
-          if (algo == ORC_FINS) r.f = flogsum(r.f, A(cur, y + o, d).f + m->tsc[o]);
-          else r.f = MAXF(r.f, A(cur, y + o, d).f + m->tsc[o]);
-        }
-      }
-      A(cur, 0, d) = r;
-    }
-    if (m->flags & CMGB_LOCAL_BEGIN) {
-      for (int y = 1; y < M; y++) {
-        int ok = isint ? (m->ibeginsc[y] != -INFTY) : NOT_IMP(m->beginsc[y]);
-        if (!ok) continue;
-        int lo = MAXF(dn0, dn[y]), hi = MINF(dx0, MINF(jr, dxW[y]));
-        for (int d = lo; d <= hi; d++) {
-          cell c = (m->stid[y] == CMGB_BEGL_S) ? BG(jrow, beglidx[y], d) : A(cur, y, d);
-          if (isint) { int s = c.i + m->ibeginsc[y]; if (A(cur, 0, d).i < s) { A(cur, 0, d).i = s; bestr[d] = y; } }
-          else { float s = c.f + m->beginsc[y]; if (A(cur, 0, d).f < s) { A(cur, 0, d).f = s; bestr[d] = y; } }
-        }
-      }
-    }
-    for (int d = dn0; d <= dx0; d++) {
-      bestf[d] = isint ? scorify(A(cur, 0, d).i) : A(cur, 0, d).f;
-      vsc_root = MAXF(vsc_root, bestf[d]);
-      float envsc = isint ? (float) A(cur, 0, d).i : A(cur, 0, d).f;
-      if (envsc >= env_cutoff) { if (j - d + 1 < envi) envi = j - d + 1; if (j > envj) envj = j; }
-    }
-    if (!want_hits || dn0 > dx0) { if (gamma_mode) { gmx[jp] = gmx[jp - 1]; gback[jp] = -1; } continue; }
-    if (gamma_mode) {
-      /* UpdateGammaHitMx (src/cm_mx.c:7440-7520) */
-      gmx[jp] = gmx[jp - 1]; gback[jp] = -1; gsave[jp] = IMP; gr[jp] = -1;
-      for (int d = MAXF(1, dn0); d <= dx0; d++) {
-        int64_t ip = jp - d + 1;
-        float hs = bestf[d], cum = gmx[ip - 1] + hs;
-        if (cum > gmx[jp] && NOT_IMP(hs)) {
-          int rep = 1;
-          if (act) {
-            float c3 = null3_correction(m, act[jp % (W + 1)], act[(ip - 1) % (W + 1)], d);
-            hs -= c3; cum -= c3; rep = cum > gmx[jp];
-          }
-          if (rep) { gmx[jp] = cum; gback[jp] = j - d + 1; gsave[jp] = hs; gr[jp] = bestr[d]; }
-        }
-      }
-    } else {
-      /* ReportHitsGreedily (src/cm_mx.c:7547-7628) */
-      float best = IMP;
-      for (int d = MAXF(1, dn0); d <= dx0; d++) {
-        float hs = bestf[d];
-        if (hs > best && hs >= cutoff && NOT_IMP(hs)) {
-          int rep = 1;
-          if (act) {
-            int64_t ip = jp - d + 1;
-            hs -= null3_correction(m, act[jp % (W + 1)], act[(ip - 1) % (W + 1)], d);
-            rep = (hs > best && hs >= cutoff);
-          }
-          if (rep) { hv_push(&tmp, j - d + 1, j, bestr[d], CMGB_TRMODE_J, hs); best = hs; }
-        }
-      }
-    }
-  }
-  vsc[0] = vsc_root;
+  c.vsc[0] = c.vsc_root;
   if (want_hits) {
-    if (gamma_mode) {
+    if (c.gamma_mode) {
       /* TBackGammaHitMx (src/cm_mx.c:7640-7669) */
       int64_t j = j0;
       while (j >= i0) {
         int64_t jp = j - i0 + 1;
-        if (gback[jp] == -1) j--;
+        if (c.gback[jp] == -1) j--;
         else {
-          if (gsave[jp] >= cutoff) hv_push(&fin, gback[jp], j, gr[jp], CMGB_TRMODE_J, gsave[jp]);
-          j = gback[jp] - 1;
+          if (c.gsave[jp] >= cutoff) hv_push(&c.fin, c.gback[jp], j, c.gr[jp], CMGB_TRMODE_J, c.gsave[jp]);
+          j = c.gback[jp] - 1;
         }
       }
-    } else remove_overlaps(&tmp, &fin);
+    } else remove_overlaps(&c.tmp, &c.fin);
   }
-  *ret_nhits = fin.n;
-  for (int64_t h = 0; h < fin.n && h < max_hits; h++) hits_out[h] = fin.h[h];
-  if (ret_envi) *ret_envi = (envi == j0 + 1) ? -1 : envi;
-  if (ret_envj) *ret_envj = (envj == i0 - 1) ? -1 : envj;
-  if (vsc_out) memcpy(vsc_out, vsc, sizeof(float) * M);
-  if (ret_sc) *ret_sc = vsc_root;
-  free(dn); free(dxW); free(alpha); free(begl); free(beglidx); free(init); free(vsc);
-  free(bestsc); free(bestr); free(bestf); free(act); free(tmp.h); free(fin.h);
-  free(gmx); free(gback); free(gsave); free(gr);
+  *ret_nhits = c.fin.n;
+  for (int64_t h = 0; h < c.fin.n && h < max_hits; h++) hits_out[h] = c.fin.h[h];
+  if (ret_envi) *ret_envi = (c.envi == j0 + 1) ? -1 : c.envi;
+  if (ret_envj) *ret_envj = (c.envj == i0 - 1) ? -1 : c.envj;
+  if (vsc_out) memcpy(vsc_out, c.vsc, sizeof(float) * c.M);
+  if (ret_sc) *ret_sc = c.vsc_root;
+  free(c.dn); free(c.dxW); free(c.beglidx); free(c.vsc);
+  free(c.bestf); free(c.bestr); free(c.act); free(c.tmp.h); free(c.fin.h);
+  free(c.gmx); free(c.gback); free(c.gsave); free(c.gr);
   return CMGB_OK;
-#undef A
-#undef BG
-#undef INIT
 }
 
 /* DP cell count (the algorithmic work unit of the scan). */

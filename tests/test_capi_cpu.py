@@ -1,0 +1,113 @@
+"""CPU tests of the C ABI: the built library exports every declared symbol,
+and the kernel source -- compiled for the test-only host-thread emulation of a
+CTA -- reproduces the oracle bit for bit and keeps the reference's error
+behaviour.  No GPU is used."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+from infernal_gb300 import cmfile, lib as L
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+EMU_SO = os.path.join(ROOT, "tests", "emu", "_build", "libinfernal_gb300_emu.so")
+
+
+def _declared_functions():
+    names = set()
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if fn.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", fn)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names |= set(re.findall(r"\b(cmgb_\w+)\s*\(", src))
+    return names
+
+
+def test_header_and_binding_agree():
+    assert _declared_functions() == set(L.EXPORTS)
+
+
+@pytest.fixture(scope="module")
+def built_lib():
+    import __graft_entry__ as g
+    if not os.path.exists(L.LIB_PATH):
+        g.build_library()
+    return L.LIB_PATH
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    import ctypes
+    lib = ctypes.CDLL(built_lib)      # loading touches no GPU
+    for name in _declared_functions():
+        assert hasattr(lib, name), name
+
+
+def test_count_cells_matches_oracle(built_lib, models):
+    import ctypes
+    lib = L.bind(built_lib)
+    olib = ctypes.CDLL(oracle.build_oracle())
+    olib.oracle_count_cells.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int64]
+    olib.oracle_count_cells.restype = ctypes.c_int64
+    for m in models.values():
+        keep = []
+        d = cmfile.make_desc(m, keep=keep)
+        for q in (0, 1, 2):
+            for Ln in (10, m.W - 1, m.W, 5000):
+                assert lib.cmgb_count_cells(ctypes.byref(d), q, Ln) == olib.oracle_count_cells(ctypes.byref(d), q, Ln)
+
+
+@pytest.fixture(scope="module")
+def emu():
+    os.makedirs(os.path.dirname(EMU_SO), exist_ok=True)
+    csrc = os.path.join(ROOT, "infernal_gb300", "csrc")
+    srcs = [os.path.join(csrc, f) for f in ("capi.cu", "scan_plan.cpp", "hits.cpp")]
+    if not os.path.exists(EMU_SO) or os.path.getmtime(EMU_SO) < max(os.path.getmtime(s) for s in srcs + [os.path.join(csrc, "scan_kernel.cuh")]):
+        subprocess.check_call(["g++", "-std=c++20", "-O2", "-fPIC", "-shared", "-ffp-contract=off",
+                               "-DCMGB_HOST_EMULATION", "-I", os.path.join(ROOT, "tests", "emu"),
+                               "-x", "c++", srcs[0], "-x", "none", srcs[1], srcs[2], "-o", EMU_SO, "-lpthread"])
+    return L.Scanner(lib=L.bind(EMU_SO))
+
+
+@pytest.mark.parametrize("name,algo,qdb,T,win", [
+    ("tRNA", "cyk", 1, 4, 0), ("tRNA", "inside", 2, 8, 0), ("Vault", "cyk", 2, 16, 300),
+    ("tRNA", "cyk", 0, 16, 0), ("Plant_SRP", "inside", 1, 4, 0)])
+def test_emulated_kernel_matches_oracle(emu, models, name, algo, qdb, T, win):
+    m = models[name]
+    rng = np.random.default_rng(11)
+    n = 500 if name == "Plant_SRP" else 700
+    dsq = cmfile.digitize("".join(rng.choice(list("ACGU"), n)))
+    emu.set_shape(T, win, 1)
+    r = emu.scan(m, dsq, 1, n, algo=algo, qdbidx=qdb, cutoff=-2.0, env_cutoff=1.0, want_vsc=True)
+    o = oracle.scan(m, dsq, 1, n, algo=algo, qdbidx=qdb, cutoff=-2.0, env_cutoff=1.0)
+    assert r.hits == o[0]
+    assert (r.envi, r.envj) == (o[1], o[2]) and np.float32(r.sc) == np.float32(o[3])
+    assert np.array_equal(r.vsc.view(np.int32), o[4].view(np.int32))
+
+
+def test_emulated_golden_degenerate_case(emu, models, golden):
+    """A golden case with degenerate residues and NULL3 through the emulated kernel."""
+    from conftest import hits_from_golden
+    meta, arrays = golden
+    c = next(c for c in meta if c["seq"] == "tRNA.degen" and c["algo"] == "inside")
+    emu.set_shape(8, 0, 1)
+    r = emu.scan(models["tRNA"], arrays["dsq." + c["seq"]], c["i0"], c["j0"], algo="inside", qdbidx=c["qdbidx"],
+                 cutoff=c["cutoff"], do_null3=bool(c["null3"]), env_cutoff=c["env_cutoff"])
+    assert r.hits == hits_from_golden(c)
+
+
+def test_contract_errors(emu, models):
+    """eslEINCOMPAT on contract violations, as src/cm_dpsearch.c:129-154."""
+    m = models["tRNA"]
+    dsq = cmfile.digitize("ACGU" * 30)
+    with pytest.raises(L.ScanError) as e:
+        emu.scan(m, dsq, 50, 10)
+    assert e.value.status == 10 and "i0" in str(e.value)
+    with pytest.raises(L.ScanError) as e:
+        emu.scan(m, dsq, 1, 100, qdbidx=3)
+    assert e.value.status == 10
+    with pytest.raises(L.ScanError) as e:
+        emu.set_shape(-1, 0, 0)
+    assert e.value.status == 11
