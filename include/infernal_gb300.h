@@ -140,16 +140,32 @@ void cmgb_logsum_init(void);
  * the per-worker CM_SCAN_MX clone, src/cmsearch.c:2555) ---- */
 int  cmgb_ctx_create(int device, cmgb_ctx **ret_ctx, char *errbuf);
 void cmgb_ctx_destroy(cmgb_ctx *ctx);
-/* Kernel launch shape override (0 keeps the tuned default). */
-int  cmgb_ctx_set_shape(cmgb_ctx *ctx, int tile_rows, int window_len, int ctas_per_sm);
+/* Kernel launch shape override; 0 keeps the default of each field.
+ * tile_rows: end positions per tile (the rolling-row depth, <= 64);
+ * window_len: owned end positions per CTA work item; ctas_per_sm: resident
+ * CTAs per SM (0: as many as fit); threads: threads per CTA (64..512);
+ * arena: where the DP tiles live (0 automatic, 1 shared memory, 2 a per-CTA
+ * global-memory arena served from L1/L2). */
+int  cmgb_ctx_set_shape(cmgb_ctx *ctx, int tile_rows, int window_len, int ctas_per_sm, int threads, int arena);
 /* Device time of the last scan's kernels in milliseconds (CUDA events). */
 float cmgb_ctx_last_kernel_ms(const cmgb_ctx *ctx);
 /* Number of this library's kernels launched by the last scan. */
 int  cmgb_ctx_last_launches(const cmgb_ctx *ctx);
+/* Host->device and device->host bytes the last scan moved. */
+void cmgb_ctx_last_transfer_bytes(const cmgb_ctx *ctx, int64_t *h2d, int64_t *d2h);
 
 /* ---- models: configured CM parameters uploaded to one device ---- */
 int  cmgb_model_create(cmgb_ctx *ctx, const cmgb_model_desc *desc, cmgb_model **ret_model, char *errbuf);
 void cmgb_model_destroy(cmgb_model *model);
+
+/* Autotuner: times candidate shapes (tile rows = rolling-row depth, and
+ * shared- vs global-memory tiles) for band set qdbidx and algo (0 CYK,
+ * 1 integer Inside) on a seeded iid sample of sample_len residues (0: a size
+ * that fills the device) and stores the fastest in the model; scans on a
+ * context whose tile_rows is 0 use it.  Returns the choice when the
+ * pointers are non-NULL. */
+int  cmgb_autotune(cmgb_ctx *ctx, cmgb_model *model, int qdbidx, int algo, int64_t sample_len,
+                   int *ret_tile_rows, int *ret_arena, char *errbuf);
 
 /* ---- hit lists (the CM_TOPHITS subset the scanners append to) ---- */
 cmgb_hitlist *cmgb_hitlist_create(void);

@@ -29,26 +29,39 @@ using namespace cmgb;
 #define CUDA_TRY(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) ERRF(CMGB_ENODEV, "CUDA error %s at %s:%d", cudaGetErrorString(e_), __FILE__, __LINE__); } while (0)
 
 #ifdef CMGB_HOST_EMULATION
-static const int kThreads = CMGB_EMU_THREADS;
-template <bool INS>
+static const int kDefaultThreads = CMGB_EMU_THREADS;
+template <bool INS, bool GL>
 static void launch_qdb(int grid, int nt, size_t smem, cudaStream_t, const KParams &kp)
 {
   std::vector<std::vector<float>> sm(grid, std::vector<float>(smem / 4 + 16));
   std::vector<std::barrier<> *> bars;
+  std::vector<EmuWarp *> warps;
   for (int b = 0; b < grid; b++) bars.push_back(new std::barrier<>(nt));
+  for (int b = 0; b < grid * (nt / 32); b++) warps.push_back(new EmuWarp);
   std::vector<std::thread> th;
   for (int b = 0; b < grid; b++)
     for (int t = 0; t < nt; t++)
-      th.emplace_back([&, b, t] { cmgb_emu_bar = bars[b]; qdb_scan_body<INS>(kp, sm[b].data(), t, nt, b); });
+      th.emplace_back([&, b, t] {
+        cmgb_emu_bar = bars[b]; cmgb_emu_warp = warps[b * (nt / 32) + t / 32]; cmgb_emu_lane = t & 31;
+        qdb_scan_body<INS, GL>(kp, sm[b].data(), t, nt, b);
+      });
   for (auto &x : th) x.join();
   for (auto *b : bars) delete b;
+  for (auto *w : warps) delete w;
 }
 #else
-static const int kThreads = 256;
-template <bool INS>
+static const int kDefaultThreads = 512;
+template <bool INS, bool GL>
 static void launch_qdb(int grid, int nt, size_t smem, cudaStream_t s, const KParams &kp)
 {
-  qdb_scan_kernel<INS><<<grid, nt, smem, s>>>(kp);
+  qdb_scan_kernel<INS, GL><<<grid, nt, smem, s>>>(kp);
+}
+template <bool INS, bool GL>
+static cudaError_t prepare_qdb(int nt, int smem, int *blocks_per_sm)
+{
+  cudaError_t e = cudaFuncSetAttribute(qdb_scan_kernel<INS, GL>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, qdb_scan_kernel<INS, GL>, nt, smem);
 }
 #endif
 static const int kCandCap = 1 << 22;
@@ -67,9 +80,10 @@ struct cmgb_hitlist_s { std::vector<cmgb_hit> h; };
 
 struct DevPlan {
   bool built = false;
-  int T = 0;
+  int T = 0, nt = 0, arena = -1;
   ScanPlan plan;
   StateInfo *d_states = nullptr;
+  unsigned char *d_rec = nullptr;
 };
 
 struct cmgb_model_s {
@@ -80,12 +94,14 @@ struct cmgb_model_s {
   // host copy of the description arrays (the plan builder re-reads them)
   std::vector<int8_t> sttype, stid;
   std::vector<int> cfirst, cnum, dmin1, dmax1, dmin2, dmax2, itsc, iendsc, ibeginsc;
-  std::vector<float> tsc, endsc, beginsc;
+  std::vector<float> tsc, endsc, beginsc, oesc;
+  std::vector<int> ioesc;
   float el_selfsc = 0.f; int iel_selfsc = 0;
   cmgb_model_desc desc;      // points into the vectors above
   float *d_oesc = nullptr;
   int *d_ioesc = nullptr;
-  DevPlan plans[3][2];       // [qdbidx][0: T as requested]
+  DevPlan plans[3][2];       // [qdbidx][0: CYK, 1: integer Inside]
+  int tuned_T[3][2] = {{0}}, tuned_arena[3][2] = {{0}};   // autotuner's choice (0: none yet)
 };
 
 struct cmgb_ctx_s {
@@ -96,7 +112,9 @@ struct cmgb_ctx_s {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   float last_ms = 0.f;
   int last_launches = 0;
-  int tile_rows = 16, window_len = 0, ctas_per_sm = 0;
+  int64_t last_h2d = 0, last_d2h = 0;
+  int tile_rows = 0, window_len = 0, ctas_per_sm = 0, threads = kDefaultThreads, arena = 0;
+  float *d_arena = nullptr; size_t arena_bytes = 0;
   // scratch
   float *d_carry = nullptr; size_t carry_bytes = 0;
   float *d_ring = nullptr; size_t ring_bytes = 0;
@@ -154,7 +172,7 @@ extern "C" void cmgb_ctx_destroy(cmgb_ctx *c)
 {
   if (!c) return;
   cudaSetDevice(c->device);
-  cudaFree(c->d_carry); cudaFree(c->d_ring); cudaFree(c->d_dsq); cudaFree(c->d_cand);
+  cudaFree(c->d_carry); cudaFree(c->d_ring); cudaFree(c->d_arena); cudaFree(c->d_dsq); cudaFree(c->d_cand);
   cudaFree(c->d_ctl); cudaFree(c->d_vsc); cudaFree(c->d_ilog);
   cudaFreeHost(c->h_ctl);
   cudaEventDestroy(c->ev0); cudaEventDestroy(c->ev1);
@@ -162,17 +180,28 @@ extern "C" void cmgb_ctx_destroy(cmgb_ctx *c)
   delete c;
 }
 
-extern "C" int cmgb_ctx_set_shape(cmgb_ctx *c, int tile_rows, int window_len, int ctas_per_sm)
+extern "C" int cmgb_ctx_set_shape(cmgb_ctx *c, int tile_rows, int window_len, int ctas_per_sm, int threads, int arena)
 {
   if (!c) return CMGB_EINVAL;
+  if (arena < 0 || arena > 2) return CMGB_EINVAL;
+  c->arena = arena;
   if (tile_rows < 0 || tile_rows > 64 || window_len < 0 || ctas_per_sm < 0 || ctas_per_sm > 8) return CMGB_EINVAL;
-  c->tile_rows = tile_rows ? tile_rows : 16;
+  if (threads != 0 && (threads < 64 || threads > 512 || threads % 32)) return CMGB_EINVAL;
+  c->tile_rows = tile_rows;
   c->window_len = window_len;
   c->ctas_per_sm = ctas_per_sm;
+#ifndef CMGB_HOST_EMULATION
+  c->threads = threads ? threads : kDefaultThreads;
+#endif
   return CMGB_OK;
 }
 extern "C" float cmgb_ctx_last_kernel_ms(const cmgb_ctx *c) { return c ? c->last_ms : 0.f; }
 extern "C" int cmgb_ctx_last_launches(const cmgb_ctx *c) { return c ? c->last_launches : 0; }
+extern "C" void cmgb_ctx_last_transfer_bytes(const cmgb_ctx *c, int64_t *h2d, int64_t *d2h)
+{
+  if (h2d) *h2d = c ? c->last_h2d : 0;
+  if (d2h) *d2h = c ? c->last_d2h : 0;
+}
 
 extern "C" int cmgb_model_create(cmgb_ctx *c, const cmgb_model_desc *d, cmgb_model **ret, char *errbuf)
 {
@@ -192,6 +221,8 @@ extern "C" int cmgb_model_create(cmgb_ctx *c, const cmgb_model_desc *d, cmgb_mod
   m->endsc.assign(d->endsc, d->endsc + M); m->beginsc.assign(d->beginsc, d->beginsc + M);
   m->iendsc.assign(d->iendsc, d->iendsc + M); m->ibeginsc.assign(d->ibeginsc, d->ibeginsc + M);
   m->el_selfsc = d->el_selfsc; m->iel_selfsc = d->iel_selfsc;
+  m->oesc.assign(d->oesc, d->oesc + (size_t) M * KK);
+  m->ioesc.assign(d->ioesc, d->ioesc + (size_t) M * KK);
   std::memset(&m->desc, 0, sizeof(m->desc));
   cmgb_model_desc &D = m->desc;
   D.M = M; D.W = d->W; D.K = d->K; D.Kp = d->Kp; D.flags = d->flags;
@@ -201,6 +232,7 @@ extern "C" int cmgb_model_create(cmgb_ctx *c, const cmgb_model_desc *d, cmgb_mod
   D.iendsc = m->iendsc.data(); D.ibeginsc = m->ibeginsc.data();
   D.el_selfsc = d->el_selfsc; D.iel_selfsc = d->iel_selfsc;
   D.null = m->null.data(); D.null3_omega = d->null3_omega;
+  D.oesc = m->oesc.data(); D.ioesc = m->ioesc.data();
   if (cudaSetDevice(c->device) != cudaSuccess) ERRF(CMGB_ENODEV, "cudaSetDevice failed");
   if (cudaMalloc(&m->d_oesc, sizeof(float) * (size_t) M * KK) != cudaSuccess ||
       cudaMalloc(&m->d_ioesc, sizeof(int) * (size_t) M * KK) != cudaSuccess)
@@ -216,7 +248,7 @@ extern "C" void cmgb_model_destroy(cmgb_model *m)
   if (!m) return;
   cudaSetDevice(m->ctx->device);
   cudaFree(m->d_oesc); cudaFree(m->d_ioesc);
-  for (auto &row : m->plans) for (auto &p : row) cudaFree(p.d_states);
+  for (auto &row : m->plans) for (auto &p : row) { cudaFree(p.d_states); cudaFree(p.d_rec); }
   delete m;
 }
 
@@ -233,25 +265,40 @@ extern "C" void cmgb_hitlist_clear(cmgb_hitlist *hl) { if (hl) hl->h.clear(); }
 
 // Builds (once) the plan of band set qdbidx for the context's tile size,
 // shrinking the tile until its shared memory fits the device.
-static int get_plan(cmgb_model *m, int qdbidx, DevPlan **ret, char *errbuf)
+static int get_plan(cmgb_model *m, int qdbidx, bool ins, DevPlan **ret, char *errbuf)
 {
   cmgb_ctx *c = m->ctx;
-  DevPlan &dp = m->plans[qdbidx][0];
-  if (dp.built && dp.T == c->tile_rows) { *ret = &dp; return CMGB_OK; }
+  DevPlan &dp = m->plans[qdbidx][ins ? 1 : 0];
+  // shape: the context's explicit choice, else the autotuner's, else 16 rows in shared memory
+  const int wantT = c->tile_rows ? c->tile_rows : (m->tuned_T[qdbidx][ins] ? m->tuned_T[qdbidx][ins] : 16);
+  const int wantA = c->tile_rows ? c->arena : (m->tuned_T[qdbidx][ins] ? m->tuned_arena[qdbidx][ins] : c->arena);
+  if (dp.built && dp.T == wantT && dp.nt == c->threads && dp.arena == wantA) { *ret = &dp; return CMGB_OK; }
   if (dp.d_states) { cudaFree(dp.d_states); dp.d_states = nullptr; }
+  if (dp.d_rec) { cudaFree(dp.d_rec); dp.d_rec = nullptr; }
   PlanOut po;
-  int T = c->tile_rows;
+  int T = wantT;
   for (;;) {
     po = PlanOut();
-    if (!build_plan(&m->desc, qdbidx, T, kThreads, &po)) ERRF(CMGB_EINCOMPAT, "%s", po.err.c_str());
+    // arena: 1 shared memory, 2 global memory, 0 shared when it fits the device, else global
+    bool gl = wantA == 2;
+    if (!build_plan(&m->desc, qdbidx, T, c->threads, ins, gl, &po)) ERRF(CMGB_EINCOMPAT, "%s", po.err.c_str());
+    if (!gl && wantA == 0 && po.plan.smem_bytes + 64 > c->max_smem_optin) {
+      po = PlanOut();
+      if (!build_plan(&m->desc, qdbidx, T, c->threads, ins, true, &po)) ERRF(CMGB_EINCOMPAT, "%s", po.err.c_str());
+    }
     if (po.plan.smem_bytes + 64 <= c->max_smem_optin) break;
     if (T <= 2) ERRF(CMGB_ERANGE, "model needs %d bytes of shared memory per CTA even with 2-row tiles", po.plan.smem_bytes);
     T = T > 8 ? T - 4 : T - 2;
   }
-  CUDA_TRY(cudaMalloc(&dp.d_states, sizeof(StateInfo) * m->M));
-  CUDA_TRY(cudaMemcpy(dp.d_states, po.states.data(), sizeof(StateInfo) * m->M, cudaMemcpyHostToDevice));
+  build_records(&m->desc, ins, &po);
+  CUDA_TRY(cudaMalloc(&dp.d_rec, po.records.size()));
+  CUDA_TRY(cudaMemcpy(dp.d_rec, po.records.data(), po.records.size(), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMalloc(&dp.d_states, sizeof(StateInfo) * po.phases.size()));
+  CUDA_TRY(cudaMemcpy(dp.d_states, po.phases.data(), sizeof(StateInfo) * po.phases.size(), cudaMemcpyHostToDevice));
   dp.plan = po.plan;
-  dp.T = c->tile_rows;
+  dp.T = wantT;
+  dp.nt = c->threads;
+  dp.arena = wantA;
   dp.built = true;
   *ret = &dp;
   return CMGB_OK;
@@ -274,7 +321,7 @@ static int scan_std(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, bool i
   int st;
   CUDA_TRY(cudaSetDevice(c->device));
   DevPlan *dp;
-  if ((st = get_plan(m, qdbidx, &dp, errbuf)) != CMGB_OK) return st;
+  if ((st = get_plan(m, qdbidx, ins, &dp, errbuf)) != CMGB_OK) return st;
   const ScanPlan &P = dp->plan;
   const int64_t L = j0 - i0 + 1;
   const int W = m->W;
@@ -289,10 +336,23 @@ static int scan_std(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, bool i
     CUDA_TRY(cudaMemcpyAsync(c->d_dsq, host_dsq + lo, need, cudaMemcpyHostToDevice, c->stream));
     d_dsq = c->d_dsq - lo;
   }
+  c->last_h2d = dev_dsq_in ? 0 : (int64_t) (j0 + 2 - lo);
+  c->last_h2d += (int64_t) sizeof(Control);
+  c->last_d2h = (int64_t) sizeof(Control) + (ret_vsc ? (int64_t) sizeof(unsigned) * m->M : 0);
 
   // launch shape
+  const bool gl = P.arena_global != 0;
   int cps = c->ctas_per_sm;
-  if (cps == 0) cps = (2 * (P.smem_bytes + 1024) <= 228 * 1024) ? 2 : 1;
+  if (cps == 0) {
+#ifndef CMGB_HOST_EMULATION
+    int nb = 1;
+    if (ins) { if (gl) CUDA_TRY((prepare_qdb<true, true>(c->threads, P.smem_bytes, &nb))); else CUDA_TRY((prepare_qdb<true, false>(c->threads, P.smem_bytes, &nb))); }
+    else     { if (gl) CUDA_TRY((prepare_qdb<false, true>(c->threads, P.smem_bytes, &nb))); else CUDA_TRY((prepare_qdb<false, false>(c->threads, P.smem_bytes, &nb))); }
+    cps = nb < 1 ? 1 : nb;
+#else
+    cps = 1;
+#endif
+  }
   int grid_max = c->nsm * cps;
   int64_t win = c->window_len;
   if (win <= 0) {
@@ -309,6 +369,7 @@ static int scan_std(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, bool i
   size_t ring_need = sizeof(float) * (size_t) P.ring_elems * grid;
   if ((st = grow((void **) &c->d_carry, &c->carry_bytes, carry_need, errbuf)) != CMGB_OK) return st;
   if ((st = grow((void **) &c->d_ring, &c->ring_bytes, ring_need, errbuf)) != CMGB_OK) return st;
+  if (gl && (st = grow((void **) &c->d_arena, &c->arena_bytes, sizeof(float) * (size_t) P.arena_elems * grid, errbuf)) != CMGB_OK) return st;
   if (ret_vsc && c->vsc_len < m->M) {
     cudaFree(c->d_vsc); c->d_vsc = nullptr;
     if (cudaMalloc(&c->d_vsc, sizeof(unsigned) * m->M) != cudaSuccess) ERRF(CMGB_EMEM, "out of device memory");
@@ -322,7 +383,7 @@ static int scan_std(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, bool i
 
   KParams kp;
   std::memset(&kp, 0, sizeof(kp));
-  kp.st = dp->d_states; kp.plan = P;
+  kp.st = dp->d_states; kp.plan = P; kp.rec = dp->d_rec; kp.arena = c->d_arena;
   kp.oesc = m->d_oesc; kp.ioesc = m->d_ioesc; kp.ilog = c->d_ilog;
   kp.dsq = d_dsq; kp.i0 = i0; kp.j0 = j0; kp.win_len = win; kp.nwin = (int) nwin;
   kp.queue = &c->d_ctl->queue; kp.carry = c->d_carry; kp.ring = c->d_ring;
@@ -335,12 +396,15 @@ static int scan_std(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, bool i
 
   const size_t smem = (size_t) P.smem_bytes;
 #ifndef CMGB_HOST_EMULATION
-  if (ins) CUDA_TRY(cudaFuncSetAttribute(qdb_scan_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
-  else     CUDA_TRY(cudaFuncSetAttribute(qdb_scan_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+  {
+    int nb_unused = 0;
+    if (ins) { if (gl) CUDA_TRY((prepare_qdb<true, true>(c->threads, P.smem_bytes, &nb_unused))); else CUDA_TRY((prepare_qdb<true, false>(c->threads, P.smem_bytes, &nb_unused))); }
+    else     { if (gl) CUDA_TRY((prepare_qdb<false, true>(c->threads, P.smem_bytes, &nb_unused))); else CUDA_TRY((prepare_qdb<false, false>(c->threads, P.smem_bytes, &nb_unused))); }
+  }
 #endif
   CUDA_TRY(cudaEventRecord(c->ev0, c->stream));
-  if (ins) launch_qdb<true>(grid, kThreads, smem, c->stream, kp);
-  else     launch_qdb<false>(grid, kThreads, smem, c->stream, kp);
+  if (ins) { if (gl) launch_qdb<true, true>(grid, c->threads, smem, c->stream, kp); else launch_qdb<true, false>(grid, c->threads, smem, c->stream, kp); }
+  else     { if (gl) launch_qdb<false, true>(grid, c->threads, smem, c->stream, kp); else launch_qdb<false, false>(grid, c->threads, smem, c->stream, kp); }
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaEventRecord(c->ev1, c->stream));
   CUDA_TRY(cudaMemcpyAsync(h, c->d_ctl, sizeof(Control), cudaMemcpyDeviceToHost, c->stream));
@@ -349,7 +413,8 @@ static int scan_std(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, bool i
   CUDA_TRY(cudaStreamSynchronize(c->stream));
   CUDA_TRY(cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1));
   c->last_launches = 1;
-  if (h->err) ERRF(CMGB_ERANGE, "%s, more than %d candidate hit cells; raise the cutoff", fn, kCandCap);
+  if (h->err & 2) ERRF(CMGB_ENODEV, "%s, a bounded device wait ran out (phase record copy)", fn);
+  if (h->err & 1) ERRF(CMGB_ERANGE, "%s, more than %d candidate hit cells; raise the cutoff", fn, kCandCap);
 
   auto u2f = [](unsigned u) { if (u == 0) return CMGB_IMPOSSIBLE; unsigned b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u; float f; std::memcpy(&f, &b, 4); return f; };
   const float best = u2f(h->best);
@@ -362,12 +427,14 @@ static int scan_std(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, bool i
     const int n = h->ncand;
     c->h_cand.resize(n);
     if (n > 0) CUDA_TRY(cudaMemcpy(c->h_cand.data(), c->d_cand, sizeof(Cand) * n, cudaMemcpyDeviceToHost));
+    c->last_d2h += (int64_t) sizeof(Cand) * n;
     std::vector<uint8_t> res_copy;
     const uint8_t *hd = host_dsq;
     if (do_null3 && n > 0 && hd == nullptr) {
       // device-resident residues: fetch [i0, j0] for the composition counts
       res_copy.resize((size_t) (j0 + 2));
       CUDA_TRY(cudaMemcpy(res_copy.data() + i0, dev_dsq_in + i0, (size_t) L, cudaMemcpyDeviceToHost));
+      c->last_d2h += L;
       hd = res_copy.data();
     }
     ResolveArgs ra;
@@ -405,6 +472,49 @@ extern "C" int cmgb_FastIInsideScan_dev(cmgb_ctx *c, cmgb_model *m, char *errbuf
 {
   if (d_dsq == nullptr) ERRF(CMGB_EINCOMPAT, "FastIInsideScan, dsq is NULL");
   return scan_std(c, m, errbuf, qdbidx, true, nullptr, d_dsq, i0, j0, cutoff, hl, do_null3, env_cutoff, envi, envj, vsc, sc);
+}
+
+// Times candidate shapes (tile rows x arena placement) of band set qdbidx and
+// algorithm (0 CYK, 1 integer Inside) on a seeded iid sample and keeps the
+// fastest for this model; later scans that leave the shape to the library use it.
+extern "C" int cmgb_autotune(cmgb_ctx *c, cmgb_model *m, int qdbidx, int algo, int64_t sample_len,
+                             int *ret_tile_rows, int *ret_arena, char *errbuf)
+{
+  if (!c || !m || qdbidx < 0 || qdbidx > 2 || algo < 0 || algo > 1) ERRF(CMGB_EINVAL, "cmgb_autotune: invalid argument");
+  if (sample_len <= 0) sample_len = (int64_t) c->nsm * 1500;
+  std::vector<uint8_t> dsq((size_t) sample_len + 2);
+  uint64_t x = 0x9E3779B97F4A7C15ULL;
+  for (int64_t i = 1; i <= sample_len; i++) {            // 40% GC, splitmix-style generator
+    x += 0x9E3779B97F4A7C15ULL; uint64_t z = x; z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL; z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL; z ^= z >> 31;
+    const unsigned u = (unsigned) (z % 100);
+    dsq[i] = u < 30 ? 0 : u < 50 ? 1 : u < 70 ? 2 : 3;
+  }
+  dsq[0] = dsq[sample_len + 1] = 255;
+  static const int cand[][2] = {{16, 1}, {8, 1}, {32, 2}, {48, 2}, {64, 2}};
+  const int saveT = c->tile_rows, saveA = c->arena;
+  float best_ms = 3.0e38f; int bT = 16, bA = 1;
+  int st = CMGB_OK;
+  for (const auto &cd : cand) {
+    c->tile_rows = cd[0]; c->arena = cd[1];
+    float ms = 0.f;
+    for (int rep = 0; rep < 2 && st == CMGB_OK; rep++) {   // first run builds the plan and warms up
+      if (algo) st = cmgb_FastIInsideScan(c, m, errbuf, qdbidx, dsq.data(), 1, sample_len, 1e30f, nullptr, 0, 1e30f, nullptr, nullptr, nullptr, nullptr);
+      else      st = cmgb_FastCYKScan(c, m, errbuf, qdbidx, dsq.data(), 1, sample_len, 1e30f, nullptr, 0, 1e30f, nullptr, nullptr, nullptr, nullptr);
+      ms = c->last_ms;
+    }
+    if (st != CMGB_OK) {           // a shape that does not fit this device is skipped
+      if (st == CMGB_ENODEV) break;
+      st = CMGB_OK;
+      continue;
+    }
+    if (ms < best_ms) { best_ms = ms; bT = cd[0]; bA = cd[1]; }
+  }
+  c->tile_rows = saveT; c->arena = saveA;
+  if (st != CMGB_OK) return st;
+  m->tuned_T[qdbidx][algo] = bT; m->tuned_arena[qdbidx][algo] = bA;
+  if (ret_tile_rows) *ret_tile_rows = bT;
+  if (ret_arena) *ret_arena = bA;
+  return CMGB_OK;
 }
 
 extern "C" int64_t cmgb_count_cells(const cmgb_model_desc *m, int qdbidx, int64_t L)

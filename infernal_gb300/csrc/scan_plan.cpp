@@ -13,6 +13,8 @@
 #include <string>
 #include <vector>
 
+static_assert(sizeof(StateInfo) % 16 == 0, "phase records must stay 16-byte aligned");
+
 namespace cmgb {
 
 static inline int st_delta(int t) { return t == CMGB_MP_st ? 2 : (t == CMGB_ML_st || t == CMGB_MR_st || t == CMGB_IL_st || t == CMGB_IR_st) ? 1 : 0; }
@@ -37,7 +39,7 @@ struct Arena {
   }
 };
 
-bool build_plan(const cmgb_model_desc *m, int qdbidx, int T, int nthreads, PlanOut *out)
+bool build_plan(const cmgb_model_desc *m, int qdbidx, int T, int nthreads, bool logsum_table, bool arena_global, PlanOut *out)
 {
   const int M = m->M, Wm = m->W;
   const int *dmin = qdbidx == CMGB_QDB1_TIGHT ? m->dmin1 : qdbidx == CMGB_QDB2_LOOSE ? m->dmin2 : nullptr;
@@ -94,6 +96,7 @@ bool build_plan(const cmgb_model_desc *m, int qdbidx, int T, int nthreads, PlanO
     s.has_iend = m->iendsc[v] != -CMGB_INFTY;
     s.oesc_off = v * m->Kp * m->Kp;
     s.carry = -1; s.ring = -1; s.buf = -1;
+    s.v = v;
   }
   // Integer local-begin availability must agree with the float one
   for (int v = 1; v < M; v++)
@@ -176,14 +179,33 @@ bool build_plan(const cmgb_model_desc *m, int qdbidx, int T, int nthreads, PlanO
   ScanPlan P;
   std::memset(&P, 0, sizeof(P));
   P.M = M; P.W = Wm; P.T = T; P.Kp = m->Kp; P.nthreads = nthreads;
+  int tmp_stride = 1;
+  for (int v = 0; v < M; v++) if (S[v].kind == SK_IL || S[v].kind == SK_IR) tmp_stride = std::max(tmp_stride, S[v].hi - S[v].lo + 1);
+  tmp_stride |= 1;
   int off = arena.peak;
   off = (off + 3) & ~3;
   P.const_row = off; P.const_row_len = Wm + 2; off += (Wm + 2 + 3) & ~3;
-  P.acc_off = off; off += T * (Wm + 1);
-  P.bestr_off = off; off += T * (Wm + 1);
+  P.acc_w = std::max(1, S[0].dxW - S[0].dn + 1);
+  P.acc_off = off; off += T * P.acc_w;
+  P.bestr_off = off; off += T * P.acc_w;
+  P.tmp_off = off; P.tmp_stride = tmp_stride; off += (T + 1) * tmp_stride;
+  off = (off + 3) & ~3;
+  P.arena_global = arena_global ? 1 : 0;
+  if (arena_global) {            // everything above goes to global memory; shared memory restarts at 0
+    P.arena_elems = off;
+    off = 0;
+  } else P.arena_elems = 0;
+  P.desc_words = (int) (sizeof(StateInfo) / 4);
+  P.rec_max_bytes = (int) sizeof(StateInfo) + ((m->Kp * m->Kp * 4 + 15) & ~15);
+  P.desc_off = off; off += 2 * (P.rec_max_bytes / 4);     // two record slots, 16-byte aligned
+  P.esc_off = P.desc_off + P.desc_words;                  // emission row follows the descriptor in a slot
+  off = (off + 3) & ~3;
   P.res_off = off; P.res_len = Wm + T + 2; off += (P.res_len + 3) / 4;
+  off = (off + 3) & ~3;
+  P.ltbl_off = off;
+  if (logsum_table) off += (CMGB_LOGSUM_TBL * 2 + 3) / 4;
   P.smem_elems = off;
-  P.smem_bytes = off * 4 + 16;   // + the window slot shared by the CTA
+  P.smem_bytes = off * 4 + 32;   // + the window slot and the two record mbarriers
   P.carry_elems = carry;
   P.ring_elems = ring > 0 ? ring : 1;
   P.ring_rows = R;
@@ -201,9 +223,50 @@ bool build_plan(const cmgb_model_desc *m, int qdbidx, int T, int nthreads, PlanO
       s.clo[o] = c.lo;
     }
   }
+  P.nphase = 0;
+  for (int v = 0; v < M; v++) {
+    StateInfo &q = S[v];
+    q.wp_all = std::max(1, q.hi - q.lo + 1); q.sr_all = nthreads / q.wp_all; q.sdd_all = nthreads - q.sr_all * q.wp_all;
+    q.wp_band = std::max(1, q.dxW - q.dn + 1); q.sr_band = nthreads / q.wp_band; q.sdd_band = nthreads - q.sr_band * q.wp_band;
+    q.inv_all = 1.0f / (float) q.wp_all; q.inv_band = 1.0f / (float) q.wp_band;
+  }
+  for (int v = M - 1; v >= 0; v--) if (S[v].kind != SK_E) { out->phases.push_back(S[v]); P.nphase++; }
   out->plan = P;
   out->states = std::move(S);
   return true;
 }
 
+}  // namespace cmgb
+
+namespace cmgb {
+void build_records(const cmgb_model_desc *m, bool ins, PlanOut *out)
+{
+  const int KK = m->Kp * m->Kp;
+  std::vector<int> off(out->phases.size()), bytes(out->phases.size());
+  size_t total = 0;
+  for (size_t k = 0; k < out->phases.size(); k++) {
+    const StateInfo &s = out->phases[k];
+    int elen = s.emit == 3 ? KK : s.emit ? m->Kp : 0;
+    bytes[k] = (int) sizeof(StateInfo) + ((elen * 4 + 15) & ~15);
+    off[k] = (int) total;
+    total += bytes[k];
+  }
+  out->records.assign(total, 0);
+  const size_t np = out->phases.size();
+  for (size_t k = 0; k < np; k++) {
+    StateInfo s = out->phases[k];
+    s.next_off = off[(k + 1) % np];
+    s.next_bytes = bytes[(k + 1) % np];
+    out->phases[k].next_off = s.next_off;
+    out->phases[k].next_bytes = s.next_bytes;
+    std::memcpy(&out->records[off[k]], &s, sizeof(StateInfo));
+    int elen = s.emit == 3 ? KK : s.emit ? m->Kp : 0;
+    unsigned char *e = &out->records[off[k] + sizeof(StateInfo)];
+    for (int q = 0; q < elen; q++) {
+      if (ins) { int x = m->ioesc[(size_t) s.v * KK + q]; std::memcpy(e + 4 * q, &x, 4); }
+      else { float x = m->oesc[(size_t) s.v * KK + q]; std::memcpy(e + 4 * q, &x, 4); }
+    }
+  }
+  out->plan.rec0_bytes = bytes[0];
+}
 }  // namespace cmgb

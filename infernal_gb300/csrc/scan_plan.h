@@ -30,7 +30,15 @@ struct StateInfo {
   int8_t  has_begin; // local begin into this state
   int8_t  has_end;   // local end (init_sc not IMPOSSIBLE)
   int8_t  has_iend;  // integer version of has_end
-  int8_t  pad_[7];
+  int8_t  pad_[3];
+  int     v;         // state index
+  int     next_off;  // byte offset of the next phase's record (desc + emission row) in the record array
+  int     next_bytes;// its size (multiple of 16)
+  // cell-walk constants for the kernel's thread count: padded range [lo,hi]
+  // and band [dn,dxW]: width, step in rows / columns per nt cells
+  int     wp_all, sr_all, sdd_all, wp_band, sr_band, sdd_band;
+  float   inv_all, inv_band;    // 1/width, for the first row/column split
+  int     pad3_[2];
   int     lo, hi;    // padded d range of the buffer
   int     dn, dxW;   // own band for j >= W (dx shrinks to jp for small jp)
   int     buf;       // shared-memory element offset of row 0 (E: constant row)
@@ -63,6 +71,19 @@ enum {
 // Whole-plan parameters (device copy lives in global memory).
 struct ScanPlan {
   int M, W, T;            // states, model W, tile rows
+  int nphase;             // computed states (all but E), processed in descending v
+  int desc_off;           // element offset of the two prefetched phase descriptors
+  int desc_words;         // words per descriptor (StateInfo)
+  int rec_max_bytes;      // largest phase record (descriptor + emission row)
+  int rec0_bytes;         // size of phase 0's record
+  int esc_off;            // element offset of the two prefetched emission rows (Kp*Kp each)
+  int tmp_off;            // element offset of the insert-state scratch [(T+1) x tmp_stride]
+  int tmp_stride;
+  int acc_w;              // root accumulator width (root band)
+  int ltbl_off;           // element offset of the uint16 ILogsum table (integer Inside plans only)
+  int arena_global;       // 1: tile buffers, constant row, accumulator and insert scratch live in a
+                          //    per-CTA global-memory arena (L1/L2 resident) instead of shared memory
+  int arena_elems;        // size of that per-CTA arena (elements)
   int Kp;
   int nthreads;
   int smem_elems;         // tile-buffer arena size (elements of 4 bytes)
@@ -89,10 +110,15 @@ struct ScanPlan {
 namespace cmgb {
 struct PlanOut {
   ScanPlan plan;
-  std::vector<StateInfo> states;
+  std::vector<StateInfo> states;   // indexed by state v
+  std::vector<StateInfo> phases;   // computed states in sweep order (v = M-1 .. 0, E states left out)
+  std::vector<unsigned char> records;  // per phase: StateInfo + its emission row, 16-byte aligned
   std::string err;
 };
 // Builds the plan of band set qdbidx with T-row tiles; false + err on failure.
-bool build_plan(const cmgb_model_desc *m, int qdbidx, int T, int nthreads, PlanOut *out);
+bool build_plan(const cmgb_model_desc *m, int qdbidx, int T, int nthreads, bool logsum_table, bool arena_global, PlanOut *out);
+// Packs the phase records (descriptor followed by the state's emission row,
+// float or int) that the kernel streams into shared memory one phase ahead.
+void build_records(const cmgb_model_desc *m, bool ins, PlanOut *out);
 }  // namespace cmgb
 #endif

@@ -29,10 +29,10 @@ CMGB_NOTGREEDY = 1 << 2
 # every symbol the header declares (checked by the CPU tests)
 EXPORTS = [
     "cmgb_logsum_init", "cmgb_ctx_create", "cmgb_ctx_destroy", "cmgb_ctx_set_shape",
-    "cmgb_ctx_last_kernel_ms", "cmgb_ctx_last_launches", "cmgb_model_create", "cmgb_model_destroy",
+    "cmgb_ctx_last_kernel_ms", "cmgb_ctx_last_launches", "cmgb_ctx_last_transfer_bytes", "cmgb_model_create", "cmgb_model_destroy",
     "cmgb_hitlist_create", "cmgb_hitlist_destroy", "cmgb_hitlist_count", "cmgb_hitlist_get",
     "cmgb_hitlist_clear", "cmgb_FastCYKScan", "cmgb_FastIInsideScan", "cmgb_FastCYKScan_dev",
-    "cmgb_FastIInsideScan_dev", "cmgb_count_cells",
+    "cmgb_FastIInsideScan_dev", "cmgb_count_cells", "cmgb_autotune",
 ]
 
 _SCAN_ARGS = [P, P, ctypes.c_char_p, I, P, I64, I64, F, P, I, F, P, P, P, P]
@@ -62,12 +62,13 @@ def bind(path: str) -> ctypes.CDLL:
     lib.cmgb_ctx_create.argtypes = [I, ctypes.POINTER(P), ctypes.c_char_p]
     lib.cmgb_ctx_create.restype = I
     lib.cmgb_ctx_destroy.argtypes = [P]
-    lib.cmgb_ctx_set_shape.argtypes = [P, I, I, I]
+    lib.cmgb_ctx_set_shape.argtypes = [P, I, I, I, I, I]
     lib.cmgb_ctx_set_shape.restype = I
     lib.cmgb_ctx_last_kernel_ms.argtypes = [P]
     lib.cmgb_ctx_last_kernel_ms.restype = F
     lib.cmgb_ctx_last_launches.argtypes = [P]
     lib.cmgb_ctx_last_launches.restype = I
+    lib.cmgb_ctx_last_transfer_bytes.argtypes = [P, ctypes.POINTER(I64), ctypes.POINTER(I64)]
     lib.cmgb_model_create.argtypes = [P, P, ctypes.POINTER(P), ctypes.c_char_p]
     lib.cmgb_model_create.restype = I
     lib.cmgb_model_destroy.argtypes = [P]
@@ -83,6 +84,8 @@ def bind(path: str) -> ctypes.CDLL:
         f = getattr(lib, name)
         f.argtypes = _SCAN_ARGS
         f.restype = I
+    lib.cmgb_autotune.argtypes = [P, P, I, I, I64, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.c_char_p]
+    lib.cmgb_autotune.restype = I
     lib.cmgb_count_cells.argtypes = [P, I, I64]
     lib.cmgb_count_cells.restype = I64
     lib.cmgb_logsum_init()
@@ -134,8 +137,8 @@ class Scanner:
         except Exception:
             pass
 
-    def set_shape(self, tile_rows: int = 0, window_len: int = 0, ctas_per_sm: int = 0):
-        st = self.lib.cmgb_ctx_set_shape(self._ctx, tile_rows, window_len, ctas_per_sm)
+    def set_shape(self, tile_rows: int = 0, window_len: int = 0, ctas_per_sm: int = 0, threads: int = 0, arena: int = 0):
+        st = self.lib.cmgb_ctx_set_shape(self._ctx, tile_rows, window_len, ctas_per_sm, threads, arena)
         if st != 0:
             raise ScanError(st, "invalid launch shape")
 
@@ -187,6 +190,23 @@ class Scanner:
                 self.lib.cmgb_hitlist_destroy(hl)
         return ScanResult(hits, envi.value, envj.value, sc.value, vsc,
                           float(self.lib.cmgb_ctx_last_kernel_ms(self._ctx)))
+
+    def autotune(self, m: cmfile.CMModel, qdbidx: int, algo: str = "cyk", sample_len: int = 0):
+        """Runs cmgb_autotune for (model, band set, algorithm); returns (tile_rows, arena)."""
+        mh = self.model(m, 0)
+        t, a = I(), I()
+        err = ctypes.create_string_buffer(256)
+        st = self.lib.cmgb_autotune(self._ctx, mh, qdbidx, 1 if algo == "inside" else 0, sample_len,
+                                    ctypes.byref(t), ctypes.byref(a), err)
+        if st != 0:
+            raise ScanError(st, err.value.decode())
+        return t.value, a.value
+
+    def last_transfer_bytes(self):
+        """(host->device, device->host) bytes moved by the last scan."""
+        a, b = I64(), I64()
+        self.lib.cmgb_ctx_last_transfer_bytes(self._ctx, ctypes.byref(a), ctypes.byref(b))
+        return a.value, b.value
 
     def last_launches(self) -> int:
         return int(self.lib.cmgb_ctx_last_launches(self._ctx))

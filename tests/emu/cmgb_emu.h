@@ -27,4 +27,39 @@ inline long long cmgb_emu_maxll(long long *p, long long v)
   while (cur < v && !__atomic_compare_exchange_n(p, &cur, v, false, __ATOMIC_SEQ_CST, __ATOMIC_SEQ_CST)) {}
   return cur;
 }
+#include <cstring>
+// warp-level primitives: the 32 threads of an emulated warp meet at a
+// per-warp barrier and exchange values through a slot array
+struct EmuWarp {
+  std::barrier<> bar{32};
+  long long slot[32];
+};
+inline thread_local EmuWarp *cmgb_emu_warp = nullptr;
+inline thread_local int cmgb_emu_lane = 0;
+template <class T> inline T cmgb_shfl_up(T x, int k)
+{
+  EmuWarp *w = cmgb_emu_warp;
+  std::memcpy(&w->slot[cmgb_emu_lane], &x, sizeof(T));
+  w->bar.arrive_and_wait();
+  T y = x;
+  if (cmgb_emu_lane >= k) std::memcpy(&y, &w->slot[cmgb_emu_lane - k], sizeof(T));
+  w->bar.arrive_and_wait();
+  return y;
+}
+inline bool cmgb_any(bool b)
+{
+  EmuWarp *w = cmgb_emu_warp;
+  w->slot[cmgb_emu_lane] = b ? 1 : 0;
+  w->bar.arrive_and_wait();
+  bool any = false;
+  for (int l = 0; l < 32; l++) any = any || w->slot[l];
+  w->bar.arrive_and_wait();
+  return any;
+}
+inline void __syncwarp_portable() { cmgb_emu_warp->bar.arrive_and_wait(); }
+inline int __ldg_int(const int *p) { return *p; }
+// TMA / mbarrier stand-ins: the copy happens at issue; waits always succeed
+inline void cmgb_mbar_init(unsigned long long *mb) { *mb = 0; }
+inline void cmgb_tma_load(void *dst, const void *src, unsigned bytes, unsigned long long *) { std::memcpy(dst, src, bytes); }
+inline bool cmgb_mbar_wait(unsigned long long *, unsigned) { return true; }
 #define CMGB_EMU_THREADS 64

@@ -33,7 +33,10 @@ def test_header_and_binding_agree():
 @pytest.fixture(scope="module")
 def built_lib():
     import __graft_entry__ as g
-    if not os.path.exists(L.LIB_PATH):
+    csrc = os.path.join(ROOT, "infernal_gb300", "csrc")
+    newest = max(os.path.getmtime(os.path.join(csrc, f)) for f in os.listdir(csrc))
+    newest = max(newest, os.path.getmtime(os.path.join(ROOT, "include", "infernal_gb300.h")))
+    if not os.path.exists(L.LIB_PATH) or os.path.getmtime(L.LIB_PATH) < newest:
         g.build_library()
     return L.LIB_PATH
 
@@ -71,15 +74,15 @@ def emu():
     return L.Scanner(lib=L.bind(EMU_SO))
 
 
-@pytest.mark.parametrize("name,algo,qdb,T,win", [
-    ("tRNA", "cyk", 1, 4, 0), ("tRNA", "inside", 2, 8, 0), ("Vault", "cyk", 2, 16, 300),
-    ("tRNA", "cyk", 0, 16, 0), ("Plant_SRP", "inside", 1, 4, 0)])
-def test_emulated_kernel_matches_oracle(emu, models, name, algo, qdb, T, win):
+@pytest.mark.parametrize("name,algo,qdb,T,win,arena", [
+    ("tRNA", "cyk", 1, 4, 0, 1), ("tRNA", "inside", 2, 8, 0, 1), ("Vault", "cyk", 2, 16, 300, 1),
+    ("tRNA", "cyk", 0, 16, 0, 2), ("Plant_SRP", "inside", 1, 40, 0, 2), ("Vault", "inside", 2, 64, 250, 2)])
+def test_emulated_kernel_matches_oracle(emu, models, name, algo, qdb, T, win, arena):
     m = models[name]
     rng = np.random.default_rng(11)
-    n = 500 if name == "Plant_SRP" else 700
+    n = 400 if name == "Plant_SRP" else 600
     dsq = cmfile.digitize("".join(rng.choice(list("ACGU"), n)))
-    emu.set_shape(T, win, 1)
+    emu.set_shape(T, win, 1, 0, arena)
     r = emu.scan(m, dsq, 1, n, algo=algo, qdbidx=qdb, cutoff=-2.0, env_cutoff=1.0, want_vsc=True)
     o = oracle.scan(m, dsq, 1, n, algo=algo, qdbidx=qdb, cutoff=-2.0, env_cutoff=1.0)
     assert r.hits == o[0]

@@ -27,10 +27,11 @@ def _check(r, hits, ei, ej, sc, vsc):
         assert np.array_equal(r.vsc.view(np.int32), np.asarray(vsc, np.float32).view(np.int32))
 
 
-@pytest.mark.parametrize("T", [16, 5])
-def test_golden_on_gpu(gpu, golden, models, T):
+@pytest.mark.parametrize("T,arena", [(16, 1), (5, 1), (48, 2)])
+def test_golden_on_gpu(gpu, golden, models, T, arena):
+    """Shared-memory tiles (arena 1) and the global-memory tile arena (arena 2)."""
     meta, arrays = golden
-    gpu.set_shape(T, 0, 0)
+    gpu.set_shape(T, 0, 0, 0, arena)
     n = 0
     for c in meta:
         if c["algo"] not in ("cyk", "refcyk", "inside"):
@@ -68,8 +69,9 @@ def test_window_and_tile_invariance(gpu, models):
     n = 60000
     dsq = cmfile.digitize("".join(rng.choice(list("ACGU"), n)))
     ref = None
-    for T, win, cps in ((16, 0, 0), (8, 1500, 1), (3, 4000, 2), (16, 777, 1)):
-        gpu.set_shape(T, win, cps)
+    for T, win, cps, nt, ar in ((16, 0, 0, 0, 1), (8, 1500, 1, 256, 1), (3, 4000, 2, 0, 1), (16, 777, 1, 0, 2),
+                                (64, 2500, 0, 0, 2), (33, 0, 0, 128, 2)):
+        gpu.set_shape(T, win, cps, nt, ar)
         r = gpu.scan(m, dsq, 1, n, algo="cyk", qdbidx=1, cutoff=-1.0, env_cutoff=3.0, want_vsc=True)
         key = (r.hits, r.envi, r.envj, r.sc, r.vsc.tobytes())
         assert ref is None or key == ref
@@ -97,3 +99,17 @@ def test_contract_errors_on_gpu(gpu, models):
     with pytest.raises(L.ScanError) as e:
         gpu.scan(m, dsq, 100, 10)
     assert e.value.status == 10
+
+
+def test_autotune_keeps_results(gpu, models):
+    """The autotuner only changes the schedule: results before and after tuning agree."""
+    m = models["Vault"]
+    rng = np.random.default_rng(21)
+    n = 30000
+    dsq = cmfile.digitize("".join(rng.choice(list("ACGU"), n)))
+    gpu.set_shape(0, 0, 0)
+    a = gpu.scan(m, dsq, 1, n, algo="inside", qdbidx=2, cutoff=0.0, env_cutoff=2.0, want_vsc=True)
+    T, arena = gpu.autotune(m, 2, "inside", 20000)
+    assert T in (8, 16, 32, 48, 64) and arena in (1, 2)
+    b = gpu.scan(m, dsq, 1, n, algo="inside", qdbidx=2, cutoff=0.0, env_cutoff=2.0, want_vsc=True)
+    assert (a.hits, a.envi, a.envj, a.sc, a.vsc.tobytes()) == (b.hits, b.envi, b.envj, b.sc, b.vsc.tobytes())
