@@ -205,6 +205,44 @@ int cmgb_FastIInsideScan_dev(cmgb_ctx *ctx, cmgb_model *model, char *errbuf, int
                              cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
                              int64_t *ret_envi, int64_t *ret_envj, float *ret_vsc, float *ret_sc);
 
+/* ---- allocation-free CYK scan ----
+ * This entry point has no counterpart in the reference.  It exists for
+ * callers that must not allocate device memory while they scan: code that
+ * records work into a CUDA stream capture, hosts where a framework's own
+ * allocator owns all device memory, and long-running services that allocate
+ * everything at start-up.  It runs the same CYK kernel as cmgb_FastCYKScan_dev
+ * but keeps the kernel's scratch (per-CTA carry rows, bifurcation history
+ * rings, tile arena and work counter) in one static device array of
+ * CMGB_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds until
+ * the process exits; nothing is allocated per call.  When a model needs more
+ * scratch per CTA than fits, fewer CTAs run; if not even one fits, the call
+ * fails with CMGB_ERANGE.  The first call on a device looks up the array's
+ * device address on that device; make that first call before any stream
+ * capture.  All calls share the array, so calls that overlap on the GPU (other
+ * host threads, other streams) race: serialise them.
+ *
+ * The model's plan for qdbidx must already exist on this context (built by an
+ * earlier cmgb_FastCYKScan / cmgb_FastCYKScan_dev / cmgb_autotune call);
+ * otherwise the call returns CMGB_EINCOMPAT without allocating one.
+ * Inputs: d_dsq as for cmgb_FastCYKScan_dev.  Outputs: the candidate cells
+ * (every root cell of [i0,j0] whose CYK score is >= cutoff; the hit list of
+ * the greedy scanner is resolved from these) are written to the caller's
+ * device array d_cells[cell_cap] in no particular order, their number to
+ * *ret_ncells; envelope and best score as in cmgb_FastCYKScan.  NULL3 and
+ * per-state scores are not computed here.  The call waits for its kernel. */
+#define CMGB_NOALLOC_SCRATCH_BYTES (64u << 20)
+typedef struct {
+  int64_t j;      /* end position of the cell */
+  int     d;      /* its length: start = j - d + 1 */
+  float   score;  /* CYK bit score of the root cell */
+  int     root;   /* root state (0 or a local-begin state) */
+  int     pad;
+} cmgb_cell;
+int cmgb_FastCYKScan_noalloc(cmgb_ctx *ctx, cmgb_model *model, char *errbuf, int qdbidx,
+                             const uint8_t *d_dsq, int64_t i0, int64_t j0, float cutoff, float env_cutoff,
+                             cmgb_cell *d_cells, int cell_cap, int *ret_ncells,
+                             int64_t *ret_envi, int64_t *ret_envj, float *ret_sc);
+
 /* DP cell count of one scan of [i0,j0] with band set qdbidx: the
  * algorithmic work unit, sum over j and non-E states of the band width
  * (the count cm_CountSearchDPCalcs() approximates, src/cm_dpsearch.c:3099). */

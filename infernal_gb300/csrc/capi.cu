@@ -533,3 +533,123 @@ extern "C" int64_t cmgb_count_cells(const cmgb_model_desc *m, int qdbidx, int64_
   }
   return cells;
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free CYK scan (cmgb_FastCYKScan_noalloc): scratch in a static
+// device array, outputs in caller-provided device memory.
+#ifndef CMGB_HOST_EMULATION
+static __device__ __align__(256) unsigned char g_noalloc_scratch[CMGB_NOALLOC_SCRATCH_BYTES];
+
+// Device address of g_noalloc_scratch on each device, looked up once per device.
+static std::mutex g_noalloc_mu;
+static void *g_noalloc_ptr[64];
+
+static __global__ void noalloc_init_kernel(int *queue, Control *ctl)
+{
+  *queue = 0;
+  ctl->queue = 0; ctl->ncand = 0; ctl->err = 0;
+  ctl->env[0] = LLONG_MAX; ctl->env[1] = -1;
+  ctl->best = 0u;
+}
+#endif
+
+extern "C" int cmgb_FastCYKScan_noalloc(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx,
+                                        const uint8_t *d_dsq, int64_t i0, int64_t j0, float cutoff, float env_cutoff,
+                                        cmgb_cell *d_cells, int cell_cap, int *ret_ncells,
+                                        int64_t *ret_envi, int64_t *ret_envj, float *ret_sc)
+{
+#ifdef CMGB_HOST_EMULATION
+  ERRF(CMGB_ENODEV, "FastCYKScan_noalloc, not available in the host emulation");
+#else
+  if (!c || !m) ERRF(CMGB_EINVAL, "FastCYKScan_noalloc, NULL context or model");
+  if (j0 < i0 || i0 < 1) ERRF(CMGB_EINCOMPAT, "FastCYKScan_noalloc, i0: %lld j0: %lld", (long long) i0, (long long) j0);
+  if (d_dsq == nullptr) ERRF(CMGB_EINCOMPAT, "FastCYKScan_noalloc, dsq is NULL");
+  if (qdbidx < 0 || qdbidx > 2) ERRF(CMGB_EINCOMPAT, "FastCYKScan_noalloc, qdbidx is invalid");
+  if (d_cells == nullptr || cell_cap <= 0) ERRF(CMGB_EINVAL, "FastCYKScan_noalloc, no output cell array");
+  if (c->device < 0 || c->device >= 64) ERRF(CMGB_ENODEV, "FastCYKScan_noalloc, device index out of range");
+  CUDA_TRY(cudaSetDevice(c->device));
+  void *scratch;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[c->device]) {
+      void *ptr = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+      if (e != cudaSuccess) ERRF(CMGB_ENODEV, "FastCYKScan_noalloc, cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+      g_noalloc_ptr[c->device] = ptr;
+    }
+    scratch = g_noalloc_ptr[c->device];
+  }
+  const DevPlan &dp = m->plans[qdbidx][0];
+  if (!dp.built) ERRF(CMGB_EINCOMPAT, "FastCYKScan_noalloc, no plan for band set %d yet: run a scan on this context first", qdbidx);
+  const ScanPlan &P = dp.plan;
+  const bool gl = P.arena_global != 0;
+  const int64_t L = j0 - i0 + 1;
+
+  // scratch layout (256-byte aligned regions): work counter, control block, then per CTA
+  // carry rows (two parities), BEGL ring and, for global-arena plans, the tile arena
+  auto al = [](size_t x) { return (x + 255) & ~(size_t) 255; };
+  const size_t per_cta = al(sizeof(float) * 2 * (size_t) P.carry_elems) + al(sizeof(float) * (size_t) P.ring_elems) +
+                         (gl ? al(sizeof(float) * (size_t) P.arena_elems) : 0);
+  const size_t head = 256 + al(sizeof(Control));
+  if (head + per_cta + 1024 > (size_t) CMGB_NOALLOC_SCRATCH_BYTES)
+    ERRF(CMGB_ERANGE, "FastCYKScan_noalloc, the model needs %zu bytes of scratch per CTA; the static array holds %u",
+         per_cta, (unsigned) CMGB_NOALLOC_SCRATCH_BYTES);
+  int nb = 1;
+  if (gl) CUDA_TRY((prepare_qdb<false, true>(c->threads, P.smem_bytes, &nb)));
+  else    CUDA_TRY((prepare_qdb<false, false>(c->threads, P.smem_bytes, &nb)));
+  int64_t grid_max = (int64_t) c->nsm * (nb < 1 ? 1 : nb);
+  const int64_t fit = (int64_t) (((size_t) CMGB_NOALLOC_SCRATCH_BYTES - head - 1024) / per_cta);   // 1024: room for region alignment
+  if (grid_max > fit) grid_max = fit;
+  int64_t win = (L + grid_max - 1) / grid_max;
+  if (win < 8LL * m->W) win = 8LL * m->W;
+  win = ((win + P.T - 1) / P.T) * P.T;
+  const int64_t nwin = (L + win - 1) / win;
+  if (nwin > INT_MAX) ERRF(CMGB_ERANGE, "FastCYKScan_noalloc, too many windows");
+  const int grid = (int) std::min<int64_t>(nwin, grid_max);
+
+  unsigned char *base = (unsigned char *) scratch;
+  int *queue = (int *) base;
+  Control *ctl = (Control *) (base + 256);
+  unsigned char *cta0 = base + head;
+  // carry, ring and arena are laid out as [grid][...] arrays, as the kernel indexes them
+  float *carry = (float *) cta0;
+  float *ring = (float *) (cta0 + al(sizeof(float) * 2 * (size_t) P.carry_elems * grid));
+  float *arena = (float *) ((unsigned char *) ring + al(sizeof(float) * (size_t) P.ring_elems * grid));
+  if ((size_t) ((unsigned char *) arena - base) + (gl ? sizeof(float) * (size_t) P.arena_elems * grid : 0) > (size_t) CMGB_NOALLOC_SCRATCH_BYTES)
+    ERRF(CMGB_ERANGE, "FastCYKScan_noalloc, scratch layout exceeds the static array");
+
+  noalloc_init_kernel<<<1, 1, 0, c->stream>>>(queue, ctl);
+  CUDA_TRY(cudaGetLastError());
+  KParams kp;
+  std::memset(&kp, 0, sizeof(kp));
+  kp.st = dp.d_states; kp.plan = P; kp.rec = dp.d_rec; kp.arena = gl ? arena : nullptr;
+  kp.oesc = m->d_oesc; kp.ioesc = m->d_ioesc; kp.ilog = c->d_ilog;
+  kp.dsq = d_dsq; kp.i0 = i0; kp.j0 = j0; kp.win_len = win; kp.nwin = (int) nwin;
+  kp.queue = queue; kp.carry = carry; kp.ring = ring;
+  kp.cand = reinterpret_cast<Cand *>(d_cells); kp.ncand = &ctl->ncand; kp.cand_cap = cell_cap;
+  kp.cand_cut = cutoff; kp.cand_pos = 0;
+  kp.env_cut = env_cutoff; kp.env = ctl->env; kp.vsc = nullptr; kp.best = &ctl->best; kp.err = &ctl->err;
+  CUDA_TRY(cudaEventRecord(c->ev0, c->stream));
+  if (gl) launch_qdb<false, true>(grid, c->threads, (size_t) P.smem_bytes, c->stream, kp);
+  else    launch_qdb<false, false>(grid, c->threads, (size_t) P.smem_bytes, c->stream, kp);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaEventRecord(c->ev1, c->stream));
+  Control h;
+  CUDA_TRY(cudaMemcpyAsync(&h, ctl, sizeof(Control), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  CUDA_TRY(cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1));
+  c->last_launches = 2;
+  if (h.err & 2) ERRF(CMGB_ENODEV, "FastCYKScan_noalloc, a bounded device wait ran out (phase record copy)");
+  if (h.err & 1) ERRF(CMGB_ERANGE, "FastCYKScan_noalloc, more than %d candidate cells", cell_cap);
+  if (ret_ncells) *ret_ncells = h.ncand;
+  if (ret_envi) *ret_envi = (h.env[1] < 0) ? -1 : h.env[0];
+  if (ret_envj) *ret_envj = (h.env[1] < 0) ? -1 : h.env[1];
+  if (ret_sc) {
+    const unsigned u = h.best;
+    float f = CMGB_IMPOSSIBLE;
+    if (u != 0) { unsigned b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u; std::memcpy(&f, &b, 4); }
+    *ret_sc = f;
+  }
+  return CMGB_OK;
+#endif
+}

@@ -32,7 +32,7 @@ EXPORTS = [
     "cmgb_ctx_last_kernel_ms", "cmgb_ctx_last_launches", "cmgb_ctx_last_transfer_bytes", "cmgb_model_create", "cmgb_model_destroy",
     "cmgb_hitlist_create", "cmgb_hitlist_destroy", "cmgb_hitlist_count", "cmgb_hitlist_get",
     "cmgb_hitlist_clear", "cmgb_FastCYKScan", "cmgb_FastIInsideScan", "cmgb_FastCYKScan_dev",
-    "cmgb_FastIInsideScan_dev", "cmgb_count_cells", "cmgb_autotune",
+    "cmgb_FastIInsideScan_dev", "cmgb_count_cells", "cmgb_autotune", "cmgb_FastCYKScan_noalloc",
 ]
 
 _SCAN_ARGS = [P, P, ctypes.c_char_p, I, P, I64, I64, F, P, I, F, P, P, P, P]
@@ -86,6 +86,9 @@ def bind(path: str) -> ctypes.CDLL:
         f.restype = I
     lib.cmgb_autotune.argtypes = [P, P, I, I, I64, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.c_char_p]
     lib.cmgb_autotune.restype = I
+    lib.cmgb_FastCYKScan_noalloc.argtypes = [P, P, ctypes.c_char_p, I, P, I64, I64, F, F, P, I, ctypes.POINTER(I),
+                                             ctypes.POINTER(I64), ctypes.POINTER(I64), ctypes.POINTER(F)]
+    lib.cmgb_FastCYKScan_noalloc.restype = I
     lib.cmgb_count_cells.argtypes = [P, I, I64]
     lib.cmgb_count_cells.restype = I64
     lib.cmgb_logsum_init()
