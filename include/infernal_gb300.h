@@ -160,7 +160,7 @@ void cmgb_model_destroy(cmgb_model *model);
 
 /* Autotuner: times candidate shapes (tile rows = rolling-row depth, and
  * shared- vs global-memory tiles) for band set qdbidx and algo (0 CYK,
- * 1 integer Inside) on a seeded iid sample of sample_len residues (0: a size
+ * 1 integer Inside, 2 float Inside) on a seeded iid sample of sample_len residues (0: a size
  * that fills the device) and stores the fastest in the model; scans on a
  * context whose tile_rows is 0 use it.  Returns the choice when the
  * pointers are non-NULL. */
@@ -194,6 +194,13 @@ int cmgb_FastIInsideScan(cmgb_ctx *ctx, cmgb_model *model, char *errbuf, int qdb
                          cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
                          int64_t *ret_envi, int64_t *ret_envj, float *ret_vsc, float *ret_sc);
 
+/* Replaces FastFInsideScan() (src/cm_dpsearch.c:1731-2320): Inside over float
+ * scores with the FLogsum table (src/logsum.c:160-168). */
+int cmgb_FastFInsideScan(cmgb_ctx *ctx, cmgb_model *model, char *errbuf, int qdbidx,
+                         const uint8_t *dsq, int64_t i0, int64_t j0, float cutoff,
+                         cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
+                         int64_t *ret_envi, int64_t *ret_envj, float *ret_vsc, float *ret_sc);
+
 /* Same scans with the residues already resident in device memory:
  * d_dsq points at a device copy of dsq[0..j0+1] (same indexing as dsq). */
 int cmgb_FastCYKScan_dev(cmgb_ctx *ctx, cmgb_model *model, char *errbuf, int qdbidx,
@@ -201,6 +208,10 @@ int cmgb_FastCYKScan_dev(cmgb_ctx *ctx, cmgb_model *model, char *errbuf, int qdb
                          cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
                          int64_t *ret_envi, int64_t *ret_envj, float *ret_vsc, float *ret_sc);
 int cmgb_FastIInsideScan_dev(cmgb_ctx *ctx, cmgb_model *model, char *errbuf, int qdbidx,
+                             const uint8_t *d_dsq, int64_t i0, int64_t j0, float cutoff,
+                             cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
+                             int64_t *ret_envi, int64_t *ret_envj, float *ret_vsc, float *ret_sc);
+int cmgb_FastFInsideScan_dev(cmgb_ctx *ctx, cmgb_model *model, char *errbuf, int qdbidx,
                              const uint8_t *d_dsq, int64_t i0, int64_t j0, float cutoff,
                              cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
                              int64_t *ret_envi, int64_t *ret_envj, float *ret_vsc, float *ret_sc);

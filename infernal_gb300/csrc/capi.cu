@@ -30,7 +30,7 @@ using namespace cmgb;
 
 #ifdef CMGB_HOST_EMULATION
 static const int kDefaultThreads = CMGB_EMU_THREADS;
-template <bool INS, bool GL>
+template <int ALG, bool GL>
 static void launch_qdb(int grid, int nt, size_t smem, cudaStream_t, const KParams &kp)
 {
   std::vector<std::vector<float>> sm(grid, std::vector<float>(smem / 4 + 16));
@@ -43,7 +43,7 @@ static void launch_qdb(int grid, int nt, size_t smem, cudaStream_t, const KParam
     for (int t = 0; t < nt; t++)
       th.emplace_back([&, b, t] {
         cmgb_emu_bar = bars[b]; cmgb_emu_warp = warps[b * (nt / 32) + t / 32]; cmgb_emu_lane = t & 31;
-        qdb_scan_body<INS, GL>(kp, sm[b].data(), t, nt, b);
+        qdb_scan_body<ALG, GL>(kp, sm[b].data(), t, nt, b);
       });
   for (auto &x : th) x.join();
   for (auto *b : bars) delete b;
@@ -51,20 +51,46 @@ static void launch_qdb(int grid, int nt, size_t smem, cudaStream_t, const KParam
 }
 #else
 static const int kDefaultThreads = 512;
-template <bool INS, bool GL>
+template <int ALG, bool GL>
 static void launch_qdb(int grid, int nt, size_t smem, cudaStream_t s, const KParams &kp)
 {
-  qdb_scan_kernel<INS, GL><<<grid, nt, smem, s>>>(kp);
+  qdb_scan_kernel<ALG, GL><<<grid, nt, smem, s>>>(kp);
 }
-template <bool INS, bool GL>
+template <int ALG, bool GL>
 static cudaError_t prepare_qdb(int nt, int smem, int *blocks_per_sm)
 {
-  cudaError_t e = cudaFuncSetAttribute(qdb_scan_kernel<INS, GL>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaError_t e = cudaFuncSetAttribute(qdb_scan_kernel<ALG, GL>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, qdb_scan_kernel<INS, GL>, nt, smem);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, qdb_scan_kernel<ALG, GL>, nt, smem);
 }
 #endif
 static const int kCandCap = 1 << 22;
+
+// Runtime dispatch over (algorithm, tile placement) to the kernel instantiations.
+#ifndef CMGB_HOST_EMULATION
+static cudaError_t prepare_any(int alg, bool gl, int nt, int smem, int *nb)
+{
+  switch (alg * 2 + (gl ? 1 : 0)) {
+  case 0: return prepare_qdb<0, false>(nt, smem, nb);
+  case 1: return prepare_qdb<0, true>(nt, smem, nb);
+  case 2: return prepare_qdb<1, false>(nt, smem, nb);
+  case 3: return prepare_qdb<1, true>(nt, smem, nb);
+  case 4: return prepare_qdb<2, false>(nt, smem, nb);
+  default: return prepare_qdb<2, true>(nt, smem, nb);
+  }
+}
+#endif
+static void launch_any(int alg, bool gl, int grid, int nt, size_t smem, cudaStream_t s, const KParams &kp)
+{
+  switch (alg * 2 + (gl ? 1 : 0)) {
+  case 0: launch_qdb<0, false>(grid, nt, smem, s, kp); break;
+  case 1: launch_qdb<0, true>(grid, nt, smem, s, kp); break;
+  case 2: launch_qdb<1, false>(grid, nt, smem, s, kp); break;
+  case 3: launch_qdb<1, true>(grid, nt, smem, s, kp); break;
+  case 4: launch_qdb<2, false>(grid, nt, smem, s, kp); break;
+  default: launch_qdb<2, true>(grid, nt, smem, s, kp); break;
+  }
+}
 
 struct Control {            // device control block, zeroed/initialised per scan
   int queue;
@@ -100,8 +126,8 @@ struct cmgb_model_s {
   cmgb_model_desc desc;      // points into the vectors above
   float *d_oesc = nullptr;
   int *d_ioesc = nullptr;
-  DevPlan plans[3][2];       // [qdbidx][0: CYK, 1: integer Inside]
-  int tuned_T[3][2] = {{0}}, tuned_arena[3][2] = {{0}};   // autotuner's choice (0: none yet)
+  DevPlan plans[3][3];       // [qdbidx][algorithm: 0 CYK, 1 integer Inside, 2 float Inside]
+  int tuned_T[3][3] = {{0}}, tuned_arena[3][3] = {{0}};   // autotuner's choice (0: none yet)
 };
 
 struct cmgb_ctx_s {
@@ -123,6 +149,7 @@ struct cmgb_ctx_s {
   Control *d_ctl = nullptr;
   unsigned *d_vsc = nullptr; int vsc_len = 0;
   int *d_ilog = nullptr;
+  float *d_flog = nullptr;
   Control *h_ctl = nullptr;       // pinned
   std::vector<CandHost> h_cand;
 };
@@ -164,6 +191,10 @@ extern "C" int cmgb_ctx_create(int device, cmgb_ctx **ret, char *errbuf)
   logsum_tables(nullptr, &ilog);
   CUDA_TRY(cudaMalloc(&c->d_ilog, sizeof(int) * 23000));
   CUDA_TRY(cudaMemcpy(c->d_ilog, ilog, sizeof(int) * 23000, cudaMemcpyHostToDevice));
+  const float *flog;
+  logsum_tables(&flog, nullptr);
+  CUDA_TRY(cudaMalloc(&c->d_flog, sizeof(float) * 23000));
+  CUDA_TRY(cudaMemcpy(c->d_flog, flog, sizeof(float) * 23000, cudaMemcpyHostToDevice));
   *ret = c.release();
   return CMGB_OK;
 }
@@ -173,7 +204,7 @@ extern "C" void cmgb_ctx_destroy(cmgb_ctx *c)
   if (!c) return;
   cudaSetDevice(c->device);
   cudaFree(c->d_carry); cudaFree(c->d_ring); cudaFree(c->d_arena); cudaFree(c->d_dsq); cudaFree(c->d_cand);
-  cudaFree(c->d_ctl); cudaFree(c->d_vsc); cudaFree(c->d_ilog);
+  cudaFree(c->d_ctl); cudaFree(c->d_vsc); cudaFree(c->d_ilog); cudaFree(c->d_flog);
   cudaFreeHost(c->h_ctl);
   cudaEventDestroy(c->ev0); cudaEventDestroy(c->ev1);
   cudaStreamDestroy(c->stream);
@@ -265,13 +296,13 @@ extern "C" void cmgb_hitlist_clear(cmgb_hitlist *hl) { if (hl) hl->h.clear(); }
 
 // Builds (once) the plan of band set qdbidx for the context's tile size,
 // shrinking the tile until its shared memory fits the device.
-static int get_plan(cmgb_model *m, int qdbidx, bool ins, DevPlan **ret, char *errbuf)
+static int get_plan(cmgb_model *m, int qdbidx, int alg, DevPlan **ret, char *errbuf)
 {
   cmgb_ctx *c = m->ctx;
-  DevPlan &dp = m->plans[qdbidx][ins ? 1 : 0];
+  DevPlan &dp = m->plans[qdbidx][alg];
   // shape: the context's explicit choice, else the autotuner's, else 16 rows in shared memory
-  const int wantT = c->tile_rows ? c->tile_rows : (m->tuned_T[qdbidx][ins] ? m->tuned_T[qdbidx][ins] : 16);
-  const int wantA = c->tile_rows ? c->arena : (m->tuned_T[qdbidx][ins] ? m->tuned_arena[qdbidx][ins] : c->arena);
+  const int wantT = c->tile_rows ? c->tile_rows : (m->tuned_T[qdbidx][alg] ? m->tuned_T[qdbidx][alg] : 16);
+  const int wantA = c->tile_rows ? c->arena : (m->tuned_T[qdbidx][alg] ? m->tuned_arena[qdbidx][alg] : c->arena);
   if (dp.built && dp.T == wantT && dp.nt == c->threads && dp.arena == wantA) { *ret = &dp; return CMGB_OK; }
   if (dp.d_states) { cudaFree(dp.d_states); dp.d_states = nullptr; }
   if (dp.d_rec) { cudaFree(dp.d_rec); dp.d_rec = nullptr; }
@@ -281,16 +312,16 @@ static int get_plan(cmgb_model *m, int qdbidx, bool ins, DevPlan **ret, char *er
     po = PlanOut();
     // arena: 1 shared memory, 2 global memory, 0 shared when it fits the device, else global
     bool gl = wantA == 2;
-    if (!build_plan(&m->desc, qdbidx, T, c->threads, ins, gl, &po)) ERRF(CMGB_EINCOMPAT, "%s", po.err.c_str());
+    if (!build_plan(&m->desc, qdbidx, T, c->threads, alg == 1, gl, &po)) ERRF(CMGB_EINCOMPAT, "%s", po.err.c_str());
     if (!gl && wantA == 0 && po.plan.smem_bytes + 64 > c->max_smem_optin) {
       po = PlanOut();
-      if (!build_plan(&m->desc, qdbidx, T, c->threads, ins, true, &po)) ERRF(CMGB_EINCOMPAT, "%s", po.err.c_str());
+      if (!build_plan(&m->desc, qdbidx, T, c->threads, alg == 1, true, &po)) ERRF(CMGB_EINCOMPAT, "%s", po.err.c_str());
     }
     if (po.plan.smem_bytes + 64 <= c->max_smem_optin) break;
     if (T <= 2) ERRF(CMGB_ERANGE, "model needs %d bytes of shared memory per CTA even with 2-row tiles", po.plan.smem_bytes);
     T = T > 8 ? T - 4 : T - 2;
   }
-  build_records(&m->desc, ins, &po);
+  build_records(&m->desc, alg == 1, &po);
   CUDA_TRY(cudaMalloc(&dp.d_rec, po.records.size()));
   CUDA_TRY(cudaMemcpy(dp.d_rec, po.records.data(), po.records.size(), cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMalloc(&dp.d_states, sizeof(StateInfo) * po.phases.size()));
@@ -307,12 +338,12 @@ static int get_plan(cmgb_model *m, int qdbidx, bool ins, DevPlan **ret, char *er
 // Common driver of the standard scanners.  dev_dsq: device residues indexed
 // by sequence coordinate (may be shifted); host_dsq: host residues (for
 // NULL3), may be NULL when do_null3 is FALSE or the device copy suffices.
-static int scan_std(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, bool ins,
+static int scan_std(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, int alg,
                     const uint8_t *host_dsq, const uint8_t *dev_dsq_in, int64_t i0, int64_t j0,
                     float cutoff, cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
                     int64_t *ret_envi, int64_t *ret_envj, float *ret_vsc, float *ret_sc)
 {
-  const char *fn = ins ? "FastIInsideScan" : "FastCYKScan";
+  const char *fn = alg == 1 ? "FastIInsideScan" : alg == 2 ? "FastFInsideScan" : "FastCYKScan";
   if (!c || !m) ERRF(CMGB_EINVAL, "%s, NULL context or model", fn);
   if (j0 < i0) ERRF(CMGB_EINCOMPAT, "%s, i0: %lld j0: %lld", fn, (long long) i0, (long long) j0);
   if (i0 < 1) ERRF(CMGB_EINCOMPAT, "%s, i0 must be >= 1", fn);
@@ -321,7 +352,7 @@ static int scan_std(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, bool i
   int st;
   CUDA_TRY(cudaSetDevice(c->device));
   DevPlan *dp;
-  if ((st = get_plan(m, qdbidx, ins, &dp, errbuf)) != CMGB_OK) return st;
+  if ((st = get_plan(m, qdbidx, alg, &dp, errbuf)) != CMGB_OK) return st;
   const ScanPlan &P = dp->plan;
   const int64_t L = j0 - i0 + 1;
   const int W = m->W;
@@ -346,8 +377,7 @@ static int scan_std(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, bool i
   if (cps == 0) {
 #ifndef CMGB_HOST_EMULATION
     int nb = 1;
-    if (ins) { if (gl) CUDA_TRY((prepare_qdb<true, true>(c->threads, P.smem_bytes, &nb))); else CUDA_TRY((prepare_qdb<true, false>(c->threads, P.smem_bytes, &nb))); }
-    else     { if (gl) CUDA_TRY((prepare_qdb<false, true>(c->threads, P.smem_bytes, &nb))); else CUDA_TRY((prepare_qdb<false, false>(c->threads, P.smem_bytes, &nb))); }
+    CUDA_TRY(prepare_any(alg, gl, c->threads, P.smem_bytes, &nb));
     cps = nb < 1 ? 1 : nb;
 #else
     cps = 1;
@@ -384,7 +414,7 @@ static int scan_std(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, bool i
   KParams kp;
   std::memset(&kp, 0, sizeof(kp));
   kp.st = dp->d_states; kp.plan = P; kp.rec = dp->d_rec; kp.arena = c->d_arena;
-  kp.oesc = m->d_oesc; kp.ioesc = m->d_ioesc; kp.ilog = c->d_ilog;
+  kp.oesc = m->d_oesc; kp.ioesc = m->d_ioesc; kp.ilog = c->d_ilog; kp.flog = c->d_flog;
   kp.dsq = d_dsq; kp.i0 = i0; kp.j0 = j0; kp.win_len = win; kp.nwin = (int) nwin;
   kp.queue = &c->d_ctl->queue; kp.carry = c->d_carry; kp.ring = c->d_ring;
   kp.cand = c->d_cand; kp.ncand = &c->d_ctl->ncand; kp.cand_cap = kCandCap;
@@ -398,13 +428,11 @@ static int scan_std(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, bool i
 #ifndef CMGB_HOST_EMULATION
   {
     int nb_unused = 0;
-    if (ins) { if (gl) CUDA_TRY((prepare_qdb<true, true>(c->threads, P.smem_bytes, &nb_unused))); else CUDA_TRY((prepare_qdb<true, false>(c->threads, P.smem_bytes, &nb_unused))); }
-    else     { if (gl) CUDA_TRY((prepare_qdb<false, true>(c->threads, P.smem_bytes, &nb_unused))); else CUDA_TRY((prepare_qdb<false, false>(c->threads, P.smem_bytes, &nb_unused))); }
+    CUDA_TRY(prepare_any(alg, gl, c->threads, P.smem_bytes, &nb_unused));
   }
 #endif
   CUDA_TRY(cudaEventRecord(c->ev0, c->stream));
-  if (ins) { if (gl) launch_qdb<true, true>(grid, c->threads, smem, c->stream, kp); else launch_qdb<true, false>(grid, c->threads, smem, c->stream, kp); }
-  else     { if (gl) launch_qdb<false, true>(grid, c->threads, smem, c->stream, kp); else launch_qdb<false, false>(grid, c->threads, smem, c->stream, kp); }
+  launch_any(alg, gl, grid, c->threads, smem, c->stream, kp);
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaEventRecord(c->ev1, c->stream));
   CUDA_TRY(cudaMemcpyAsync(h, c->d_ctl, sizeof(Control), cudaMemcpyDeviceToHost, c->stream));
@@ -450,37 +478,52 @@ extern "C" int cmgb_FastCYKScan(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qd
                                 float *vsc, float *sc)
 {
   if (dsq == nullptr) ERRF(CMGB_EINCOMPAT, "FastCYKScan, dsq is NULL");
-  return scan_std(c, m, errbuf, qdbidx, false, dsq, nullptr, i0, j0, cutoff, hl, do_null3, env_cutoff, envi, envj, vsc, sc);
+  return scan_std(c, m, errbuf, qdbidx, 0, dsq, nullptr, i0, j0, cutoff, hl, do_null3, env_cutoff, envi, envj, vsc, sc);
 }
 extern "C" int cmgb_FastIInsideScan(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, const uint8_t *dsq, int64_t i0, int64_t j0,
                                     float cutoff, cmgb_hitlist *hl, int do_null3, float env_cutoff, int64_t *envi, int64_t *envj,
                                     float *vsc, float *sc)
 {
   if (dsq == nullptr) ERRF(CMGB_EINCOMPAT, "FastIInsideScan, dsq is NULL");
-  return scan_std(c, m, errbuf, qdbidx, true, dsq, nullptr, i0, j0, cutoff, hl, do_null3, env_cutoff, envi, envj, vsc, sc);
+  return scan_std(c, m, errbuf, qdbidx, 1, dsq, nullptr, i0, j0, cutoff, hl, do_null3, env_cutoff, envi, envj, vsc, sc);
 }
 extern "C" int cmgb_FastCYKScan_dev(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, const uint8_t *d_dsq, int64_t i0, int64_t j0,
                                     float cutoff, cmgb_hitlist *hl, int do_null3, float env_cutoff, int64_t *envi, int64_t *envj,
                                     float *vsc, float *sc)
 {
   if (d_dsq == nullptr) ERRF(CMGB_EINCOMPAT, "FastCYKScan, dsq is NULL");
-  return scan_std(c, m, errbuf, qdbidx, false, nullptr, d_dsq, i0, j0, cutoff, hl, do_null3, env_cutoff, envi, envj, vsc, sc);
+  return scan_std(c, m, errbuf, qdbidx, 0, nullptr, d_dsq, i0, j0, cutoff, hl, do_null3, env_cutoff, envi, envj, vsc, sc);
 }
 extern "C" int cmgb_FastIInsideScan_dev(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, const uint8_t *d_dsq, int64_t i0, int64_t j0,
                                         float cutoff, cmgb_hitlist *hl, int do_null3, float env_cutoff, int64_t *envi, int64_t *envj,
                                         float *vsc, float *sc)
 {
   if (d_dsq == nullptr) ERRF(CMGB_EINCOMPAT, "FastIInsideScan, dsq is NULL");
-  return scan_std(c, m, errbuf, qdbidx, true, nullptr, d_dsq, i0, j0, cutoff, hl, do_null3, env_cutoff, envi, envj, vsc, sc);
+  return scan_std(c, m, errbuf, qdbidx, 1, nullptr, d_dsq, i0, j0, cutoff, hl, do_null3, env_cutoff, envi, envj, vsc, sc);
+}
+
+extern "C" int cmgb_FastFInsideScan(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, const uint8_t *dsq, int64_t i0, int64_t j0,
+                                    float cutoff, cmgb_hitlist *hl, int do_null3, float env_cutoff, int64_t *envi, int64_t *envj,
+                                    float *vsc, float *sc)
+{
+  if (dsq == nullptr) ERRF(CMGB_EINCOMPAT, "FastFInsideScan, dsq is NULL");
+  return scan_std(c, m, errbuf, qdbidx, 2, dsq, nullptr, i0, j0, cutoff, hl, do_null3, env_cutoff, envi, envj, vsc, sc);
+}
+extern "C" int cmgb_FastFInsideScan_dev(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, const uint8_t *d_dsq, int64_t i0, int64_t j0,
+                                        float cutoff, cmgb_hitlist *hl, int do_null3, float env_cutoff, int64_t *envi, int64_t *envj,
+                                        float *vsc, float *sc)
+{
+  if (d_dsq == nullptr) ERRF(CMGB_EINCOMPAT, "FastFInsideScan, dsq is NULL");
+  return scan_std(c, m, errbuf, qdbidx, 2, nullptr, d_dsq, i0, j0, cutoff, hl, do_null3, env_cutoff, envi, envj, vsc, sc);
 }
 
 // Times candidate shapes (tile rows x arena placement) of band set qdbidx and
-// algorithm (0 CYK, 1 integer Inside) on a seeded iid sample and keeps the
+// algorithm (0 CYK, 1 integer Inside, 2 float Inside) on a seeded iid sample and keeps the
 // fastest for this model; later scans that leave the shape to the library use it.
 extern "C" int cmgb_autotune(cmgb_ctx *c, cmgb_model *m, int qdbidx, int algo, int64_t sample_len,
                              int *ret_tile_rows, int *ret_arena, char *errbuf)
 {
-  if (!c || !m || qdbidx < 0 || qdbidx > 2 || algo < 0 || algo > 1) ERRF(CMGB_EINVAL, "cmgb_autotune: invalid argument");
+  if (!c || !m || qdbidx < 0 || qdbidx > 2 || algo < 0 || algo > 2) ERRF(CMGB_EINVAL, "cmgb_autotune: invalid argument");
   if (sample_len <= 0) sample_len = (int64_t) c->nsm * 1500;
   std::vector<uint8_t> dsq((size_t) sample_len + 2);
   uint64_t x = 0x9E3779B97F4A7C15ULL;
@@ -498,8 +541,7 @@ extern "C" int cmgb_autotune(cmgb_ctx *c, cmgb_model *m, int qdbidx, int algo, i
     c->tile_rows = cd[0]; c->arena = cd[1];
     float ms = 0.f;
     for (int rep = 0; rep < 2 && st == CMGB_OK; rep++) {   // first run builds the plan and warms up
-      if (algo) st = cmgb_FastIInsideScan(c, m, errbuf, qdbidx, dsq.data(), 1, sample_len, 1e30f, nullptr, 0, 1e30f, nullptr, nullptr, nullptr, nullptr);
-      else      st = cmgb_FastCYKScan(c, m, errbuf, qdbidx, dsq.data(), 1, sample_len, 1e30f, nullptr, 0, 1e30f, nullptr, nullptr, nullptr, nullptr);
+      st = scan_std(c, m, errbuf, qdbidx, algo, dsq.data(), nullptr, 1, sample_len, 1e30f, nullptr, 0, 1e30f, nullptr, nullptr, nullptr, nullptr);
       ms = c->last_ms;
     }
     if (st != CMGB_OK) {           // a shape that does not fit this device is skipped

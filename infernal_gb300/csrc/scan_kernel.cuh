@@ -25,6 +25,7 @@
 // host-thread emulation of one CTA (CMGB_HOST_EMULATION), which is how the
 // indexing is checked on machines without a GPU.
 #pragma once
+#include <cmath>
 #include "scan_plan.h"
 
 #ifndef CMGB_HOST_EMULATION
@@ -109,6 +110,7 @@ struct KParams {
   const float *oesc;
   const int *ioesc;
   const int *ilog;            // ILogsum table (integer Inside)
+  const float *flog;          // FLogsum table (float Inside)
   const unsigned char *dsq;   // device residues, indexed by sequence coordinate
   long long i0, j0;           // scan range
   long long win_len;          // owned end positions per window
@@ -137,10 +139,11 @@ CMGB_DEV unsigned cmgb_f2u(float f)
   return (x.u & 0x80000000u) ? ~x.u : (x.u | 0x80000000u);
 }
 
-// Score semiring: CYK is (max, +) over float; integer Inside is
-// (ILogsum, +) over int (src/logsum.c:87-92).
-template <bool INS> struct Sr;
-template <> struct Sr<false> {
+// Score semirings, selected by ALG: 0 CYK (max, +) over float; 1 integer
+// Inside (ILogsum, +) over int (src/logsum.c:87-92); 2 float Inside
+// (FLogsum, +) over float (src/logsum.c:160-168).
+template <int ALG> struct Sr;
+template <> struct Sr<0> {
   typedef float T;
   static CMGB_DEV T imp() { return CMGB_IMP; }
   static CMGB_DEV T add(T a, T b) { return CMGB_FADD(a, b); }
@@ -161,7 +164,7 @@ template <> struct Sr<false> {
   static CMGB_DEV T esc(const KParams &p, int idx) { return CMGB_LDG(p.oesc + idx); }
   static CMGB_DEV T acc_init() { return -3.0e38f; }
 };
-template <> struct Sr<true> {
+template <> struct Sr<1> {
   typedef int T;
   static CMGB_DEV T imp() { return -CMGB_INF; }
   static CMGB_DEV T add(T a, T b) { return a + b; }
@@ -188,6 +191,31 @@ template <> struct Sr<true> {
   static CMGB_DEV T esc(const KParams &p, int idx) { return CMGB_LDG(p.ioesc + idx); }
   static CMGB_DEV T acc_init() { return (int) 0x80000000; }
 };
+template <> struct Sr<2> {
+  typedef float T;
+  static CMGB_DEV T imp() { return CMGB_IMP; }
+  static CMGB_DEV T add(T a, T b) { return CMGB_FADD(a, b); }
+  // tbl: the FLogsum table (float, in global memory), passed as the same pointer type
+  static CMGB_DEV T comb(T a, T b, const unsigned short *tblp) {
+    const float *tbl = reinterpret_cast<const float *>(tblp);
+    const float mx = a > b ? a : b, mn = a < b ? a : b;
+    if (mn == -INFINITY || CMGB_FADD(mx, -mn) >= 23.f) return mx;
+    return CMGB_FADD(mx, CMGB_LDG(tbl + (int) CMGB_FMUL(CMGB_FADD(mx, -mn), 1000.0f)));
+  }
+  static CMGB_DEV T rootfirst(T x) { return CMGB_IMP > x ? CMGB_IMP : x; }
+  static CMGB_DEV float score(T x) { return x; }
+  static CMGB_DEV float envval(T x) { return x; }
+  static CMGB_DEV T init_sc(const StateInfo &s, int d, float el, int) {
+    return s.has_end ? CMGB_FADD(CMGB_FMUL(el, CMGB_I2F(d)), s.endsc) : CMGB_IMP;
+  }
+  static CMGB_DEV T init_h(bool hasend, float endsc, int, int d, float el, int) {
+    return hasend ? CMGB_FADD(CMGB_FMUL(el, CMGB_I2F(d)), endsc) : CMGB_IMP;
+  }
+  static CMGB_DEV T init0(const StateInfo &s) { return s.init0; }
+  static CMGB_DEV T tsc(const StateInfo &s, int o) { return s.tsc[o]; }
+  static CMGB_DEV T beginsc(const StateInfo &s) { return s.beginsc; }
+  static CMGB_DEV T acc_init() { return -3.0e38f; }
+};
 
 // Flattened walk over the cells (r, d), r = 1..nrows, d = lo..hi, of one
 // phase: thread tid visits cells tid, tid + nt, ... in row-major order with
@@ -205,11 +233,12 @@ struct CellWalk {
   CMGB_DEV void next() { d += sdd; r += sr; if (d > hi) { d -= wp; r++; } }
 };
 
-template <bool INS, bool GL>
+template <int ALG, bool GL>
 CMGB_DEV void qdb_scan_body(const KParams &p, float *smf, int tid, int nt, int bid)
 {
-  typedef Sr<INS> R;
+  typedef Sr<ALG> R;
   typedef typename R::T T;
+  constexpr bool INS = ALG == 1;
   const ScanPlan &P = p.plan;
   const int W = P.W, TT = P.T, NP = P.nphase;
   const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
@@ -224,7 +253,8 @@ CMGB_DEV void qdb_scan_body(const KParams &p, float *smf, int tid, int nt, int b
   int *s_win = reinterpret_cast<int *>(smf) + P.smem_elems;   // one shared int past the plan's arena
   T *carry0 = reinterpret_cast<T *>(p.carry) + (size_t) bid * 2 * P.carry_elems;
   T *ringb = reinterpret_cast<T *>(p.ring) + (size_t) bid * P.ring_elems;
-  const unsigned short *tbl = reinterpret_cast<const unsigned short *>(smf + P.ltbl_off);
+  const unsigned short *tbl = ALG == 2 ? reinterpret_cast<const unsigned short *>(p.flog)
+                                        : reinterpret_cast<const unsigned short *>(smf + P.ltbl_off);
   if (INS) {
     unsigned short *t16 = reinterpret_cast<unsigned short *>(smf + P.ltbl_off);
     for (int q = tid; q < CMGB_LTBL; q += nt) t16[q] = (unsigned short) CMGB_LDG(p.ilog + q);
@@ -542,10 +572,10 @@ CMGB_DEV void qdb_scan_body(const KParams &p, float *smf, int tid, int nt, int b
 }
 
 #ifndef CMGB_HOST_EMULATION
-template <bool INS, bool GL>
+template <int ALG, bool GL>
 __global__ void __launch_bounds__(512) qdb_scan_kernel(KParams p)
 {
   extern __shared__ __align__(128) float smem_dyn[];
-  qdb_scan_body<INS, GL>(p, smem_dyn, threadIdx.x, blockDim.x, blockIdx.x);
+  qdb_scan_body<ALG, GL>(p, smem_dyn, threadIdx.x, blockDim.x, blockIdx.x);
 }
 #endif

@@ -33,6 +33,7 @@ EXPORTS = [
     "cmgb_hitlist_create", "cmgb_hitlist_destroy", "cmgb_hitlist_count", "cmgb_hitlist_get",
     "cmgb_hitlist_clear", "cmgb_FastCYKScan", "cmgb_FastIInsideScan", "cmgb_FastCYKScan_dev",
     "cmgb_FastIInsideScan_dev", "cmgb_count_cells", "cmgb_autotune", "cmgb_FastCYKScan_noalloc",
+    "cmgb_FastFInsideScan", "cmgb_FastFInsideScan_dev",
 ]
 
 _SCAN_ARGS = [P, P, ctypes.c_char_p, I, P, I64, I64, F, P, I, F, P, P, P, P]
@@ -80,7 +81,8 @@ def bind(path: str) -> ctypes.CDLL:
     lib.cmgb_hitlist_get.argtypes = [P, I64, ctypes.POINTER(Hit)]
     lib.cmgb_hitlist_get.restype = I
     lib.cmgb_hitlist_clear.argtypes = [P]
-    for name in ("cmgb_FastCYKScan", "cmgb_FastIInsideScan", "cmgb_FastCYKScan_dev", "cmgb_FastIInsideScan_dev"):
+    for name in ("cmgb_FastCYKScan", "cmgb_FastIInsideScan", "cmgb_FastCYKScan_dev", "cmgb_FastIInsideScan_dev",
+                 "cmgb_FastFInsideScan", "cmgb_FastFInsideScan_dev"):
         f = getattr(lib, name)
         f.argtypes = _SCAN_ARGS
         f.restype = I
@@ -161,11 +163,12 @@ class Scanner:
     def scan(self, m: cmfile.CMModel, dsq, i0: int, j0: int, algo: str = "cyk", qdbidx: int = 1,
              cutoff: float = 0.0, do_null3: bool = True, env_cutoff: float = 0.0, want_hits: bool = True,
              want_vsc: bool = False, notgreedy: bool = False, device_ptr: Optional[int] = None) -> ScanResult:
-        """Runs cmgb_FastCYKScan (algo="cyk") or cmgb_FastIInsideScan (algo="inside").
+        """Runs cmgb_FastCYKScan (algo="cyk"), cmgb_FastIInsideScan (algo="inside") or
+        cmgb_FastFInsideScan (algo="finside").
         dsq: numpy uint8 Easel digital sequence (dsq[0], dsq[L+1] sentinels);
         device_ptr: optional device address of the same array (the *_dev entry points)."""
         mh = self.model(m, CMGB_NOTGREEDY if notgreedy else 0)
-        fn = {"cyk": "cmgb_FastCYKScan", "inside": "cmgb_FastIInsideScan"}[algo]
+        fn = {"cyk": "cmgb_FastCYKScan", "inside": "cmgb_FastIInsideScan", "finside": "cmgb_FastFInsideScan"}[algo]
         if device_ptr is not None:
             fn += "_dev"
             dptr = device_ptr
@@ -199,7 +202,7 @@ class Scanner:
         mh = self.model(m, 0)
         t, a = I(), I()
         err = ctypes.create_string_buffer(256)
-        st = self.lib.cmgb_autotune(self._ctx, mh, qdbidx, 1 if algo == "inside" else 0, sample_len,
+        st = self.lib.cmgb_autotune(self._ctx, mh, qdbidx, {"cyk": 0, "inside": 1, "finside": 2}[algo], sample_len,
                                     ctypes.byref(t), ctypes.byref(a), err)
         if st != 0:
             raise ScanError(st, err.value.decode())

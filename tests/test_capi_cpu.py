@@ -76,7 +76,8 @@ def emu():
 
 @pytest.mark.parametrize("name,algo,qdb,T,win,arena", [
     ("tRNA", "cyk", 1, 4, 0, 1), ("tRNA", "inside", 2, 8, 0, 1), ("Vault", "cyk", 2, 16, 300, 1),
-    ("tRNA", "cyk", 0, 16, 0, 2), ("Plant_SRP", "inside", 1, 40, 0, 2), ("Vault", "inside", 2, 64, 250, 2)])
+    ("tRNA", "cyk", 0, 16, 0, 2), ("Plant_SRP", "inside", 1, 40, 0, 2), ("Vault", "inside", 2, 64, 250, 2),
+    ("tRNA", "finside", 2, 12, 0, 1)])
 def test_emulated_kernel_matches_oracle(emu, models, name, algo, qdb, T, win, arena):
     m = models[name]
     rng = np.random.default_rng(11)

@@ -34,9 +34,9 @@ def test_golden_on_gpu(gpu, golden, models, T, arena):
     gpu.set_shape(T, 0, 0, 0, arena)
     n = 0
     for c in meta:
-        if c["algo"] not in ("cyk", "refcyk", "inside"):
+        if c["algo"] not in ("cyk", "refcyk", "inside", "finside"):
             continue
-        algo = "inside" if c["algo"] == "inside" else "cyk"
+        algo = "cyk" if c["algo"] == "refcyk" else c["algo"]
         r = gpu.scan(models[c["model"]], arrays["dsq." + c["seq"]], c["i0"], c["j0"], algo=algo, qdbidx=c["qdbidx"],
                      cutoff=c["cutoff"], do_null3=bool(c["null3"]), env_cutoff=c["env_cutoff"],
                      notgreedy=bool(c["notgreedy"]), want_vsc=True)
@@ -47,7 +47,8 @@ def test_golden_on_gpu(gpu, golden, models, T, arena):
 
 
 @pytest.mark.parametrize("name,algo,qdb", [("tRNA", "cyk", 1), ("Vault", "cyk", 1), ("Plant_SRP", "cyk", 1),
-                                           ("tRNA", "inside", 2), ("Vault", "inside", 2), ("Plant_SRP", "inside", 2)])
+                                           ("tRNA", "inside", 2), ("Vault", "inside", 2), ("Plant_SRP", "inside", 2),
+                                           ("Vault", "finside", 2)])
 def test_random_targets_vs_oracle(gpu, models, name, algo, qdb):
     m = models[name]
     rng = np.random.default_rng(hash((name, algo)) & 0xffff)
