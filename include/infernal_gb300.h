@@ -67,17 +67,33 @@ extern "C" {
 #define CMGB_INFTY      987654321
 #define CMGB_LOGSUM_TBL 23000
 
-/* Truncated-pass indices (PLI_PASS_*, src/infernal.h:2097-2104). */
-#define CMGB_PASS_STD_ANY         0
+/* Pipeline pass indices (PLI_PASS_*, src/infernal.h:2097-2103); the
+ * truncated scanners accept passes 2..5 (cm_TrFillFromPassIdx,
+ * src/cm_dpsearch_trunc.c:3566). */
+#define CMGB_PASS_STD_ANY         1
 #define CMGB_PASS_5P_ONLY_FORCE   2
 #define CMGB_PASS_3P_ONLY_FORCE   3
 #define CMGB_PASS_5P_AND_3P_FORCE 4
+#define CMGB_PASS_5P_AND_3P_ANY   5
+#define CMGB_PASS_HMM_ONLY_ANY    6
 
 /* Truncation modes of a hit (TRMODE_*, src/infernal.h). */
 #define CMGB_TRMODE_J 3
 #define CMGB_TRMODE_L 2
 #define CMGB_TRMODE_R 1
 #define CMGB_TRMODE_T 0
+#define CMGB_TRMODE_UNKNOWN 4
+
+/* Node types (src/infernal.h:209-216). */
+#define CMGB_BIF_nd  0
+#define CMGB_MATP_nd 1
+#define CMGB_MATL_nd 2
+#define CMGB_MATR_nd 3
+#define CMGB_BEGL_nd 4
+#define CMGB_BEGR_nd 5
+#define CMGB_ROOT_nd 6
+#define CMGB_END_nd  7
+#define CMGB_END_E   18   /* unique state id of END_E: the state after a detached insert */
 
 /* Flat view of a configured CM_t: exactly the fields the scanners read.
  * Per-state tables are indexed [v] for v in 0..M-1; tsc/itsc have a fixed
@@ -118,6 +134,8 @@ typedef struct {
   const int   *emap_lpos;  /* [nodes] cm->emap->lpos */
   const int   *emap_rpos;  /* [nodes] cm->emap->rpos */
   int          clen;       /* cm->clen */
+  const int8_t *ndtype;    /* [nodes] cm->ndtype[nd] (read by the truncated hit filter) */
+  int          nodes;      /* cm->nodes */
 } cmgb_model_desc;
 
 /* One hit (the fields of CM_HIT that the scanners set, src/infernal.h:2424). */

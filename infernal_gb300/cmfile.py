@@ -198,6 +198,13 @@ class CMModel:
     rmesc: np.ndarray = None
     ilmesc: np.ndarray = None
     irmesc: np.ndarray = None
+    # truncated scanning (truncation_tables)
+    emap_lpos: np.ndarray = None
+    emap_rpos: np.ndarray = None
+    tr_g_pty: np.ndarray = None
+    tr_l_pty: np.ndarray = None
+    tr_ig_pty: np.ndarray = None
+    tr_il_pty: np.ndarray = None
     configured: bool = False
     ecm: Dict[str, tuple] = field(default_factory=dict)
 
@@ -530,12 +537,191 @@ def configure(m: CMModel, local: bool = True) -> CMModel:
                     ioesc[v, a * Kp + b] = int(math.floor(0.5 + float(f32(INTSCALE * oesc[v, a * Kp + b]))))
     m.oesc, m.ioesc = oesc, ioesc
     m.configured = True
+    if m.t_global is not None and m.plast is not None:
+        truncation_tables(m)
     return m
 
 
 def load(path: str, which: int = 0, local: bool = True) -> CMModel:
     """Read and configure a CM for scanning."""
-    return configure(read_cm(path, which), local=local)
+    return truncation_tables(configure(read_cm(path, which), local=local))
+
+
+# ---- truncated-scan tables ----------------------------------------------------
+def emit_map(m: CMModel):
+    """Consensus coordinates of every node: CreateEmitMap (src/display.c:1110).
+    A depth-first walk of the guide tree counts consensus columns; lpos[nd] is
+    the column at the node's left side, rpos[nd] one past its right side.
+    Returns (lpos, rpos) as int32 arrays of length ``nodes``."""
+    lpos = np.full(m.nodes, -1, np.int32)
+    rpos = np.full(m.nodes, -1, np.int32)
+    cpos = 0
+    stack = [(0, False)]
+    while stack:
+        nd, on_right = stack.pop()
+        t = int(m.ndtype[nd])
+        if on_right:
+            rpos[nd] = cpos + 1
+            if t in (MATP_nd, MATR_nd):
+                cpos += 1
+            continue
+        if t in (MATP_nd, MATL_nd):
+            cpos += 1
+        lpos[nd] = cpos
+        stack.append((nd, True))
+        if t == BIF_nd:
+            v = int(m.nodemap[nd])
+            stack.append((int(m.ndidx[m.cnum[v]]), False))     # right subtree, visited second
+            stack.append((int(m.ndidx[m.cfirst[v]]), False))   # left subtree, visited first
+        elif t != END_nd:
+            stack.append((nd + 1, False))
+    if (lpos < 0).any() or (rpos < 0).any():
+        raise ValueError("emit map: unreachable node")
+    return lpos, rpos
+
+
+def _detached(m: CMModel, v: int) -> bool:
+    """StateIsDetached (src/cm.c:1775): the state just before an END_E."""
+    return v + 1 < m.M and int(m.stid[v + 1]) == END_E
+
+
+def state_occupancy(m: CMModel) -> np.ndarray:
+    """Expected number of visits of each state in a global parse,
+    cm_ExpectedStateOccupancy (src/cm.c:4250-4330), over the transitions
+    before local configuration.  A parent x reaches child v through its
+    transition v - cfirst[x]; an insert adds its self-loop's geometric
+    series.  Double precision, as the reference."""
+    t = m.t_global
+    psi = np.zeros(m.M, np.float64)
+    for v in range(m.M):
+        st = int(m.sttype[v])
+        if st == S_st:
+            psi[v] = 1.0
+            continue
+        ins = st in (IL_st, IR_st)
+        acc = 0.0
+        for y in range(int(m.pnum[v]) - 1, (1 if ins else 0) - 1, -1):
+            x = int(m.plast[v]) - y
+            acc += psi[x] * float(t[x, v - int(m.cfirst[x])])
+        if ins:
+            acc += acc * (float(t[v, 0]) / (1.0 - float(t[v, 0])))
+        psi[v] = acc
+    return psi
+
+
+def _inserts_of_node(m: CMModel, nd: int):
+    """InsertsGivenNodeIndex (src/cm.c:4897): insert states of node nd."""
+    v = int(m.nodemap[nd])
+    t = int(m.ndtype[nd])
+    if t == MATP_nd:
+        return v + 4, v + 5
+    if t in (MATL_nd, MATR_nd):
+        return v + 2, -1
+    if t == BEGR_nd:
+        return v + 1, -1
+    if t == ROOT_nd:
+        return v + 1, v + 2
+    return -1, -1
+
+
+def truncation_tables(m: CMModel) -> CMModel:
+    """Truncated-begin penalties and emit map of a CM: cm_tr_penalties_Create
+    (src/cm_trunc.c:51-440) with cm_CalculateLocalBeginProbs
+    (src/cm_modelconfig.c:397) and CreateEmitMap (src/display.c:1110).
+
+    Fills m.emap_lpos/emap_rpos and the [3, M] tables tr_g_pty, tr_l_pty
+    (float, log2 probabilities, IMPOSSIBLE where no truncated begin is
+    allowed) and tr_ig_pty, tr_il_pty (integer scores, -INFTY), indexed
+    [pty_idx][v] with pty_idx 0 = 5' and 3', 1 = 5' only, 2 = 3' only.
+    The penalties are probabilities until the final conversion; states the
+    conversion skips (detached inserts) keep their probability in the float
+    tables, as the reference does."""
+    if getattr(m, "tr_g_pty", None) is not None:
+        return m
+    M = m.M
+    lpos_map, rpos_map = emit_map(m)
+    m.emap_lpos, m.emap_rpos = lpos_map, rpos_map
+    psi = state_occupancy(m)
+    # local begin probabilities from pbegin (cm_CalculateLocalBeginProbs)
+    internal = (MATP_nd, MATL_nd, MATR_nd, BIF_nd)
+    nstarts = sum(1 for nd in range(2, m.nodes) if m.ndtype[nd] in internal)
+    begin = np.zeros(M, np.float32)
+    begin[m.nodemap[1]] = f32(1.0 - float(m.pbegin))
+    pb = f32(f32(m.pbegin) / f32(nstarts))
+    for nd in range(2, m.nodes):
+        if m.ndtype[nd] in internal:
+            begin[m.nodemap[nd]] = pb
+    P53, P5, P3 = 0, 1, 2
+    g = np.full((3, M), f32(IMPOSSIBLE), np.float32)
+    l = np.full((3, M), f32(IMPOSSIBLE), np.float32)
+    g_5and3 = f32(2.0 / (m.clen * (m.clen + 1)))
+    g_5or3 = f32(1.0 / m.clen)
+    prv5 = prv3 = prv53 = f32(0.0)
+    for nd in range(m.nodes):
+        t = int(m.ndtype[nd])
+        lpos = int(lpos_map[nd]) if t in (MATP_nd, MATL_nd) else int(lpos_map[nd]) + 1
+        rpos = int(rpos_map[nd]) if t in (MATP_nd, MATR_nd) else int(rpos_map[nd]) - 1
+        if t == END_nd:
+            prv5 = prv3 = prv53 = f32(0.0)
+        elif t in (BEGL_nd, BEGR_nd):
+            b = int(m.plast[m.nodemap[nd]])          # the parent bifurcation
+            prv5 = f32(0.0) if t == BEGL_nd else l[P5, b]
+            prv3 = f32(0.0) if t == BEGR_nd else l[P3, b]
+            prv53 = l[P53, b]
+        elif t in internal:
+            s = int(m.nodemap[nd])
+            i1, i2 = _inserts_of_node(m, nd - 1)
+            # (the reference's extra MATP pair-state term compares a node type
+            # with a state id and never applies, so m_psi is psi[s] alone)
+            m_psi = f32(psi[s])
+            i1_psi = f32(psi[i1]) if i1 != -1 else f32(0.0)
+            i2_psi = f32(psi[i2]) if i2 != -1 else f32(0.0)
+            summed = f32(f32(m_psi + i1_psi) + i2_psi)
+            shares = [(s, f32(m_psi / summed))]
+            if i1 != -1:
+                shares.append((i1, f32(i1_psi / summed)))
+            if i2 != -1:
+                shares.append((i2, f32(i2_psi / summed)))
+            for x, w in shares:
+                if g[P53, x] > -9.999e35 or l[P53, x] > -9.999e35:
+                    raise ValueError(f"truncation penalty of state {x} set twice")
+                g[P53, x] = f32(w * g_5and3)
+                if rpos == m.clen:
+                    g[P5, x] = f32(w * g_5or3)
+                if lpos == 1:
+                    g[P3, x] = f32(w * g_5or3)
+            sub = rpos - lpos + 1
+            nfrag53 = (sub * (sub + 1)) // 2
+            cur5 = f32(f32(begin[s] / f32(sub)) + prv5)
+            cur3 = f32(f32(begin[s] / f32(sub)) + prv3)
+            cur53 = f32(f32(begin[s] / f32(nfrag53)) + prv53)
+            for x, w in shares:
+                l[P53, x] = f32(w * cur53)
+                l[P5, x] = f32(w * cur5)
+                l[P3, x] = f32(w * cur3)
+            prv5 = cur5 if t == MATL_nd else f32(0.0)
+            prv3 = cur3 if t == MATR_nd else f32(0.0)
+            prv53 = cur53
+    ig = np.full((3, M), -INFTY, np.int32)
+    il = np.full((3, M), -INFTY, np.int32)
+    for v in range(M):
+        sid, st = int(m.stid[v]), int(m.sttype[v])
+        if not (sid in (MATP_MP, MATL_ML, MATR_MR, BIF_B) or (st in (IL_st, IR_st) and not _detached(m, v))):
+            continue
+        if sid == MATP_IL and int(m.ndtype[int(m.ndidx[v]) + 1]) == END_nd:
+            continue
+        if not g[P53, v] > -9.999e35:
+            raise ValueError(f"state {v}: missing global truncation penalty")
+        for p in (P53, P5, P3):
+            if g[p, v] > -9.999e35:
+                ig[p, v] = Prob2Score(g[p, v], 1.0)
+                g[p, v] = f32(sreLOG2(g[p, v]))
+            if not l[p, v] > -9.999e35:
+                raise ValueError(f"state {v}: missing local truncation penalty")
+            il[p, v] = Prob2Score(l[p, v], 1.0)
+            l[p, v] = f32(sreLOG2(l[p, v]))
+    m.tr_g_pty, m.tr_l_pty, m.tr_ig_pty, m.tr_il_pty = g, l, ig, il
+    return m
 
 
 # ---- ctypes view of cmgb_model_desc -----------------------------------------
@@ -553,7 +739,8 @@ class ModelDesc(ctypes.Structure):
                 ("null", _p), ("null3_omega", ctypes.c_float),
                 ("lmesc", _p), ("rmesc", _p), ("ilmesc", _p), ("irmesc", _p),
                 ("tr_g_pty", _p), ("tr_l_pty", _p), ("tr_ig_pty", _p), ("tr_il_pty", _p),
-                ("ndidx", _p), ("emap_lpos", _p), ("emap_rpos", _p), ("clen", ctypes.c_int)]
+                ("ndidx", _p), ("emap_lpos", _p), ("emap_rpos", _p), ("clen", ctypes.c_int),
+                ("ndtype", _p), ("nodes", ctypes.c_int)]
 
 
 def make_desc(m: CMModel, flags_extra: int = 0, keep: Optional[list] = None) -> ModelDesc:
@@ -586,6 +773,12 @@ def make_desc(m: CMModel, flags_extra: int = 0, keep: Optional[list] = None) -> 
     d.ilmesc, d.irmesc = ptr(m.ilmesc, np.int32), ptr(m.irmesc, np.int32)
     d.ndidx = ptr(m.ndidx, np.int32)
     d.clen = m.clen
+    if getattr(m, "tr_g_pty", None) is not None:
+        d.tr_g_pty, d.tr_l_pty = ptr(m.tr_g_pty, np.float32), ptr(m.tr_l_pty, np.float32)
+        d.tr_ig_pty, d.tr_il_pty = ptr(m.tr_ig_pty, np.int32), ptr(m.tr_il_pty, np.int32)
+        d.emap_lpos, d.emap_rpos = ptr(m.emap_lpos, np.int32), ptr(m.emap_rpos, np.int32)
+    d.ndtype = ptr(m.ndtype, np.int8)
+    d.nodes = m.nodes
     d._keep = keep
     return d
 
@@ -621,4 +814,6 @@ def load_npz(path: str) -> CMModel:
     for s in _F32:
         setattr(m, s, f32(z[s]))
     m.configured = True
+    if m.t_global is not None and m.plast is not None:
+        truncation_tables(m)
     return m

@@ -63,6 +63,12 @@ def _load(path):
         if hasattr(lib, "oracle_scan"):
             lib.oracle_scan.argtypes = [P, I, I, P, I64, I64, F, I, F, I, P, I64, P, P, P, P, P, P]
             lib.oracle_scan.restype = I
+        if hasattr(lib, "oracle_tr_scan"):
+            lib.oracle_tr_scan.argtypes = [P, I, I, I, P, I64, I64, F, I, F, I, P, I64, P, P, P, P, P, P, P]
+            lib.oracle_tr_scan.restype = I
+        if hasattr(lib, "refh_tr_penalties"):
+            lib.refh_tr_penalties.argtypes = [I, I, I] + [P] * 10 + [F] + [P] * 7
+            lib.refh_tr_penalties.restype = I
         if hasattr(lib, "refh_scan"):
             lib.refh_scan.argtypes = [P, I, I, I, P, I64, I64, F, I, F, I, I, P, I64, P, P, P, P, P, P, P]
             lib.refh_scan.restype = I
@@ -77,8 +83,6 @@ def scan(m, dsq, i0, j0, algo="cyk", qdbidx=1, cutoff=0.0, do_null3=True, env_cu
     from infernal_gb300 import cmfile
     keep: list = []
     desc = cmfile.make_desc(m, flags_extra=(4 if notgreedy else 0), keep=keep)
-    if getattr(m, "_tr", None) is not None:
-        m._tr.fill(desc, keep)
     dsq = np.ascontiguousarray(dsq, dtype=np.uint8)
     hits = (_Hit * max_hits)()
     nh, ei, ej, sc, mode = I64(), I64(), I64(), F(), I()
@@ -100,3 +104,62 @@ def scan(m, dsq, i0, j0, algo="cyk", qdbidx=1, cutoff=0.0, do_null3=True, env_cu
         raise RuntimeError(f"oracle status {st}: {err.value.decode()}")
     H = [(hits[k].start, hits[k].stop, hits[k].root, hits[k].mode, hits[k].score) for k in range(min(nh.value, max_hits))]
     return H, ei.value, ej.value, sc.value, vsc
+
+
+TR_ALGOS = {"trcyk": 0, "trinside": 1}
+
+
+def tr_scan(m, dsq, i0, j0, algo="trcyk", qdbidx=1, pass_idx=4, cutoff=0.0, do_null3=True, env_cutoff=0.0,
+            want_hits=True, notgreedy=False, reference=False, max_hits=200000):
+    """Truncated scan (RefTrCYKScan / RefITrInsideScan) by the restatement or
+    the reference; returns (hits, envi, envj, sc, vsc, mode)."""
+    from infernal_gb300 import cmfile
+    keep: list = []
+    desc = cmfile.make_desc(m, flags_extra=(4 if notgreedy else 0), keep=keep)
+    dsq = np.ascontiguousarray(dsq, dtype=np.uint8)
+    hits = (_Hit * max_hits)()
+    nh, ei, ej, sc, mode = I64(), I64(), I64(), F(), I()
+    vsc = np.zeros(m.M, np.float32)
+    err = ctypes.create_string_buffer(256)
+    if reference:
+        lib = _load(REF_SO)
+        st = lib.refh_scan(ctypes.byref(desc), m.nodes, REF_ALGOS[algo], qdbidx, dsq.ctypes.data, i0, j0,
+                           cutoff, int(do_null3), env_cutoff, pass_idx, int(want_hits), ctypes.cast(hits, P),
+                           max_hits, ctypes.byref(nh), ctypes.byref(ei), ctypes.byref(ej), vsc.ctypes.data,
+                           ctypes.byref(sc), ctypes.byref(mode), err)
+    else:
+        lib = _load(build_oracle())
+        st = lib.oracle_tr_scan(ctypes.byref(desc), TR_ALGOS[algo], qdbidx, pass_idx, dsq.ctypes.data, i0, j0,
+                                cutoff, int(do_null3), env_cutoff, int(want_hits), ctypes.cast(hits, P), max_hits,
+                                ctypes.byref(nh), ctypes.byref(ei), ctypes.byref(ej), vsc.ctypes.data,
+                                ctypes.byref(sc), ctypes.byref(mode), err)
+    if st != 0:
+        raise RuntimeError(f"oracle status {st}: {err.value.decode()}")
+    H = [(hits[k].start, hits[k].stop, hits[k].root, hits[k].mode, hits[k].score) for k in range(min(nh.value, max_hits))]
+    return H, ei.value, ej.value, sc.value, vsc, mode.value
+
+
+def ref_tr_penalties(m):
+    """Truncation penalties and emit map computed by the reference's own
+    cm_tr_penalties_Create / CreateEmitMap (oracle/_ref); returns
+    (lpos, rpos, g, l, ig, il) with the penalty tables shaped [3, M]."""
+    lib = _load(REF_SO)
+    M, n = m.M, m.nodes
+    keep = []
+
+    def c(a, dt):
+        x = np.ascontiguousarray(a, dt)
+        keep.append(x)
+        return x.ctypes.data
+    lp, rp = np.zeros(n, np.int32), np.zeros(n, np.int32)
+    g, l = np.zeros(3 * M, np.float32), np.zeros(3 * M, np.float32)
+    ig, il = np.zeros(3 * M, np.int32), np.zeros(3 * M, np.int32)
+    err = ctypes.create_string_buffer(256)
+    st = lib.refh_tr_penalties(M, n, m.clen, c(m.sttype, np.int8), c(m.stid, np.int8), c(m.ndidx, np.int32),
+                               c(m.cfirst, np.int32), c(m.cnum, np.int32), c(m.plast, np.int32),
+                               c(m.pnum, np.int32), c(m.ndtype, np.int8), c(m.nodemap, np.int32),
+                               c(m.t_global, np.float32), float(m.pbegin), lp.ctypes.data, rp.ctypes.data,
+                               g.ctypes.data, l.ctypes.data, ig.ctypes.data, il.ctypes.data, err)
+    if st != 0:
+        raise RuntimeError(f"refh_tr_penalties status {st}: {err.value.decode()}")
+    return lp, rp, g.reshape(3, M), l.reshape(3, M), ig.reshape(3, M), il.reshape(3, M)

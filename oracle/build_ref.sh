@@ -16,7 +16,8 @@ CFLAGS="-O2 -fPIC -ffp-contract=off -w -I$HERE/ref_shim -I$SRC"
 rm -f "$OUT"/obj/*.o "$OUT/libinfernal_ref.so"
 export CFLAGS OUT
 printf '%s\n' "$SRC/cm_dpsearch.c" "$SRC/cm_dpsearch_trunc.c" "$SRC/logsum.c" "$SRC/cm_mx.c" \
-  "$SRC/cm_tophits.c" "$SRC/cm_trunc.c" "$SRC/cm_qdband.c" "$HERE/ref_harness.c" "$HERE/ref_offpath.c" |
+  "$SRC/cm_tophits.c" "$SRC/cm_trunc.c" "$SRC/cm_qdband.c" "$SRC/display.c" "$SRC/cm_modelconfig.c" \
+  "$HERE/ref_harness.c" "$HERE/ref_offpath.c" |
   xargs -P 8 -I{} sh -c 'gcc $CFLAGS -c "{}" -o "$OUT/obj/$(basename "{}" .c).o"'
 gcc -shared -o "$OUT/libinfernal_ref.so" "$OUT"/obj/*.o -lm
 echo "built $OUT/libinfernal_ref.so"

@@ -24,6 +24,12 @@
  *   null3_correction()    ScoreCorrectionNull3  src/cm_parsetree.c:2352-2380
  *   remove_overlaps()     cm_tophits_SortForOverlapRemoval + RemoveOrMarkOverlaps
  *                         src/cm_tophits.c:220-245, 400, 1097-1275
+ *   oracle_tr_scan()      RefTrCYKScan          src/cm_dpsearch_trunc.c:79-700
+ *                         RefITrInsideScan      src/cm_dpsearch_trunc.c:741-1338
+ *   tr matrix init        cm_tr_scan_mx_Initialize{Floats,Integers} src/cm_mx.c:6853-6960
+ *   fill flags/penalty    cm_TrFillFromPassIdx  src/cm_dpsearch_trunc.c:3566
+ *                         cm_tr_penalties_IdxForPass src/cm_trunc.c:464
+ *   allow_trunc()         cm_hit_AllowTruncation src/cm_tophits.c:3048-3090
  */
 #include <math.h>
 #include <stdint.h>
@@ -157,10 +163,38 @@ typedef struct {
   double (*act)[8];
   float *vsc, vsc_root;
   float *bestf; int *bestr;
-  float *gmx; int64_t *gback; float *gsave; int *gr;
+  int *bestmode;                 /* truncated scans: mode per d (NULL otherwise) */
+  int fill_L, fill_R, fill_T, pass_idx, pty_idx, vmode_root;
+  float *gmx; int64_t *gback; float *gsave; int *gr; int *gmode;
   hitvec tmp, fin;
   int64_t envi, envj;
 } scanctx;
+
+/* cm_hit_AllowTruncation (src/cm_tophits.c:3048-3090): may a truncated
+ * hit of this mode, rooted at state b, be reported in pass pass_idx? */
+static int allow_trunc(const cmgb_model_desc *m, int pass_idx, int64_t start, int64_t stop,
+                       int64_t i0, int64_t j0, int mode, int b)
+{
+  const int nd = m->ndidx[b], nt = m->ndtype[nd];
+  const int lpos = (nt == CMGB_MATP_nd || nt == CMGB_MATL_nd) ? m->emap_lpos[nd] : m->emap_lpos[nd] + 1;
+  const int rpos = (nt == CMGB_MATP_nd || nt == CMGB_MATR_nd) ? m->emap_rpos[nd] : m->emap_rpos[nd] - 1;
+  if (pass_idx == CMGB_PASS_STD_ANY || pass_idx == CMGB_PASS_5P_AND_3P_ANY || pass_idx == CMGB_PASS_HMM_ONLY_ANY) return 1;
+  if (start == i0 && stop == j0) return 1;
+  if (m->flags & CMGB_LOCAL_BEGIN) {
+    switch (mode) {
+    case CMGB_TRMODE_J: return 1;
+    case CMGB_TRMODE_L: return stop == j0;
+    case CMGB_TRMODE_R: return start == i0;
+    default: return 0;
+    }
+  }
+  switch (mode) {
+  case CMGB_TRMODE_J: return lpos == 1 && rpos == m->clen;
+  case CMGB_TRMODE_L: return stop == j0 && lpos == 1;
+  case CMGB_TRMODE_R: return start == i0 && rpos == m->clen;
+  default: return 0;
+  }
+}
 
 /* per-j hit bookkeeping: ReportHitsGreedily (src/cm_mx.c:7547) or
  * UpdateGammaHitMx (src/cm_mx.c:7440) */
@@ -175,11 +209,13 @@ static void report_j(scanctx *c, int64_t j, int64_t jp, int dn0, int dx0)
       float hs = c->bestf[d], cum = c->gmx[ip - 1] + hs;
       if (cum > c->gmx[jp] && NOT_IMP(hs)) {
         int rep = 1;
-        if (c->act) {
+        const int mode = c->bestmode ? c->bestmode[d] : CMGB_TRMODE_J;
+        if (c->bestmode) rep = allow_trunc(c->m, c->pass_idx, j - d + 1, j, c->i0, c->j0, mode, c->bestr[d]);
+        if (rep && c->act) {
           float c3 = null3_correction(c->m, c->act[jp % (W + 1)], c->act[(ip - 1) % (W + 1)], d);
           hs -= c3; cum -= c3; rep = cum > c->gmx[jp];
         }
-        if (rep) { c->gmx[jp] = cum; c->gback[jp] = j - d + 1; c->gsave[jp] = hs; c->gr[jp] = c->bestr[d]; }
+        if (rep) { c->gmx[jp] = cum; c->gback[jp] = j - d + 1; c->gsave[jp] = hs; c->gr[jp] = c->bestr[d]; c->gmode[jp] = mode; }
       }
     }
   } else {
@@ -188,12 +224,14 @@ static void report_j(scanctx *c, int64_t j, int64_t jp, int dn0, int dx0)
       float hs = c->bestf[d];
       if (hs > best && hs >= c->cutoff && NOT_IMP(hs)) {
         int rep = 1;
-        if (c->act) {
+        const int mode = c->bestmode ? c->bestmode[d] : CMGB_TRMODE_J;
+        if (c->bestmode) rep = allow_trunc(c->m, c->pass_idx, j - d + 1, j, c->i0, c->j0, mode, c->bestr[d]);
+        if (rep && c->act) {
           int64_t ip = jp - d + 1;
           hs -= null3_correction(c->m, c->act[jp % (W + 1)], c->act[(ip - 1) % (W + 1)], d);
           rep = (hs > best && hs >= c->cutoff);
         }
-        if (rep) { hv_push(&c->tmp, j - d + 1, j, c->bestr[d], CMGB_TRMODE_J, hs); best = hs; }
+        if (rep) { hv_push(&c->tmp, j - d + 1, j, c->bestr[d], mode, hs); best = hs; }
       }
     }
   }
@@ -293,6 +331,7 @@ int oracle_scan(const cmgb_model_desc *m, int algo, int qdbidx,
   if (c.gamma_mode) {
     c.gmx = malloc(sizeof(float) * (c.L + 1)); c.gback = malloc(sizeof(int64_t) * (c.L + 1));
     c.gsave = malloc(sizeof(float) * (c.L + 1)); c.gr = malloc(sizeof(int) * (c.L + 1));
+    c.gmode = malloc(sizeof(int) * (c.L + 1));
     c.gmx[0] = 0.f; c.gback[0] = -1;
   }
   c.envi = j0 + 1; c.envj = i0 - 1;
@@ -324,7 +363,131 @@ int oracle_scan(const cmgb_model_desc *m, int algo, int qdbidx,
   if (ret_sc) *ret_sc = c.vsc_root;
   free(c.dn); free(c.dxW); free(c.beglidx); free(c.vsc);
   free(c.bestf); free(c.bestr); free(c.act); free(c.tmp.h); free(c.fin.h);
-  free(c.gmx); free(c.gback); free(c.gsave); free(c.gr);
+  free(c.gmx); free(c.gback); free(c.gsave); free(c.gr); free(c.gmode);
+  return CMGB_OK;
+}
+
+/* C's float -> int conversion as compiled for x86-64 and aarch64: truncation
+ * toward zero, saturating to INT_MIN below the int range (IMPOSSIBLE). */
+static inline int float_to_int_c(float x) { return x > -2147483648.0f ? (int) x : (int) 0x80000000; }
+
+/* Truncated scanner cores: CYK (RefTrCYKScan) and integer Inside
+ * (RefITrInsideScan). */
+#define TR_CORE_NAME tr_core_cyk
+#define SCT float
+#define IMPV IMP
+#define COMB(a, b) MAXF((a), (b))
+#define IS_PTY(p) NOT_IMP(p)
+#define SCOREF(x) (x)
+#define TSC(v, o) m->tsc[(v) * MAXC + (o)]
+#define ESC(v) (m->oesc + (size_t) (v) * Kp * Kp)
+#define LMESC(v) (m->lmesc + (size_t) (v) * Kp)
+#define RMESC(v) (m->rmesc + (size_t) (v) * Kp)
+#define PTY(y) (((m->flags & CMGB_LOCAL_BEGIN) ? m->tr_l_pty : m->tr_g_pty)[(size_t) c->pty_idx * M + (y)])
+#define ENDSC(v) m->endsc[v]
+#define INIT_SC(v, d) (NOT_IMP(m->endsc[v]) ? (float) (m->el_selfsc * (d)) + m->endsc[v] : IMP)
+#define RUNNING_VSC 1
+#include "cm_tr_oracle_core.h"
+
+#define TR_CORE_NAME tr_core_iinside
+#define SCT int
+#define IMPV (-INFTY)
+#define COMB(a, b) ilogsum((a), (b))
+#define IS_PTY(p) ((p) != -INFTY)
+#define SCOREF(x) scorify(x)
+#define TSC(v, o) m->itsc[(v) * MAXC + (o)]
+#define ESC(v) (m->ioesc + (size_t) (v) * Kp * Kp)
+#define LMESC(v) (m->ilmesc + (size_t) (v) * Kp)
+#define RMESC(v) (m->irmesc + (size_t) (v) * Kp)
+#define PTY(y) (((m->flags & CMGB_LOCAL_BEGIN) ? m->tr_il_pty : m->tr_ig_pty)[(size_t) c->pty_idx * M + (y)])
+/* the integer matrix's d = 0 cells start from the float endsc converted to
+ * int (src/cm_mx.c:6941, 6957), not from iendsc */
+#define ENDSC(v) float_to_int_c(m->endsc[v])
+#define INIT_SC(v, d) ((m->iendsc[v] != -INFTY) ? m->iel_selfsc * (d) + m->iendsc[v] : -INFTY)
+#define RUNNING_VSC 0
+#include "cm_tr_oracle_core.h"
+
+/* One truncated scan of dsq[i0..j0] (algo 0: RefTrCYKScan, 1:
+ * RefITrInsideScan) for pipeline pass pass_idx (2..5).  Outputs as
+ * oracle_scan, plus *ret_mode, the mode of the best-scoring parse. */
+int oracle_tr_scan(const cmgb_model_desc *m, int algo, int qdbidx, int pass_idx,
+                   const uint8_t *dsq, int64_t i0, int64_t j0, float cutoff,
+                   int do_null3, float env_cutoff, int want_hits,
+                   cmgb_hit *hits_out, int64_t max_hits, int64_t *ret_nhits,
+                   int64_t *ret_envi, int64_t *ret_envj, float *vsc_out, float *ret_sc,
+                   int *ret_mode, char *errbuf)
+{
+  init_tables();
+  scanctx c;
+  memset(&c, 0, sizeof(c));
+  /* cm_TrFillFromPassIdx / cm_tr_penalties_IdxForPass */
+  switch (pass_idx) {
+  case CMGB_PASS_5P_AND_3P_FORCE: case CMGB_PASS_5P_AND_3P_ANY: c.fill_L = c.fill_R = c.fill_T = 1; c.pty_idx = 0; break;
+  case CMGB_PASS_5P_ONLY_FORCE: c.fill_R = 1; c.pty_idx = 1; break;
+  case CMGB_PASS_3P_ONLY_FORCE: c.fill_L = 1; c.pty_idx = 2; break;
+  default: if (errbuf) snprintf(errbuf, CMGB_ERRBUFSIZE, "oracle: unexpected pass idx: %d", pass_idx); return CMGB_EINVAL;
+  }
+  if (j0 < i0) { if (errbuf) snprintf(errbuf, CMGB_ERRBUFSIZE, "oracle: j0 < i0"); return CMGB_EINCOMPAT; }
+  if (dsq == NULL) { if (errbuf) snprintf(errbuf, CMGB_ERRBUFSIZE, "oracle: dsq is NULL"); return CMGB_EINCOMPAT; }
+  if (m->tr_g_pty == NULL || m->lmesc == NULL || m->emap_lpos == NULL || m->ndtype == NULL) {
+    if (errbuf) snprintf(errbuf, CMGB_ERRBUFSIZE, "oracle: model has no truncation tables");
+    return CMGB_EINCOMPAT;
+  }
+  c.pass_idx = pass_idx;
+  c.m = m; c.dsq = dsq; c.i0 = i0; c.j0 = j0; c.L = j0 - i0 + 1;
+  c.M = m->M; c.Wm = m->W; c.Kp = m->Kp; c.K = m->K;
+  c.W = (int) (c.Wm > c.L ? c.L : c.Wm);
+  c.WP = c.Wm + 1;
+  if (qdbidx == CMGB_QDB1_TIGHT) { c.dmin = m->dmin1; c.dmax = m->dmax1; }
+  else if (qdbidx == CMGB_QDB2_LOOSE) { c.dmin = m->dmin2; c.dmax = m->dmax2; }
+  else if (qdbidx != CMGB_NOQDB) { if (errbuf) snprintf(errbuf, CMGB_ERRBUFSIZE, "oracle: bad qdbidx"); return CMGB_EINCOMPAT; }
+  /* truncated bands: dn = 1 for every state (src/cm_mx.c:6432-6438) */
+  c.dn = malloc(sizeof(int) * c.M); c.dxW = malloc(sizeof(int) * c.M);
+  for (int v = 0; v < c.M; v++) { c.dn[v] = 1; c.dxW[v] = c.dmax ? MINF(c.dmax[v], c.Wm) : c.Wm; }
+  c.beglidx = malloc(sizeof(int) * c.M);
+  for (int v = 0; v < c.M; v++) c.beglidx[v] = (m->stid[v] == CMGB_BEGL_S) ? c.nbegl++ : -1;
+  c.cutoff = cutoff; c.env_cutoff = env_cutoff; c.want_hits = want_hits;
+  c.vsc = malloc(sizeof(float) * c.M);
+  for (int v = 0; v < c.M; v++) c.vsc[v] = IMP;
+  c.vsc_root = IMP; c.vmode_root = CMGB_TRMODE_UNKNOWN;
+  c.bestf = malloc(sizeof(float) * c.WP); c.bestr = malloc(sizeof(int) * c.WP); c.bestmode = malloc(sizeof(int) * c.WP);
+  c.act = do_null3 ? calloc((size_t) c.W + 1, sizeof(double[8])) : NULL;
+  c.gamma_mode = want_hits && (m->flags & CMGB_NOTGREEDY);
+  if (c.gamma_mode) {
+    c.gmx = malloc(sizeof(float) * (c.L + 1)); c.gback = malloc(sizeof(int64_t) * (c.L + 1));
+    c.gsave = malloc(sizeof(float) * (c.L + 1)); c.gr = malloc(sizeof(int) * (c.L + 1));
+    c.gmode = malloc(sizeof(int) * (c.L + 1));
+    c.gmx[0] = 0.f; c.gback[0] = -1;
+  }
+  c.envi = j0 + 1; c.envj = i0 - 1;
+
+  if (algo == 1) tr_core_iinside(&c);
+  else tr_core_cyk(&c);
+
+  c.vsc[0] = c.vsc_root;
+  if (want_hits) {
+    if (c.gamma_mode) {
+      int64_t j = j0;
+      while (j >= i0) {
+        int64_t jp = j - i0 + 1;
+        if (c.gback[jp] == -1) j--;
+        else {
+          if (c.gsave[jp] >= cutoff) hv_push(&c.fin, c.gback[jp], j, c.gr[jp], c.gmode[jp], c.gsave[jp]);
+          j = c.gback[jp] - 1;
+        }
+      }
+    } else remove_overlaps(&c.tmp, &c.fin);
+  }
+  *ret_nhits = c.fin.n;
+  for (int64_t h = 0; h < c.fin.n && h < max_hits; h++) hits_out[h] = c.fin.h[h];
+  if (ret_envi) *ret_envi = (c.envi == j0 + 1) ? -1 : c.envi;
+  if (ret_envj) *ret_envj = (c.envj == i0 - 1) ? -1 : c.envj;
+  if (vsc_out) memcpy(vsc_out, c.vsc, sizeof(float) * c.M);
+  if (ret_sc) *ret_sc = c.vsc_root;
+  if (ret_mode) *ret_mode = c.vmode_root;
+  free(c.dn); free(c.dxW); free(c.beglidx); free(c.vsc);
+  free(c.bestf); free(c.bestr); free(c.bestmode); free(c.act); free(c.tmp.h); free(c.fin.h);
+  free(c.gmx); free(c.gback); free(c.gsave); free(c.gr); free(c.gmode);
   return CMGB_OK;
 }
 

@@ -145,6 +145,78 @@ int cm_TrFillFromMode(char mode, int *fl, int *fr, int *ft)
   return eslOK;
 }
 
+/* Easel's integer push-down stack (esl_stack.c), used by CreateEmitMap. */
+struct esl_stack_s { int *idata; int n, nalloc; };
+ESL_STACK *esl_stack_ICreate(void)
+{
+  ESL_STACK *s = calloc(1, sizeof(ESL_STACK));
+  s->nalloc = 128; s->idata = malloc(sizeof(int) * s->nalloc);
+  return s;
+}
+int esl_stack_IPush(ESL_STACK *s, int x)
+{
+  if (s->n == s->nalloc) { s->nalloc *= 2; s->idata = realloc(s->idata, sizeof(int) * s->nalloc); }
+  s->idata[s->n++] = x;
+  return eslOK;
+}
+int esl_stack_IPop(ESL_STACK *s, int *ret_x)
+{
+  if (s->n == 0) { *ret_x = 0; return eslEOD; }
+  *ret_x = s->idata[--s->n];
+  return eslOK;
+}
+void esl_stack_Destroy(ESL_STACK *s) { if (s) { free(s->idata); free(s); } }
+
+/* src/cm.c:4897 */
+void InsertsGivenNodeIndex(CM_t *cm, int nd, int *ret_i1, int *ret_i2)
+{
+  int i1 = -1, i2 = -1, v = cm->nodemap[nd];
+  switch (cm->ndtype[nd]) {
+  case MATP_nd: i1 = v + 4; i2 = v + 5; break;
+  case MATL_nd: i1 = v + 2; break;
+  case MATR_nd: i1 = v + 2; break;
+  case BEGR_nd: i1 = v + 1; break;
+  case ROOT_nd: i1 = v + 1; i2 = v + 2; break;
+  }
+  *ret_i1 = i1; *ret_i2 = i2;
+}
+
+/* src/cm.c:4250-4330 cm_ExpectedStateOccupancy and src/cm.c:4405
+ * cm_ExpectedPositionOccupancy, for a CM without local begins or ends (the
+ * state cm_tr_penalties_Create sees during cm_Configure).  The reference
+ * looks the parent->child transition up in its transition map; the map's
+ * entry for parent x and child v is v's offset in x's child list,
+ * v - cfirst[x], which is what is used here. */
+int cm_ExpectedPositionOccupancy(CM_t *cm, float **ret_mexpocc, float **ret_iexpocc, double **opt_psi,
+                                 int **opt_m2v_1, int **opt_m2v_2, int **opt_i2v)
+{
+  double *psi = calloc(cm->M, sizeof(double));
+  for (int v = 0; v < cm->M; v++) {
+    int is_insert = (cm->sttype[v] == IL_st || cm->sttype[v] == IR_st);
+    if (cm->sttype[v] == S_st) { psi[v] = 1.0; continue; }
+    for (int y = cm->pnum[v] - 1; y >= (is_insert ? 1 : 0); y--) {
+      int x = cm->plast[v] - y;
+      psi[v] += psi[x] * cm->t[x][v - cm->cfirst[x]];
+    }
+    if (is_insert) psi[v] += psi[v] * (cm->t[v][0] / (1. - cm->t[v][0]));
+  }
+  float *mexpocc = calloc(cm->clen + 1, sizeof(float)), *iexpocc = calloc(cm->clen + 1, sizeof(float));
+  for (int v = 0; v < cm->M; v++) {
+    if (StateIsDetached(cm, v)) continue;
+    int nd = cm->ndidx[v], lpos = cm->emap->lpos[nd], rpos = cm->emap->rpos[nd];
+    if (cm->sttype[v] == MP_st || cm->sttype[v] == ML_st) mexpocc[lpos] += psi[v];
+    if (cm->sttype[v] == MP_st || cm->sttype[v] == MR_st) mexpocc[rpos] += psi[v];
+    if (cm->sttype[v] == IL_st) iexpocc[lpos] = psi[v];
+    if (cm->sttype[v] == IR_st) iexpocc[rpos - 1] = psi[v];
+  }
+  *ret_mexpocc = mexpocc; *ret_iexpocc = iexpocc;
+  if (opt_psi) *opt_psi = psi; else free(psi);
+  if (opt_m2v_1) *opt_m2v_1 = NULL;
+  if (opt_m2v_2) *opt_m2v_2 = NULL;
+  if (opt_i2v) *opt_i2v = NULL;
+  return eslOK;
+}
+
 /* ------------------------------------------------------------------ */
 /* RNA alphabet (Easel's eslRNA: "ACGU-RYMKSWHBVDN*~")                   */
 /* ------------------------------------------------------------------ */
@@ -185,6 +257,8 @@ static CM_t *build_cm(const cmgb_model_desc *m, int nodes)
     cm->cfirst[v] = m->cfirst[v]; cm->cnum[v] = m->cnum[v];
     if (m->ndidx) cm->ndidx[v] = m->ndidx[v];
   }
+  cm->ndtype = calloc(nodes + 1, 1);
+  if (m->ndtype) for (int nd = 0; nd < nodes; nd++) cm->ndtype[nd] = m->ndtype[nd];
   cm->sttype[M] = cm->stid[M] = -1;
   cm->qdbinfo = calloc(1, sizeof(CM_QDBINFO));
   cm->qdbinfo->M = M;
@@ -297,4 +371,43 @@ int refh_scan(const cmgb_model_desc *m, int nodes, int algo, int qdbidx,
    * a handful of scans per process and their destructors touch fields this
    * shell never allocates. */
   return status;
+}
+
+/* Truncation penalties and emit map of a CM, computed by the reference's own
+ * cm_tr_penalties_Create (src/cm_trunc.c:51), CreateEmitMap
+ * (src/display.c:1110) and cm_CalculateLocalBeginProbs
+ * (src/cm_modelconfig.c:397), on the renormalised global transition
+ * probabilities t[M*6].  Outputs: lpos/rpos[nodes]; g/l/ig/il[3*M] indexed
+ * [pty_idx*M + v]. */
+int refh_tr_penalties(int M, int nodes, int clen, const int8_t *sttype, const int8_t *stid,
+                      const int *ndidx, const int *cfirst, const int *cnum, const int *plast,
+                      const int *pnum, const int8_t *ndtype, const int *nodemap, const float *t,
+                      float pbegin, int *lpos_out, int *rpos_out, float *g_out, float *l_out,
+                      int *ig_out, int *il_out, char *errbuf)
+{
+  CM_t *cm = calloc(1, sizeof(CM_t));
+  cm->M = M; cm->nodes = nodes; cm->clen = clen; cm->pbegin = pbegin;
+  cm->sttype = malloc(M + 1); cm->stid = malloc(M + 1);
+  cm->ndidx = malloc(sizeof(int) * M); cm->cfirst = malloc(sizeof(int) * M); cm->cnum = malloc(sizeof(int) * M);
+  cm->plast = malloc(sizeof(int) * M); cm->pnum = malloc(sizeof(int) * M);
+  cm->ndtype = malloc(nodes + 1); cm->nodemap = malloc(sizeof(int) * nodes);
+  cm->t = malloc(sizeof(float *) * M);
+  for (int v = 0; v < M; v++) {
+    cm->sttype[v] = sttype[v]; cm->stid[v] = stid[v]; cm->ndidx[v] = ndidx[v];
+    cm->cfirst[v] = cfirst[v]; cm->cnum[v] = cnum[v]; cm->plast[v] = plast[v]; cm->pnum[v] = pnum[v];
+    cm->t[v] = (float *) t + (size_t) v * MAXCONNECT;
+  }
+  cm->sttype[M] = cm->stid[M] = -1;
+  for (int nd = 0; nd < nodes; nd++) { cm->ndtype[nd] = ndtype[nd]; cm->nodemap[nd] = nodemap[nd]; }
+  cm->ndtype[nodes] = -1;
+  if ((cm->emap = CreateEmitMap(cm)) == NULL) { snprintf(errbuf, 128, "CreateEmitMap failed"); return eslFAIL; }
+  CM_TR_PENALTIES *trp = cm_tr_penalties_Create(cm, FALSE, errbuf);
+  if (trp == NULL) { snprintf(errbuf, 128, "cm_tr_penalties_Create failed"); return eslFAIL; }
+  for (int nd = 0; nd < nodes; nd++) { lpos_out[nd] = cm->emap->lpos[nd]; rpos_out[nd] = cm->emap->rpos[nd]; }
+  for (int p = 0; p < NTRPENALTY; p++)
+    for (int v = 0; v < M; v++) {
+      g_out[p * M + v] = trp->g_ptyAA[p][v];  l_out[p * M + v] = trp->l_ptyAA[p][v];
+      ig_out[p * M + v] = trp->ig_ptyAA[p][v]; il_out[p * M + v] = trp->il_ptyAA[p][v];
+    }
+  return eslOK;
 }

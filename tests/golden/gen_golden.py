@@ -10,9 +10,11 @@ project's reader (infernal_gb300/cmfile.py) and stores their score tables as
 with the reference test suite's CM-emitted sequences (testsuite/emitted-*.fa)
 embedded on both strands, plus short, sub-range and degenerate-residue cases;
 (3) runs the REFERENCE'S OWN scanners (FastCYKScan, RefCYKScan,
-FastIInsideScan, RefIInsideScan, FastFInsideScan; src/cm_dpsearch.c, compiled
-from source by oracle/build_ref.sh) on every case and stores hits, envelope,
-best score and per-state best scores in ``golden.npz`` / ``golden.json``.
+FastIInsideScan, RefIInsideScan, FastFInsideScan; src/cm_dpsearch.c, and the
+truncated RefTrCYKScan / RefITrInsideScan of src/cm_dpsearch_trunc.c on
+5'/3'-truncated targets for pipeline passes 2-5; compiled from source by
+oracle/build_ref.sh) on every case and stores hits, envelope, best score (and
+mode), and per-state best scores in ``golden.npz`` / ``golden.json``.
 
 The parity tests replay these cases against the CPU restatement
 (oracle/cm_scan_oracle.c) and against the GPU scanners.
@@ -73,6 +75,33 @@ def cases_for(name, rng, emitted):
     return cs
 
 
+def tr_cases_for(name, rng, emitted):
+    """Truncated-scan cases: a 5'-truncated emitted sequence at the start of
+    the target and a 3'-truncated one at its end, as the pipeline's terminal
+    windows see them."""
+    s = emitted[1 % len(emitted)]
+    bg = lambda n: "".join(rng.choice(list("ACGU"), n))
+    c5 = int(rng.integers(len(s) // 5, len(s) // 2))
+    c3 = int(rng.integers(len(s) // 2, 4 * len(s) // 5))
+    t5 = s[c5:] + bg(int(len(s) * 0.8))
+    t3 = bg(int(len(s) * 0.7)) + s[:c3]
+    return [("tr5", t5, 1, len(t5)), ("tr3", t3, 1, len(t3)), ("tr3sub", t3, 9, len(t3))]
+
+
+TR_RUNS = [  # (algo, qdbidx, pass_idx, cutoff, null3, env_cutoff, notgreedy, which cases)
+    ("trcyk", 1, 2, 0.0, 1, 2.0, 0, "all"),
+    ("trcyk", 1, 3, 0.0, 1, 2.0, 0, "all"),
+    ("trcyk", 1, 4, 0.0, 1, 2.0, 0, "all"),
+    ("trcyk", 0, 4, -5.0, 0, 0.0, 0, "tr5"),
+    ("trcyk", 2, 5, 0.0, 1, 2.0, 0, "tr3"),
+    ("trcyk", 1, 4, 0.0, 1, 2.0, 1, "tr5"),
+    ("trinside", 2, 2, 0.0, 1, 2.0, 0, "all"),
+    ("trinside", 2, 3, 0.0, 1, 2.0, 0, "all"),
+    ("trinside", 2, 4, 0.0, 1, 2.0, 0, "all"),
+    ("trinside", 1, 4, 3.0, 0, 0.0, 1, "tr3"),
+]
+
+
 RUNS = [  # (algo, qdbidx, cutoff, null3, env_cutoff, notgreedy, which cases)
     ("cyk", 1, 0.0, 1, 2.0, 0, "all"),
     ("cyk", 2, 0.0, 0, 5.0, 0, "all"),
@@ -114,6 +143,28 @@ def main(ref_root="/root/reference"):
                                  sc=float(np.float32(sc)).hex(),
                                  hits=[[h[0], h[1], h[2], h[3], float(np.float32(h[4])).hex()] for h in hits]))
                 print(f"{cid:3d} {key:18s} {algo:9s} qdb{qdb} n3={n3} ng={ng} hits={len(hits)} sc={sc:.3f}")
+    # truncated scanners (RefTrCYKScan / RefITrInsideScan), own seeded stream
+    rng = np.random.default_rng(20261204)
+    for name, fa in MODELS.items():
+        m = cmfile.load_npz(os.path.join(HERE, f"{name}.model.npz"))
+        emitted = [s.upper().replace("T", "U") for _, s in cmfile.read_fasta(os.path.join(ref_root, "testsuite", fa))]
+        for label, seq, i0, j0 in tr_cases_for(name, rng, emitted):
+            key = f"{name}.{label}"
+            dsq = cmfile.digitize(seq)
+            arrays[f"dsq.{key}"] = dsq
+            for algo, qdb, pidx, cut, n3, envc, ng, which in TR_RUNS:
+                if which != "all" and which != label:
+                    continue
+                hits, ei, ej, sc, vsc, mode = oracle.tr_scan(m, dsq, i0, j0, algo=algo, qdbidx=qdb, pass_idx=pidx,
+                                                             cutoff=cut, do_null3=bool(n3), env_cutoff=envc,
+                                                             notgreedy=bool(ng), reference=True)
+                cid = len(meta)
+                arrays[f"vsc.{cid}"] = vsc
+                meta.append(dict(id=cid, model=name, seq=key, i0=i0, j0=j0, algo=algo, qdbidx=qdb, pass_idx=pidx,
+                                 cutoff=cut, null3=n3, env_cutoff=envc, notgreedy=ng, envi=ei, envj=ej,
+                                 sc=float(np.float32(sc)).hex(), mode=mode,
+                                 hits=[[h[0], h[1], h[2], h[3], float(np.float32(h[4])).hex()] for h in hits]))
+                print(f"{cid:3d} {key:18s} {algo:9s} qdb{qdb} pass{pidx} n3={n3} ng={ng} hits={len(hits)} sc={sc:.3f} mode={mode}")
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **arrays)
     with open(os.path.join(HERE, "golden.json"), "w") as fh:
         json.dump(meta, fh, indent=0)
