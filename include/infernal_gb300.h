@@ -234,6 +234,42 @@ int cmgb_FastFInsideScan_dev(cmgb_ctx *ctx, cmgb_model *model, char *errbuf, int
                              cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
                              int64_t *ret_envi, int64_t *ret_envj, float *ret_vsc, float *ret_sc);
 
+/* ---- truncated scanners ----
+ * pass_idx is the pipeline pass (CMGB_PASS_5P_ONLY_FORCE, _3P_ONLY_FORCE,
+ * _5P_AND_3P_FORCE or _5P_AND_3P_ANY); it selects the truncation modes that
+ * are scored and the truncated-begin penalties (cm_TrFillFromPassIdx,
+ * src/cm_dpsearch_trunc.c:3566), and which hits may be reported
+ * (cm_hit_AllowTruncation, src/cm_tophits.c:3048); any other value returns
+ * CMGB_EINVAL.  ret_mode (may be NULL) receives the mode (CMGB_TRMODE_*) of
+ * the best-scoring parse; hits carry their own mode.  The model must have
+ * been created with the truncation fields of cmgb_model_desc (lmesc ..
+ * nodes); otherwise CMGB_EINCOMPAT.  Other arguments as for the standard
+ * scanners; ret_vsc receives, as in the reference, the best score of each
+ * state over all end positions for CYK and at the final end position j0 for
+ * integer Inside. */
+
+/* Replaces RefTrCYKScan() (src/cm_dpsearch_trunc.c:79-700, declared src/infernal.h:2722). */
+int cmgb_RefTrCYKScan(cmgb_ctx *ctx, cmgb_model *model, char *errbuf, int qdbidx, int pass_idx,
+                      const uint8_t *dsq, int64_t i0, int64_t j0, float cutoff,
+                      cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
+                      int64_t *ret_envi, int64_t *ret_envj, float *ret_vsc, int *ret_mode, float *ret_sc);
+
+/* Replaces RefITrInsideScan() (src/cm_dpsearch_trunc.c:741-1338, declared src/infernal.h:2724). */
+int cmgb_RefITrInsideScan(cmgb_ctx *ctx, cmgb_model *model, char *errbuf, int qdbidx, int pass_idx,
+                          const uint8_t *dsq, int64_t i0, int64_t j0, float cutoff,
+                          cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
+                          int64_t *ret_envi, int64_t *ret_envj, float *ret_vsc, int *ret_mode, float *ret_sc);
+
+/* Same truncated scans with device-resident residues (as the _dev scanners above). */
+int cmgb_RefTrCYKScan_dev(cmgb_ctx *ctx, cmgb_model *model, char *errbuf, int qdbidx, int pass_idx,
+                          const uint8_t *d_dsq, int64_t i0, int64_t j0, float cutoff,
+                          cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
+                          int64_t *ret_envi, int64_t *ret_envj, float *ret_vsc, int *ret_mode, float *ret_sc);
+int cmgb_RefITrInsideScan_dev(cmgb_ctx *ctx, cmgb_model *model, char *errbuf, int qdbidx, int pass_idx,
+                              const uint8_t *d_dsq, int64_t i0, int64_t j0, float cutoff,
+                              cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
+                              int64_t *ret_envi, int64_t *ret_envj, float *ret_vsc, int *ret_mode, float *ret_sc);
+
 /* ---- allocation-free CYK scan ----
  * This entry point has no counterpart in the reference.  It exists for
  * callers that must not allocate device memory while they scan: code that

@@ -22,6 +22,7 @@
 #include "hits.h"
 #include "scan_kernel.cuh"
 #include "scan_plan.h"
+#include "trscan_kernel.cuh"
 
 using namespace cmgb;
 
@@ -49,8 +50,39 @@ static void launch_qdb(int grid, int nt, size_t smem, cudaStream_t, const KParam
   for (auto *b : bars) delete b;
   for (auto *w : warps) delete w;
 }
+template <int ALG, bool GL>
+static void launch_tr(int grid, int nt, size_t smem, cudaStream_t, const TrKParams &kp)
+{
+  std::vector<std::vector<float>> sm(grid, std::vector<float>(smem / 4 + 16));
+  std::vector<std::barrier<> *> bars;
+  std::vector<EmuWarp *> warps;
+  for (int b = 0; b < grid; b++) bars.push_back(new std::barrier<>(nt));
+  for (int b = 0; b < grid * (nt / 32); b++) warps.push_back(new EmuWarp);
+  std::vector<std::thread> th;
+  for (int b = 0; b < grid; b++)
+    for (int t = 0; t < nt; t++)
+      th.emplace_back([&, b, t] {
+        cmgb_emu_bar = bars[b]; cmgb_emu_warp = warps[b * (nt / 32) + t / 32]; cmgb_emu_lane = t & 31;
+        tr_scan_body<ALG, GL>(kp, sm[b].data(), t, nt, b);
+      });
+  for (auto &x : th) x.join();
+  for (auto *b : bars) delete b;
+  for (auto *w : warps) delete w;
+}
 #else
 static const int kDefaultThreads = 512;
+template <int ALG, bool GL>
+static void launch_tr(int grid, int nt, size_t smem, cudaStream_t s, const TrKParams &kp)
+{
+  tr_scan_kernel<ALG, GL><<<grid, nt, smem, s>>>(kp);
+}
+template <int ALG, bool GL>
+static cudaError_t prepare_tr(int nt, int smem, int *blocks_per_sm)
+{
+  cudaError_t e = cudaFuncSetAttribute(tr_scan_kernel<ALG, GL>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, tr_scan_kernel<ALG, GL>, nt, smem);
+}
 template <int ALG, bool GL>
 static void launch_qdb(int grid, int nt, size_t smem, cudaStream_t s, const KParams &kp)
 {
@@ -92,6 +124,27 @@ static void launch_any(int alg, bool gl, int grid, int nt, size_t smem, cudaStre
   }
 }
 
+#ifndef CMGB_HOST_EMULATION
+static cudaError_t prepare_tr_any(int alg, bool gl, int nt, int smem, int *nb)
+{
+  switch (alg * 2 + (gl ? 1 : 0)) {
+  case 0: return prepare_tr<0, false>(nt, smem, nb);
+  case 1: return prepare_tr<0, true>(nt, smem, nb);
+  case 2: return prepare_tr<1, false>(nt, smem, nb);
+  default: return prepare_tr<1, true>(nt, smem, nb);
+  }
+}
+#endif
+static void launch_tr_any(int alg, bool gl, int grid, int nt, size_t smem, cudaStream_t s, const TrKParams &kp)
+{
+  switch (alg * 2 + (gl ? 1 : 0)) {
+  case 0: launch_tr<0, false>(grid, nt, smem, s, kp); break;
+  case 1: launch_tr<0, true>(grid, nt, smem, s, kp); break;
+  case 2: launch_tr<1, false>(grid, nt, smem, s, kp); break;
+  default: launch_tr<1, true>(grid, nt, smem, s, kp); break;
+  }
+}
+
 struct Control {            // device control block, zeroed/initialised per scan
   int queue;
   int ncand;
@@ -112,6 +165,13 @@ struct DevPlan {
   unsigned char *d_rec = nullptr;
 };
 
+struct DevTrPlan {
+  bool built = false;
+  int T = 0, nt = 0, arena = -1;
+  ScanPlan plan;
+  TrStateInfo *d_states = nullptr;
+};
+
 struct cmgb_model_s {
   cmgb_ctx *ctx = nullptr;
   int M = 0, W = 0, K = 0, Kp = 0, flags = 0;
@@ -127,6 +187,15 @@ struct cmgb_model_s {
   float *d_oesc = nullptr;
   int *d_ioesc = nullptr;
   DevPlan plans[3][3];       // [qdbidx][algorithm: 0 CYK, 1 integer Inside, 2 float Inside]
+  // truncated scanning (present when the description carries the tables)
+  bool has_tr = false;
+  std::vector<float> lmesc, rmesc, tr_g, tr_l;
+  std::vector<int> ilmesc, irmesc, tr_ig, tr_il, ndidx, emap_lpos, emap_rpos;
+  std::vector<int8_t> ndtype;
+  int clen = 0, nodes = 0;
+  float *d_lmesc = nullptr, *d_rmesc = nullptr;
+  int *d_ilmesc = nullptr, *d_irmesc = nullptr;
+  DevTrPlan trplans[3][2];   // [qdbidx][0 TrCYK, 1 integer TrInside]
   int tuned_T[3][3] = {{0}}, tuned_arena[3][3] = {{0}};   // autotuner's choice (0: none yet)
 };
 
@@ -152,6 +221,10 @@ struct cmgb_ctx_s {
   float *d_flog = nullptr;
   Control *h_ctl = nullptr;       // pinned
   std::vector<CandHost> h_cand;
+  // truncated scans
+  TrCand *d_trcand = nullptr; size_t trcand_bytes = 0;
+  unsigned long long *d_winbest = nullptr; size_t winbest_bytes = 0;
+  float *d_wmax = nullptr; size_t wmax_bytes = 0;
 };
 
 static int grow(void **p, size_t *cur, size_t need, char *errbuf)
@@ -205,6 +278,7 @@ extern "C" void cmgb_ctx_destroy(cmgb_ctx *c)
   cudaSetDevice(c->device);
   cudaFree(c->d_carry); cudaFree(c->d_ring); cudaFree(c->d_arena); cudaFree(c->d_dsq); cudaFree(c->d_cand);
   cudaFree(c->d_ctl); cudaFree(c->d_vsc); cudaFree(c->d_ilog); cudaFree(c->d_flog);
+  cudaFree(c->d_trcand); cudaFree(c->d_winbest); cudaFree(c->d_wmax);
   cudaFreeHost(c->h_ctl);
   cudaEventDestroy(c->ev0); cudaEventDestroy(c->ev1);
   cudaStreamDestroy(c->stream);
@@ -270,6 +344,31 @@ extern "C" int cmgb_model_create(cmgb_ctx *c, const cmgb_model_desc *d, cmgb_mod
     ERRF(CMGB_EMEM, "out of device memory for emission tables");
   CUDA_TRY(cudaMemcpy(m->d_oesc, d->oesc, sizeof(float) * (size_t) M * KK, cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMemcpy(m->d_ioesc, d->ioesc, sizeof(int) * (size_t) M * KK, cudaMemcpyHostToDevice));
+  // truncated scanning tables (cm->lmesc/rmesc, cm->trp, cm->emap), when given
+  if (d->lmesc && d->rmesc && d->ilmesc && d->irmesc && d->tr_g_pty && d->tr_l_pty && d->tr_ig_pty && d->tr_il_pty &&
+      d->ndidx && d->emap_lpos && d->emap_rpos && d->ndtype && d->nodes > 0) {
+    const size_t MK = (size_t) M * d->Kp;
+    m->lmesc.assign(d->lmesc, d->lmesc + MK); m->rmesc.assign(d->rmesc, d->rmesc + MK);
+    m->ilmesc.assign(d->ilmesc, d->ilmesc + MK); m->irmesc.assign(d->irmesc, d->irmesc + MK);
+    m->tr_g.assign(d->tr_g_pty, d->tr_g_pty + 3 * M); m->tr_l.assign(d->tr_l_pty, d->tr_l_pty + 3 * M);
+    m->tr_ig.assign(d->tr_ig_pty, d->tr_ig_pty + 3 * M); m->tr_il.assign(d->tr_il_pty, d->tr_il_pty + 3 * M);
+    m->ndidx.assign(d->ndidx, d->ndidx + M);
+    m->nodes = d->nodes; m->clen = d->clen;
+    m->ndtype.assign(d->ndtype, d->ndtype + d->nodes);
+    m->emap_lpos.assign(d->emap_lpos, d->emap_lpos + d->nodes); m->emap_rpos.assign(d->emap_rpos, d->emap_rpos + d->nodes);
+    D.lmesc = m->lmesc.data(); D.rmesc = m->rmesc.data(); D.ilmesc = m->ilmesc.data(); D.irmesc = m->irmesc.data();
+    D.tr_g_pty = m->tr_g.data(); D.tr_l_pty = m->tr_l.data(); D.tr_ig_pty = m->tr_ig.data(); D.tr_il_pty = m->tr_il.data();
+    D.ndidx = m->ndidx.data(); D.ndtype = m->ndtype.data(); D.emap_lpos = m->emap_lpos.data(); D.emap_rpos = m->emap_rpos.data();
+    D.clen = m->clen; D.nodes = m->nodes;
+    if (cudaMalloc(&m->d_lmesc, sizeof(float) * MK) != cudaSuccess || cudaMalloc(&m->d_rmesc, sizeof(float) * MK) != cudaSuccess ||
+        cudaMalloc(&m->d_ilmesc, sizeof(int) * MK) != cudaSuccess || cudaMalloc(&m->d_irmesc, sizeof(int) * MK) != cudaSuccess)
+      ERRF(CMGB_EMEM, "out of device memory for marginal emission tables");
+    CUDA_TRY(cudaMemcpy(m->d_lmesc, d->lmesc, sizeof(float) * MK, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(m->d_rmesc, d->rmesc, sizeof(float) * MK, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(m->d_ilmesc, d->ilmesc, sizeof(int) * MK, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(m->d_irmesc, d->irmesc, sizeof(int) * MK, cudaMemcpyHostToDevice));
+    m->has_tr = true;
+  }
   *ret = m.release();
   return CMGB_OK;
 }
@@ -279,7 +378,9 @@ extern "C" void cmgb_model_destroy(cmgb_model *m)
   if (!m) return;
   cudaSetDevice(m->ctx->device);
   cudaFree(m->d_oesc); cudaFree(m->d_ioesc);
+  cudaFree(m->d_lmesc); cudaFree(m->d_rmesc); cudaFree(m->d_ilmesc); cudaFree(m->d_irmesc);
   for (auto &row : m->plans) for (auto &p : row) { cudaFree(p.d_states); cudaFree(p.d_rec); }
+  for (auto &row : m->trplans) for (auto &p : row) cudaFree(p.d_states);
   delete m;
 }
 
@@ -515,6 +616,290 @@ extern "C" int cmgb_FastFInsideScan_dev(cmgb_ctx *c, cmgb_model *m, char *errbuf
 {
   if (d_dsq == nullptr) ERRF(CMGB_EINCOMPAT, "FastFInsideScan, dsq is NULL");
   return scan_std(c, m, errbuf, qdbidx, 2, nullptr, d_dsq, i0, j0, cutoff, hl, do_null3, env_cutoff, envi, envj, vsc, sc);
+}
+
+// ---------------------------------------------------------------------------
+// Truncated scanners (RefTrCYKScan / RefITrInsideScan).
+static const int kTrCandCap = 1 << 21;
+
+static int get_tr_plan(cmgb_model *m, int qdbidx, int alg, DevTrPlan **ret, char *errbuf)
+{
+  cmgb_ctx *c = m->ctx;
+  DevTrPlan &dp = m->trplans[qdbidx][alg];
+  const int wantT = c->tile_rows ? c->tile_rows : 16;
+  const int wantA = c->arena;
+  if (dp.built && dp.T == wantT && dp.nt == c->threads && dp.arena == wantA) { *ret = &dp; return CMGB_OK; }
+  if (dp.d_states) { cudaFree(dp.d_states); dp.d_states = nullptr; }
+  TrPlanOut po;
+  int T = wantT;
+  for (;;) {
+    po = TrPlanOut();
+    // arena: 1 shared memory, 2 global memory, 0 shared when it fits the device, else global
+    bool gl = wantA == 2;
+    if (!build_tr_plan(&m->desc, qdbidx, T, c->threads, alg == 1, gl, &po)) ERRF(CMGB_EINCOMPAT, "%s", po.err.c_str());
+    if (!gl && wantA == 0 && po.plan.smem_bytes + 64 > c->max_smem_optin) {
+      po = TrPlanOut();
+      if (!build_tr_plan(&m->desc, qdbidx, T, c->threads, alg == 1, true, &po)) ERRF(CMGB_EINCOMPAT, "%s", po.err.c_str());
+    }
+    if (po.plan.smem_bytes + 64 <= c->max_smem_optin) break;
+    if (T <= 2) ERRF(CMGB_ERANGE, "model needs %d bytes of shared memory per CTA even with 2-row tiles", po.plan.smem_bytes);
+    T = T > 8 ? T - 4 : T - 2;
+  }
+  CUDA_TRY(cudaMalloc(&dp.d_states, sizeof(TrStateInfo) * po.phases.size()));
+  CUDA_TRY(cudaMemcpy(dp.d_states, po.phases.data(), sizeof(TrStateInfo) * po.phases.size(), cudaMemcpyHostToDevice));
+  dp.plan = po.plan;
+  dp.T = wantT;
+  dp.nt = c->threads;
+  dp.arena = wantA;
+  dp.built = true;
+  *ret = &dp;
+  return CMGB_OK;
+}
+
+// Common driver of the truncated scanners.  alg: 0 TrCYK (float), 1 integer
+// TrInside.  The kernel reports, per window, the root cells that set a new
+// running maximum within the window; cells are kept when they also beat the
+// maxima of every earlier window (the reference's sequential root test,
+// src/cm_dpsearch_trunc.c:548-605), then resolved per end position.
+static int scan_tr(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, int pass_idx, int alg,
+                   const uint8_t *host_dsq, const uint8_t *dev_dsq_in, int64_t i0, int64_t j0,
+                   float cutoff, cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
+                   int64_t *ret_envi, int64_t *ret_envj, float *ret_vsc, int *ret_mode, float *ret_sc)
+{
+  const char *fn = alg == 1 ? "RefITrInsideScan" : "RefTrCYKScan";
+  if (!c || !m) ERRF(CMGB_EINVAL, "%s, NULL context or model", fn);
+  int fill_L = 0, fill_R = 0, fill_T = 0, pty_idx = -1;   // cm_TrFillFromPassIdx / cm_tr_penalties_IdxForPass
+  switch (pass_idx) {
+  case CMGB_PASS_5P_AND_3P_FORCE: case CMGB_PASS_5P_AND_3P_ANY: fill_L = fill_R = fill_T = 1; pty_idx = 0; break;
+  case CMGB_PASS_5P_ONLY_FORCE: fill_R = 1; pty_idx = 1; break;
+  case CMGB_PASS_3P_ONLY_FORCE: fill_L = 1; pty_idx = 2; break;
+  default: ERRF(CMGB_EINVAL, "%s(), unexpected pass idx: %d", fn, pass_idx);
+  }
+  if (j0 < i0) ERRF(CMGB_EINCOMPAT, "%s, i0: %lld j0: %lld", fn, (long long) i0, (long long) j0);
+  if (i0 < 1) ERRF(CMGB_EINCOMPAT, "%s, i0 must be >= 1", fn);
+  if (host_dsq == nullptr && dev_dsq_in == nullptr) ERRF(CMGB_EINCOMPAT, "%s, dsq is NULL", fn);
+  if (qdbidx < 0 || qdbidx > 2) ERRF(CMGB_EINCOMPAT, "%s, qdbidx is invalid", fn);
+  if (!m->has_tr) ERRF(CMGB_EINCOMPAT, "%s, the model was created without truncation tables", fn);
+  int st;
+  CUDA_TRY(cudaSetDevice(c->device));
+  DevTrPlan *dp;
+  if ((st = get_tr_plan(m, qdbidx, alg, &dp, errbuf)) != CMGB_OK) return st;
+  const ScanPlan &P = dp->plan;
+  const int64_t L = j0 - i0 + 1;
+  const int W = m->W;
+
+  const unsigned char *d_dsq;
+  int64_t lo = i0 - W - 1; if (lo < 0) lo = 0;
+  if (dev_dsq_in) d_dsq = dev_dsq_in;
+  else {
+    size_t need = (size_t) (j0 + 2 - lo);
+    if ((st = grow((void **) &c->d_dsq, &c->dsq_bytes, need, errbuf)) != CMGB_OK) return st;
+    CUDA_TRY(cudaMemcpyAsync(c->d_dsq, host_dsq + lo, need, cudaMemcpyHostToDevice, c->stream));
+    d_dsq = c->d_dsq - lo;
+  }
+  c->last_h2d = (dev_dsq_in ? 0 : (int64_t) (j0 + 2 - lo)) + (int64_t) sizeof(Control);
+
+  const bool gl = P.arena_global != 0;
+  int cps = c->ctas_per_sm;
+  if (cps == 0) {
+#ifndef CMGB_HOST_EMULATION
+    int nb = 1;
+    CUDA_TRY(prepare_tr_any(alg, gl, c->threads, P.smem_bytes, &nb));
+    cps = nb < 1 ? 1 : nb;
+#else
+    cps = 1;
+#endif
+  }
+  const int grid_max = c->nsm * cps;
+  int64_t win = c->window_len;
+  if (win <= 0) {
+    win = (L + grid_max - 1) / grid_max;
+    if (win < 8LL * W) win = 8LL * W;
+  }
+  // a window's root cells are numbered (row, length, mode) in 32 bits
+  const int64_t win_cap = ((int64_t) 1 << 30) / (W + 1);
+  if (win > win_cap) win = win_cap;
+  win = ((win + P.T - 1) / P.T) * P.T;
+  if (win > win_cap) win -= P.T;
+  const int64_t nwin = (L + win - 1) / win;
+  if (nwin > (1 << 24)) ERRF(CMGB_ERANGE, "%s, too many windows", fn);
+  const int grid = (int) std::min<int64_t>(nwin, grid_max);
+
+  const int accw = P.acc_w;
+  size_t carry_need = sizeof(float) * 2 * (size_t) P.carry_elems * grid;
+  size_t ring_need = sizeof(float) * (size_t) P.ring_elems * grid;
+  if ((st = grow((void **) &c->d_carry, &c->carry_bytes, carry_need, errbuf)) != CMGB_OK) return st;
+  if ((st = grow((void **) &c->d_ring, &c->ring_bytes, ring_need, errbuf)) != CMGB_OK) return st;
+  if (gl && (st = grow((void **) &c->d_arena, &c->arena_bytes, sizeof(float) * (size_t) P.arena_elems * grid, errbuf)) != CMGB_OK) return st;
+  if ((st = grow((void **) &c->d_trcand, &c->trcand_bytes, sizeof(TrCand) * (size_t) kTrCandCap, errbuf)) != CMGB_OK) return st;
+  if ((st = grow((void **) &c->d_winbest, &c->winbest_bytes, sizeof(unsigned long long) * (size_t) nwin, errbuf)) != CMGB_OK) return st;
+  if ((st = grow((void **) &c->d_wmax, &c->wmax_bytes, sizeof(float) * 8 * (size_t) accw * nwin, errbuf)) != CMGB_OK) return st;
+  if (ret_vsc && c->vsc_len < m->M) {
+    cudaFree(c->d_vsc); c->d_vsc = nullptr;
+    if (cudaMalloc(&c->d_vsc, sizeof(unsigned) * m->M) != cudaSuccess) ERRF(CMGB_EMEM, "out of device memory");
+    c->vsc_len = m->M;
+  }
+  Control *h = c->h_ctl;
+  std::memset(h, 0, sizeof(Control));
+  CUDA_TRY(cudaMemcpyAsync(c->d_ctl, h, sizeof(Control), cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaMemsetAsync(c->d_winbest, 0, sizeof(unsigned long long) * (size_t) nwin, c->stream));
+  if (ret_vsc) CUDA_TRY(cudaMemsetAsync(c->d_vsc, 0, sizeof(unsigned) * m->M, c->stream));
+
+  TrKParams kp;
+  std::memset(&kp, 0, sizeof(kp));
+  kp.st = dp->d_states; kp.plan = P; kp.arena = c->d_arena;
+  kp.oesc = m->d_oesc; kp.ioesc = m->d_ioesc;
+  kp.lmesc = m->d_lmesc; kp.rmesc = m->d_rmesc; kp.ilmesc = m->d_ilmesc; kp.irmesc = m->d_irmesc;
+  kp.ilog = c->d_ilog;
+  kp.dsq = d_dsq; kp.i0 = i0; kp.j0 = j0; kp.win_len = win; kp.nwin = (int) nwin;
+  kp.queue = &c->d_ctl->queue; kp.carry = c->d_carry; kp.ring = c->d_ring;
+  kp.cand = c->d_trcand; kp.ncand = &c->d_ctl->ncand; kp.cand_cap = kTrCandCap;
+  const bool greedy = !(m->flags & CMGB_NOTGREEDY);
+  kp.cand_cut = cutoff; kp.cand_pos = (hitlist && !greedy) ? 1 : 0;
+  if (!hitlist) { kp.cand_cut = 3.0e38f; kp.cand_pos = 0; }
+  kp.env_cut = (ret_envi || ret_envj) ? env_cutoff : 3.0e38f;
+  kp.fill_L = fill_L; kp.fill_R = fill_R; kp.fill_T = fill_T; kp.pty_idx = pty_idx;
+  kp.vsc = ret_vsc ? c->d_vsc : nullptr;
+  kp.winbest = c->d_winbest; kp.wmax = c->d_wmax; kp.err = &c->d_ctl->err;
+
+  const size_t smem = (size_t) P.smem_bytes;
+  CUDA_TRY(cudaEventRecord(c->ev0, c->stream));
+  launch_tr_any(alg, gl, grid, c->threads, smem, c->stream, kp);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaEventRecord(c->ev1, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(h, c->d_ctl, sizeof(Control), cudaMemcpyDeviceToHost, c->stream));
+  std::vector<unsigned long long> winbest((size_t) nwin);
+  CUDA_TRY(cudaMemcpyAsync(winbest.data(), c->d_winbest, sizeof(unsigned long long) * (size_t) nwin, cudaMemcpyDeviceToHost, c->stream));
+  std::vector<unsigned> vscu;
+  if (ret_vsc) { vscu.resize(m->M); CUDA_TRY(cudaMemcpyAsync(vscu.data(), c->d_vsc, sizeof(unsigned) * m->M, cudaMemcpyDeviceToHost, c->stream)); }
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  CUDA_TRY(cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1));
+  c->last_launches = 1;
+  c->last_d2h = (int64_t) sizeof(Control) + (int64_t) sizeof(unsigned long long) * nwin + (ret_vsc ? (int64_t) sizeof(unsigned) * m->M : 0);
+  if (h->err & 1) ERRF(CMGB_ERANGE, "%s, more than %d candidate root cells; raise the cutoff", fn, kTrCandCap);
+
+  auto u2f = [](unsigned u) { if (u == 0) return CMGB_IMPOSSIBLE; unsigned b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u; float f; std::memcpy(&f, &b, 4); return f; };
+  // best parse over all windows: highest score, earliest window on ties
+  float best = CMGB_IMPOSSIBLE; int bmode = CMGB_TRMODE_UNKNOWN; bool any = false;
+  for (int64_t w = 0; w < nwin; w++) {
+    const unsigned long long k = winbest[(size_t) w];
+    if (!k) continue;
+    const float f = u2f((unsigned) (k >> 32));
+    if (!any || f > best) {
+      best = f; any = true;
+      const unsigned pos = 0xFFFFFFFFu - (unsigned) (k & 0xFFFFFFFFULL);
+      bmode = 3 - (int) (pos & 3u);
+    }
+  }
+  if (ret_sc) *ret_sc = best;
+  if (ret_mode) *ret_mode = bmode;
+  if (ret_vsc) { for (int v = 0; v < m->M; v++) ret_vsc[v] = u2f(vscu[v]); ret_vsc[0] = best; }
+
+  // candidates: keep the cells that beat the running maxima of all earlier windows
+  const int n = h->ncand;
+  std::vector<TrCand> tc((size_t) n);
+  if (n > 0) CUDA_TRY(cudaMemcpy(tc.data(), c->d_trcand, sizeof(TrCand) * (size_t) n, cudaMemcpyDeviceToHost));
+  c->last_d2h += (int64_t) sizeof(TrCand) * n;
+  std::vector<int> wmx;
+  if (n > 0 && nwin > 1) {
+    wmx.resize((size_t) 8 * accw * nwin);
+    CUDA_TRY(cudaMemcpy(wmx.data(), c->d_wmax, sizeof(int) * wmx.size(), cudaMemcpyDeviceToHost));
+    c->last_d2h += (int64_t) sizeof(int) * (int64_t) wmx.size();
+  }
+  std::sort(tc.begin(), tc.end(), [](const TrCand &a, const TrCand &b) {
+    if (a.win != b.win) return a.win < b.win;
+    if (a.j != b.j) return a.j < b.j;
+    if (a.d != b.d) return a.d < b.d;
+    return a.mode > b.mode;   // J, L, R, T
+  });
+  const int imp_i = alg == 1 ? -CMGB_INFTY : 0;
+  std::vector<int> prefix((size_t) 8 * accw);
+  if (alg == 1) std::fill(prefix.begin(), prefix.end(), imp_i);
+  else { float fi = CMGB_IMPOSSIBLE; int b; std::memcpy(&b, &fi, 4); std::fill(prefix.begin(), prefix.end(), b); }
+  auto greater = [alg](int a, int b) {   // native comparison of two raw scores
+    if (alg == 1) return a > b;
+    float fa, fb; std::memcpy(&fa, &a, 4); std::memcpy(&fb, &b, 4); return fa > fb;
+  };
+  std::vector<CandHost> &out = c->h_cand;
+  out.clear();
+  int64_t envi = j0 + 1, envj = i0 - 1;
+  size_t q = 0;
+  int cur_w = 0;
+  while (q < tc.size()) {
+    while (cur_w < tc[q].win) {   // fold window cur_w's final maxima into the prefix
+      for (int x = 0; x < 8 * accw; x++) {
+        const int v = wmx[(size_t) cur_w * 8 * accw + x];
+        if (greater(v, prefix[x])) prefix[x] = v;
+      }
+      cur_w++;
+    }
+    // one (j, d) cell: its globally registered modes, best score, then smallest state, then mode order
+    size_t e = q;
+    while (e < tc.size() && tc[e].win == tc[q].win && tc[e].j == tc[q].j && tc[e].d == tc[q].d) e++;
+    int wq = -1;
+    for (size_t x = q; x < e; x++) {
+      const TrCand &t = tc[x];
+      const int mi = 3 - t.mode, pq = (int) (t.j & 1);
+      if (!greater(t.raw, prefix[(size_t) (mi * 2 + pq) * accw + t.d - 1])) continue;
+      if (wq < 0 || t.f > tc[wq].f || (t.f == tc[wq].f && t.y < tc[wq].y)) wq = (int) x;
+    }
+    if (wq >= 0) {
+      const TrCand &t = tc[wq];
+      if (t.f >= env_cutoff) { envi = std::min<int64_t>(envi, t.j - t.d + 1); envj = std::max<int64_t>(envj, t.j); }
+      if (hitlist) { CandHost ch; ch.j = t.j; ch.d = t.d; ch.sc = t.f; ch.r = t.y; ch.mode = t.mode; out.push_back(ch); }
+    }
+    q = e;
+  }
+  if (ret_envi) *ret_envi = (envi == j0 + 1) ? -1 : envi;
+  if (ret_envj) *ret_envj = (envj == i0 - 1) ? -1 : envj;
+
+  if (hitlist) {
+    std::vector<uint8_t> res_copy;
+    const uint8_t *hd = host_dsq;
+    if (do_null3 && !out.empty() && hd == nullptr) {
+      res_copy.resize((size_t) (j0 + 2));
+      CUDA_TRY(cudaMemcpy(res_copy.data() + i0, dev_dsq_in + i0, (size_t) L, cudaMemcpyDeviceToHost));
+      c->last_d2h += L;
+      hd = res_copy.data();
+    }
+    TruncFilter tf;
+    tf.pass_idx = pass_idx; tf.local = (m->flags & CMGB_LOCAL_BEGIN) ? 1 : 0; tf.clen = m->clen;
+    tf.ndidx = m->ndidx.data(); tf.ndtype = m->ndtype.data(); tf.lpos = m->emap_lpos.data(); tf.rpos = m->emap_rpos.data();
+    ResolveArgs ra;
+    ra.null = m->null.data(); ra.K = m->K; ra.null3_omega = m->null3_omega; ra.do_null3 = do_null3;
+    ra.greedy = greedy ? 1 : 0; ra.cutoff = cutoff; ra.i0 = i0; ra.j0 = j0; ra.dsq = hd; ra.tr = &tf;
+    resolve_hits(out, ra, hitlist->h);
+  }
+  return CMGB_OK;
+}
+
+extern "C" int cmgb_RefTrCYKScan(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, int pass_idx, const uint8_t *dsq,
+                                 int64_t i0, int64_t j0, float cutoff, cmgb_hitlist *hl, int do_null3, float env_cutoff,
+                                 int64_t *envi, int64_t *envj, float *vsc, int *mode, float *sc)
+{
+  if (dsq == nullptr) ERRF(CMGB_EINCOMPAT, "RefTrCYKScan, dsq is NULL");
+  return scan_tr(c, m, errbuf, qdbidx, pass_idx, 0, dsq, nullptr, i0, j0, cutoff, hl, do_null3, env_cutoff, envi, envj, vsc, mode, sc);
+}
+extern "C" int cmgb_RefITrInsideScan(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, int pass_idx, const uint8_t *dsq,
+                                     int64_t i0, int64_t j0, float cutoff, cmgb_hitlist *hl, int do_null3, float env_cutoff,
+                                     int64_t *envi, int64_t *envj, float *vsc, int *mode, float *sc)
+{
+  if (dsq == nullptr) ERRF(CMGB_EINCOMPAT, "RefITrInsideScan, dsq is NULL");
+  return scan_tr(c, m, errbuf, qdbidx, pass_idx, 1, dsq, nullptr, i0, j0, cutoff, hl, do_null3, env_cutoff, envi, envj, vsc, mode, sc);
+}
+extern "C" int cmgb_RefTrCYKScan_dev(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, int pass_idx, const uint8_t *d_dsq,
+                                     int64_t i0, int64_t j0, float cutoff, cmgb_hitlist *hl, int do_null3, float env_cutoff,
+                                     int64_t *envi, int64_t *envj, float *vsc, int *mode, float *sc)
+{
+  if (d_dsq == nullptr) ERRF(CMGB_EINCOMPAT, "RefTrCYKScan, dsq is NULL");
+  return scan_tr(c, m, errbuf, qdbidx, pass_idx, 0, nullptr, d_dsq, i0, j0, cutoff, hl, do_null3, env_cutoff, envi, envj, vsc, mode, sc);
+}
+extern "C" int cmgb_RefITrInsideScan_dev(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, int pass_idx, const uint8_t *d_dsq,
+                                         int64_t i0, int64_t j0, float cutoff, cmgb_hitlist *hl, int do_null3, float env_cutoff,
+                                         int64_t *envi, int64_t *envj, float *vsc, int *mode, float *sc)
+{
+  if (d_dsq == nullptr) ERRF(CMGB_EINCOMPAT, "RefITrInsideScan, dsq is NULL");
+  return scan_tr(c, m, errbuf, qdbidx, pass_idx, 1, nullptr, d_dsq, i0, j0, cutoff, hl, do_null3, env_cutoff, envi, envj, vsc, mode, sc);
 }
 
 // Times candidate shapes (tile rows x arena placement) of band set qdbidx and

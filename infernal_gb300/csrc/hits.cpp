@@ -103,6 +103,29 @@ static float null3(const ResolveArgs &a, const Composition &cmp, int64_t i, int6
   return logsum2(0.f, score);
 }
 
+bool allow_truncation(const TruncFilter &t, int64_t start, int64_t stop, int64_t i0, int64_t j0, int mode, int b)
+{
+  const int nd = t.ndidx[b], nt = t.ndtype[nd];
+  const int lpos = (nt == CMGB_MATP_nd || nt == CMGB_MATL_nd) ? t.lpos[nd] : t.lpos[nd] + 1;
+  const int rpos = (nt == CMGB_MATP_nd || nt == CMGB_MATR_nd) ? t.rpos[nd] : t.rpos[nd] - 1;
+  if (t.pass_idx == CMGB_PASS_STD_ANY || t.pass_idx == CMGB_PASS_5P_AND_3P_ANY || t.pass_idx == CMGB_PASS_HMM_ONLY_ANY) return true;
+  if (start == i0 && stop == j0) return true;
+  if (t.local) {
+    switch (mode) {
+    case CMGB_TRMODE_J: return true;
+    case CMGB_TRMODE_L: return stop == j0;
+    case CMGB_TRMODE_R: return start == i0;
+    default: return false;
+    }
+  }
+  switch (mode) {
+  case CMGB_TRMODE_J: return lpos == 1 && rpos == t.clen;
+  case CMGB_TRMODE_L: return stop == j0 && lpos == 1;
+  case CMGB_TRMODE_R: return start == i0 && rpos == t.clen;
+  default: return false;
+  }
+}
+
 void resolve_hits(std::vector<CandHost> &c, const ResolveArgs &a, std::vector<cmgb_hit> &out)
 {
   logsum_tables(nullptr, nullptr);
@@ -123,8 +146,10 @@ void resolve_hits(std::vector<CandHost> &c, const ResolveArgs &a, std::vector<cm
         if (hs > best && hs >= a.cutoff && not_imp(hs)) {
           bool rep = true;
           int64_t i = c[q].j - c[q].d + 1;
-          if (cmp) { hs -= null3(a, *cmp, i, c[q].j); rep = (hs > best && hs >= a.cutoff); }
-          if (rep) { cmgb_hit h; h.start = i; h.stop = c[q].j; h.root = c[q].r; h.mode = CMGB_TRMODE_J; h.score = hs; tmp.push_back(h); best = hs; }
+          const int mode = a.tr ? c[q].mode : CMGB_TRMODE_J;
+          if (a.tr) rep = allow_truncation(*a.tr, i, c[q].j, a.i0, a.j0, mode, c[q].r);
+          if (rep && cmp) { hs -= null3(a, *cmp, i, c[q].j); rep = (hs > best && hs >= a.cutoff); }
+          if (rep) { cmgb_hit h; h.start = i; h.stop = c[q].j; h.root = c[q].r; h.mode = mode; h.score = hs; tmp.push_back(h); best = hs; }
         }
       }
       k = e;
@@ -149,7 +174,7 @@ void resolve_hits(std::vector<CandHost> &c, const ResolveArgs &a, std::vector<cm
     std::vector<float> mx(L + 1);
     std::vector<int64_t> gback(L + 1, -1);
     std::vector<float> savesc(L + 1, IMPf);
-    std::vector<int> saver(L + 1, -1);
+    std::vector<int> saver(L + 1, -1), savemode(L + 1, -1);
     mx[0] = 0.f;
     size_t k = 0;
     for (int64_t jp = 1; jp <= L; jp++) {
@@ -162,8 +187,10 @@ void resolve_hits(std::vector<CandHost> &c, const ResolveArgs &a, std::vector<cm
         float hs = c[k].sc, cum = mx[ip - 1] + hs;
         if (cum > mx[jp] && not_imp(hs)) {
           bool rep = true;
-          if (cmp) { float c3 = null3(a, *cmp, j - d + 1, j); hs -= c3; cum -= c3; rep = cum > mx[jp]; }
-          if (rep) { mx[jp] = cum; gback[jp] = j - d + 1; savesc[jp] = hs; saver[jp] = c[k].r; }
+          const int mode = a.tr ? c[k].mode : CMGB_TRMODE_J;
+          if (a.tr) rep = allow_truncation(*a.tr, j - d + 1, j, a.i0, a.j0, mode, c[k].r);
+          if (rep && cmp) { float c3 = null3(a, *cmp, j - d + 1, j); hs -= c3; cum -= c3; rep = cum > mx[jp]; }
+          if (rep) { mx[jp] = cum; gback[jp] = j - d + 1; savesc[jp] = hs; saver[jp] = c[k].r; savemode[jp] = mode; }
         }
         k++;
       }
@@ -173,7 +200,7 @@ void resolve_hits(std::vector<CandHost> &c, const ResolveArgs &a, std::vector<cm
       const int64_t jp = j - a.i0 + 1;
       if (gback[jp] == -1) j--;
       else {
-        if (savesc[jp] >= a.cutoff) { cmgb_hit h; h.start = gback[jp]; h.stop = j; h.root = saver[jp]; h.mode = CMGB_TRMODE_J; h.score = savesc[jp]; out.push_back(h); }
+        if (savesc[jp] >= a.cutoff) { cmgb_hit h; h.start = gback[jp]; h.stop = j; h.root = saver[jp]; h.mode = savemode[jp]; h.score = savesc[jp]; out.push_back(h); }
         j = gback[jp] - 1;
       }
     }

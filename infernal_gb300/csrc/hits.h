@@ -18,7 +18,21 @@
 
 namespace cmgb {
 
-struct CandHost { long long j; int d; float sc; int r; int pad; };
+// A resolved root cell: end j, length d, score, root state, mode (standard
+// scans: CMGB_TRMODE_J).
+struct CandHost { long long j; int d; float sc; int r; int mode; };
+
+// Truncated scans: which hits a pass may report, cm_hit_AllowTruncation
+// (src/cm_tophits.c:3048-3090).
+struct TruncFilter {
+  int pass_idx;
+  int local;             // CMH_LOCAL_BEGIN
+  int clen;
+  const int *ndidx;      // [M]
+  const int8_t *ndtype;  // [nodes]
+  const int *lpos, *rpos;// emit map [nodes]
+};
+bool allow_truncation(const TruncFilter &t, int64_t start, int64_t stop, int64_t i0, int64_t j0, int mode, int b);
 
 struct ResolveArgs {
   const float *null;     // [K]
@@ -29,6 +43,7 @@ struct ResolveArgs {
   float cutoff;
   int64_t i0, j0;
   const uint8_t *dsq;    // host residues indexed by sequence coordinate (needed for NULL3)
+  const TruncFilter *tr = nullptr;   // truncated scans: per-hit admissibility and modes
 };
 
 // Appends the resolved hits to out (in the reference's order).

@@ -41,6 +41,7 @@
 #define CMGB_ATOMIC_MAXU(p, v) atomicMax((p), (v))
 #define CMGB_ATOMIC_MINLL(p, v) atomicMin((long long *) (p), (long long) (v))
 #define CMGB_ATOMIC_MAXLL(p, v) atomicMax((long long *) (p), (long long) (v))
+#define CMGB_ATOMIC_MAXULL(p, v) atomicMax((unsigned long long *) (p), (unsigned long long) (v))
 #else
 #define CMGB_DEV inline
 #define CMGB_SYNC() cmgb_emu_sync()
@@ -54,6 +55,7 @@
 #define CMGB_ATOMIC_MAXU(p, v) cmgb_emu_maxu((p), (v))
 #define CMGB_ATOMIC_MINLL(p, v) cmgb_emu_minll((long long *) (p), (long long) (v))
 #define CMGB_ATOMIC_MAXLL(p, v) cmgb_emu_maxll((long long *) (p), (long long) (v))
+#define CMGB_ATOMIC_MAXULL(p, v) cmgb_emu_maxull((unsigned long long *) (p), (unsigned long long) (v))
 #endif
 
 #ifndef CMGB_HOST_EMULATION

@@ -58,6 +58,23 @@ struct StateInfo {
   int     dn_y, dx_y, dn_w, dx_w, banded;
 };
 
+// Per-state descriptor of the truncated scan (RefTrCYKScan /
+// RefITrInsideScan): the standard descriptor plus the truncated-begin
+// penalties and the plane layout.  Every state keeps three score planes --
+// J (joint), L (left marginal), R (right marginal) -- of (T+1) x stride cells
+// each, mstride elements apart; its carry rows and, for BEGL_S, its history
+// ring hold the same three planes.  The T (terminal) scores of bifurcations
+// are only read by the root and go straight into its accumulators.
+struct TrStateInfo {
+  StateInfo s;          // s.buf / s.carry / s.ring address plane J
+  float pty[3];         // truncated-begin penalty into this state, per penalty index (IMPOSSIBLE: none)
+  int   ipty[3];        // integer penalties (-INFTY: none)
+  int   mstride;        // elements between this state's planes (tile buffer)
+  int   cm[CMGB_MAXC];  // children's plane strides (B: cm[0] is the BEGL ring's)
+  int   iinit0;         // d = 0 value of the integer J plane
+  int   pad_[2];
+};
+
 enum {
   SK_E = 0,      // end state: constant row, never computed
   SK_GEN = 1,    // generic: all cells independent
@@ -65,7 +82,8 @@ enum {
   SK_IR = 3,     // insert-right: self-loop on the previous row (serial along diagonals)
   SK_B = 4,      // bifurcation
   SK_BEGL = 5,   // BEGL_S: written to the global history ring
-  SK_ROOT = 6    // state 0
+  SK_ROOT = 6,   // state 0
+  SK_DET = 7     // truncated scans: detached insert (never computed, all IMPOSSIBLE)
 };
 
 // Whole-plan parameters (device copy lives in global memory).
@@ -101,6 +119,9 @@ struct ScanPlan {
   float el_selfsc;
   int iel_selfsc;
   int local_begin;
+  // truncated scans only
+  int imp_row;            // element offset of an all-IMPOSSIBLE constant row (detached states)
+  int rmax_off;           // element offset of the root's running maxima [4 modes][2 parities][acc_w]
 };
 
 #ifndef CMGB_NO_HOST_PLAN
@@ -120,5 +141,16 @@ bool build_plan(const cmgb_model_desc *m, int qdbidx, int T, int nthreads, bool 
 // Packs the phase records (descriptor followed by the state's emission row,
 // float or int) that the kernel streams into shared memory one phase ahead.
 void build_records(const cmgb_model_desc *m, bool ins, PlanOut *out);
+
+struct TrPlanOut {
+  ScanPlan plan;
+  std::vector<TrStateInfo> states;   // indexed by state v
+  std::vector<TrStateInfo> phases;   // computed states in sweep order (E and detached states left out)
+  std::string err;
+};
+// Plan of the truncated scan of band set qdbidx: every state's band is
+// d = 1 .. min(dmax, W) (src/cm_mx.c:6432-6438).  Requires the model's
+// truncation tables (lmesc/rmesc, penalties); false + err otherwise.
+bool build_tr_plan(const cmgb_model_desc *m, int qdbidx, int T, int nthreads, bool logsum_table, bool arena_global, TrPlanOut *out);
 }  // namespace cmgb
 #endif

@@ -1,7 +1,8 @@
 """ctypes bindings of the C ABI in include/infernal_gb300.h.
 
 This is the Python mirror of the reference scanner interface
-(``FastCYKScan``/``FastIInsideScan``, src/cm_dpsearch.c:90 and :1106): the
+(``FastCYKScan``/``FastIInsideScan``, src/cm_dpsearch.c:90 and :1106;
+``RefTrCYKScan``/``RefITrInsideScan``, src/cm_dpsearch_trunc.c:79 and :741): the
 same argument meaning and the same error behaviour (a non-zero Easel status
 code is raised as :class:`ScanError` carrying the errbuf text).
 
@@ -34,9 +35,12 @@ EXPORTS = [
     "cmgb_hitlist_clear", "cmgb_FastCYKScan", "cmgb_FastIInsideScan", "cmgb_FastCYKScan_dev",
     "cmgb_FastIInsideScan_dev", "cmgb_count_cells", "cmgb_autotune", "cmgb_FastCYKScan_noalloc",
     "cmgb_FastFInsideScan", "cmgb_FastFInsideScan_dev",
+    "cmgb_RefTrCYKScan", "cmgb_RefITrInsideScan", "cmgb_RefTrCYKScan_dev", "cmgb_RefITrInsideScan_dev",
 ]
 
 _SCAN_ARGS = [P, P, ctypes.c_char_p, I, P, I64, I64, F, P, I, F, P, P, P, P]
+_TR_SCAN_ARGS = [P, P, ctypes.c_char_p, I, I, P, I64, I64, F, P, I, F, P, P, P, P, P]
+TR_ALGOS = {"trcyk": "cmgb_RefTrCYKScan", "trinside": "cmgb_RefITrInsideScan"}
 
 
 class Hit(ctypes.Structure):
@@ -86,6 +90,10 @@ def bind(path: str) -> ctypes.CDLL:
         f = getattr(lib, name)
         f.argtypes = _SCAN_ARGS
         f.restype = I
+    for name in ("cmgb_RefTrCYKScan", "cmgb_RefITrInsideScan", "cmgb_RefTrCYKScan_dev", "cmgb_RefITrInsideScan_dev"):
+        f = getattr(lib, name)
+        f.argtypes = _TR_SCAN_ARGS
+        f.restype = I
     lib.cmgb_autotune.argtypes = [P, P, I, I, I64, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.c_char_p]
     lib.cmgb_autotune.restype = I
     lib.cmgb_FastCYKScan_noalloc.argtypes = [P, P, ctypes.c_char_p, I, P, I64, I64, F, F, P, I, ctypes.POINTER(I),
@@ -114,6 +122,7 @@ class ScanResult:
     sc: float
     vsc: Optional[np.ndarray]
     kernel_ms: float
+    mode: int = 3              # truncated scans: CMGB_TRMODE_* of the best parse
 
 
 class Scanner:
@@ -196,6 +205,44 @@ class Scanner:
                 self.lib.cmgb_hitlist_destroy(hl)
         return ScanResult(hits, envi.value, envj.value, sc.value, vsc,
                           float(self.lib.cmgb_ctx_last_kernel_ms(self._ctx)))
+
+    def tr_scan(self, m: cmfile.CMModel, dsq, i0: int, j0: int, algo: str = "trcyk", qdbidx: int = 1,
+                pass_idx: int = 4, cutoff: float = 0.0, do_null3: bool = True, env_cutoff: float = 0.0,
+                want_hits: bool = True, want_vsc: bool = False, notgreedy: bool = False,
+                device_ptr: Optional[int] = None) -> ScanResult:
+        """Runs cmgb_RefTrCYKScan (algo="trcyk") or cmgb_RefITrInsideScan
+        (algo="trinside") for pipeline pass pass_idx (2..5); the result's
+        .mode is the mode of the best parse."""
+        mh = self.model(m, CMGB_NOTGREEDY if notgreedy else 0)
+        fn = TR_ALGOS[algo]
+        if device_ptr is not None:
+            fn += "_dev"
+            dptr = device_ptr
+        else:
+            dsq = np.ascontiguousarray(dsq, dtype=np.uint8)
+            dptr = dsq.ctypes.data
+        hl = self.lib.cmgb_hitlist_create() if want_hits else None
+        envi, envj, sc, mode = I64(), I64(), F(), I()
+        vsc = np.zeros(m.M, np.float32) if want_vsc else None
+        err = ctypes.create_string_buffer(256)
+        try:
+            st = getattr(self.lib, fn)(self._ctx, mh, err, qdbidx, pass_idx, dptr, i0, j0, cutoff, hl,
+                                       int(do_null3), env_cutoff, ctypes.byref(envi), ctypes.byref(envj),
+                                       vsc.ctypes.data if vsc is not None else None, ctypes.byref(mode),
+                                       ctypes.byref(sc))
+            if st != 0:
+                raise ScanError(st, err.value.decode())
+            hits = []
+            if hl:
+                h = Hit()
+                for k in range(self.lib.cmgb_hitlist_count(hl)):
+                    self.lib.cmgb_hitlist_get(hl, k, ctypes.byref(h))
+                    hits.append((h.start, h.stop, h.root, h.mode, h.score))
+        finally:
+            if hl:
+                self.lib.cmgb_hitlist_destroy(hl)
+        return ScanResult(hits, envi.value, envj.value, sc.value, vsc,
+                          float(self.lib.cmgb_ctx_last_kernel_ms(self._ctx)), mode.value)
 
     def autotune(self, m: cmfile.CMModel, qdbidx: int, algo: str = "cyk", sample_len: int = 0):
         """Runs cmgb_autotune for (model, band set, algorithm); returns (tile_rows, arena)."""

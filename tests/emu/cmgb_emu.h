@@ -27,6 +27,12 @@ inline long long cmgb_emu_maxll(long long *p, long long v)
   while (cur < v && !__atomic_compare_exchange_n(p, &cur, v, false, __ATOMIC_SEQ_CST, __ATOMIC_SEQ_CST)) {}
   return cur;
 }
+inline unsigned long long cmgb_emu_maxull(unsigned long long *p, unsigned long long v)
+{
+  unsigned long long cur = __atomic_load_n(p, __ATOMIC_SEQ_CST);
+  while (cur < v && !__atomic_compare_exchange_n(p, &cur, v, false, __ATOMIC_SEQ_CST, __ATOMIC_SEQ_CST)) {}
+  return cur;
+}
 #include <cstring>
 // warp-level primitives: the 32 threads of an emulated warp meet at a
 // per-warp barrier and exchange values through a slot array

@@ -4,7 +4,6 @@ CTA -- reproduces the oracle bit for bit and keeps the reference's error
 behaviour.  No GPU is used."""
 import os
 import re
-import subprocess
 
 import numpy as np
 import pytest
@@ -13,7 +12,6 @@ import oracle
 from infernal_gb300 import cmfile, lib as L
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-EMU_SO = os.path.join(ROOT, "tests", "emu", "_build", "libinfernal_gb300_emu.so")
 
 
 def _declared_functions():
@@ -60,18 +58,6 @@ def test_count_cells_matches_oracle(built_lib, models):
         for q in (0, 1, 2):
             for Ln in (10, m.W - 1, m.W, 5000):
                 assert lib.cmgb_count_cells(ctypes.byref(d), q, Ln) == olib.oracle_count_cells(ctypes.byref(d), q, Ln)
-
-
-@pytest.fixture(scope="module")
-def emu():
-    os.makedirs(os.path.dirname(EMU_SO), exist_ok=True)
-    csrc = os.path.join(ROOT, "infernal_gb300", "csrc")
-    srcs = [os.path.join(csrc, f) for f in ("capi.cu", "scan_plan.cpp", "hits.cpp")]
-    if not os.path.exists(EMU_SO) or os.path.getmtime(EMU_SO) < max(os.path.getmtime(s) for s in srcs + [os.path.join(csrc, "scan_kernel.cuh")]):
-        subprocess.check_call(["g++", "-std=c++20", "-O2", "-fPIC", "-shared", "-ffp-contract=off",
-                               "-DCMGB_HOST_EMULATION", "-I", os.path.join(ROOT, "tests", "emu"),
-                               "-x", "c++", srcs[0], "-x", "none", srcs[1], srcs[2], "-o", EMU_SO, "-lpthread"])
-    return L.Scanner(lib=L.bind(EMU_SO))
 
 
 @pytest.mark.parametrize("name,algo,qdb,T,win,arena", [
