@@ -270,6 +270,32 @@ int cmgb_RefITrInsideScan_dev(cmgb_ctx *ctx, cmgb_model *model, char *errbuf, in
                               cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
                               int64_t *ret_envi, int64_t *ret_envj, float *ret_vsc, int *ret_mode, float *ret_sc);
 
+/* ---- batched scans ----
+ * Runs nseq independent scans of one model in one persistent launch: what
+ * the reference's callers do in a loop (pli_dispatch_cm_search per window,
+ * src/cm_pipeline.c:4187; cmcalibrate per sequence, src/cmcalibrate.c:2338)
+ * with one CTA work item per sequence, longest sequence first.  It has no
+ * reference counterpart of its own; each sequence's results equal those of
+ * the single-sequence scanner named by algo on that sequence over [1, L].
+ * Sequence q is the Easel digital sequence at seqs + offsets[q]: a sentinel,
+ * lengths[q] residues, a sentinel, all within seqs[0 .. seqs_len-1].
+ * Outputs per sequence (arrays of nseq, each may be NULL): ret_nhits (hits
+ * it added to hitlist, which receives sequence 0's hits, then sequence 1's,
+ * ..., each in the single scanner's order, with start/stop local to the
+ * sequence), ret_envi/ret_envj (local, -1 if none), ret_sc (best score),
+ * ret_mode (mode of the best parse; CMGB_TRMODE_J for the standard scans).
+ * pass_idx is read by the truncated algorithms only.  Per-state scores
+ * (ret_vsc) are not produced here. */
+#define CMGB_ALGO_CYK       0   /* FastCYKScan      */
+#define CMGB_ALGO_IINSIDE   1   /* FastIInsideScan  */
+#define CMGB_ALGO_FINSIDE   2   /* FastFInsideScan  */
+#define CMGB_ALGO_TRCYK     3   /* RefTrCYKScan     */
+#define CMGB_ALGO_ITRINSIDE 4   /* RefITrInsideScan */
+int cmgb_ScanBatch(cmgb_ctx *ctx, cmgb_model *model, char *errbuf, int algo, int qdbidx, int pass_idx,
+                   const uint8_t *seqs, int64_t seqs_len, const int64_t *offsets, const int64_t *lengths,
+                   int nseq, float cutoff, cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
+                   int64_t *ret_nhits, int64_t *ret_envi, int64_t *ret_envj, float *ret_sc, int *ret_mode);
+
 /* ---- allocation-free CYK scan ----
  * This entry point has no counterpart in the reference.  It exists for
  * callers that must not allocate device memory while they scan: code that

@@ -902,6 +902,216 @@ extern "C" int cmgb_RefITrInsideScan_dev(cmgb_ctx *c, cmgb_model *m, char *errbu
   return scan_tr(c, m, errbuf, qdbidx, pass_idx, 1, nullptr, d_dsq, i0, j0, cutoff, hl, do_null3, env_cutoff, envi, envj, vsc, mode, sc);
 }
 
+// ---------------------------------------------------------------------------
+// Batched scans: n independent sequences of one model in one persistent
+// launch, one work item per sequence, longest first.
+extern "C" int cmgb_ScanBatch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo, int qdbidx, int pass_idx,
+                              const uint8_t *seqs, int64_t seqs_len, const int64_t *offsets, const int64_t *lengths,
+                              int nseq, float cutoff, cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
+                              int64_t *ret_nhits, int64_t *ret_envi, int64_t *ret_envj, float *ret_sc, int *ret_mode)
+{
+  static const char *fn = "ScanBatch";
+  if (!c || !m) ERRF(CMGB_EINVAL, "%s, NULL context or model", fn);
+  if (algo < CMGB_ALGO_CYK || algo > CMGB_ALGO_ITRINSIDE) ERRF(CMGB_EINVAL, "%s, unknown algorithm %d", fn, algo);
+  if (seqs == nullptr || offsets == nullptr || lengths == nullptr || nseq < 1) ERRF(CMGB_EINCOMPAT, "%s, no sequences", fn);
+  if (qdbidx < 0 || qdbidx > 2) ERRF(CMGB_EINCOMPAT, "%s, qdbidx is invalid", fn);
+  const bool tr = algo >= CMGB_ALGO_TRCYK;
+  const int alg = tr ? algo - CMGB_ALGO_TRCYK : algo;
+  int fill_L = 0, fill_R = 0, fill_T = 0, pty_idx = 0;
+  if (tr) {
+    switch (pass_idx) {
+    case CMGB_PASS_5P_AND_3P_FORCE: case CMGB_PASS_5P_AND_3P_ANY: fill_L = fill_R = fill_T = 1; pty_idx = 0; break;
+    case CMGB_PASS_5P_ONLY_FORCE: fill_R = 1; pty_idx = 1; break;
+    case CMGB_PASS_3P_ONLY_FORCE: fill_L = 1; pty_idx = 2; break;
+    default: ERRF(CMGB_EINVAL, "%s, unexpected pass idx: %d", fn, pass_idx);
+    }
+    if (!m->has_tr) ERRF(CMGB_EINCOMPAT, "%s, the model was created without truncation tables", fn);
+  }
+  for (int q = 0; q < nseq; q++)   // sentinel, lengths[q] residues, sentinel, all inside the buffer
+    if (!(lengths[q] >= 1 && offsets[q] >= 0 && offsets[q] + lengths[q] + 1 <= seqs_len - 1))
+      ERRF(CMGB_EINCOMPAT, "%s, sequence %d lies outside the buffer", fn, q);
+  int st;
+  CUDA_TRY(cudaSetDevice(c->device));
+  const ScanPlan *P;
+  const void *d_states = nullptr;
+  const unsigned char *d_rec = nullptr;
+  if (tr) { DevTrPlan *dp; if ((st = get_tr_plan(m, qdbidx, alg, &dp, errbuf)) != CMGB_OK) return st; P = &dp->plan; d_states = dp->d_states; }
+  else { DevPlan *dp; if ((st = get_plan(m, qdbidx, alg, &dp, errbuf)) != CMGB_OK) return st; P = &dp->plan; d_states = dp->d_states; d_rec = dp->d_rec; }
+
+  // work items, longest sequence first (band area grows with length)
+  std::vector<int> order(nseq);
+  for (int q = 0; q < nseq; q++) order[q] = q;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return lengths[a] > lengths[b]; });
+  std::vector<long long> ws(nseq), we(nseq);
+  for (int w = 0; w < nseq; w++) { ws[w] = offsets[order[w]] + 1; we[w] = offsets[order[w]] + lengths[order[w]]; }
+  // one device block: residues, window ranges, per-window outputs
+  auto al = [](size_t x) { return (x + 255) & ~(size_t) 255; };
+  const size_t o_ws = al((size_t) seqs_len), o_we = o_ws + al(sizeof(long long) * nseq), o_out = o_we + al(sizeof(long long) * nseq);
+  const size_t out_bytes = tr ? sizeof(unsigned long long) * nseq : sizeof(long long) * 2 * nseq + sizeof(unsigned) * nseq;
+  if ((st = grow((void **) &c->d_dsq, &c->dsq_bytes, o_out + al(out_bytes), errbuf)) != CMGB_OK) return st;
+  unsigned char *blk = c->d_dsq;
+  std::vector<unsigned char> out_init(out_bytes, 0);
+  if (!tr) {
+    long long *env = reinterpret_cast<long long *>(out_init.data());
+    for (int w = 0; w < nseq; w++) { env[2 * w] = LLONG_MAX; env[2 * w + 1] = -1; }
+  }
+  CUDA_TRY(cudaMemcpyAsync(blk, seqs, (size_t) seqs_len, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(blk + o_ws, ws.data(), sizeof(long long) * nseq, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(blk + o_we, we.data(), sizeof(long long) * nseq, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(blk + o_out, out_init.data(), out_bytes, cudaMemcpyHostToDevice, c->stream));
+  c->last_h2d = seqs_len + (int64_t) (2 * sizeof(long long) * nseq + out_bytes + sizeof(Control));
+
+  const bool gl = P->arena_global != 0;
+  int cps = c->ctas_per_sm;
+  if (cps == 0) {
+#ifndef CMGB_HOST_EMULATION
+    int nb = 1;
+    if (tr) CUDA_TRY(prepare_tr_any(alg, gl, c->threads, P->smem_bytes, &nb));
+    else CUDA_TRY(prepare_any(alg, gl, c->threads, P->smem_bytes, &nb));
+    cps = nb < 1 ? 1 : nb;
+#else
+    cps = 1;
+#endif
+  }
+  const int grid = std::min(nseq, c->nsm * cps);
+  if ((st = grow((void **) &c->d_carry, &c->carry_bytes, sizeof(float) * 2 * (size_t) P->carry_elems * grid, errbuf)) != CMGB_OK) return st;
+  if ((st = grow((void **) &c->d_ring, &c->ring_bytes, sizeof(float) * (size_t) P->ring_elems * grid, errbuf)) != CMGB_OK) return st;
+  if (gl && (st = grow((void **) &c->d_arena, &c->arena_bytes, sizeof(float) * (size_t) P->arena_elems * grid, errbuf)) != CMGB_OK) return st;
+  if (tr && (st = grow((void **) &c->d_trcand, &c->trcand_bytes, sizeof(TrCand) * (size_t) kTrCandCap, errbuf)) != CMGB_OK) return st;
+  Control *h = c->h_ctl;
+  std::memset(h, 0, sizeof(Control));
+  CUDA_TRY(cudaMemcpyAsync(c->d_ctl, h, sizeof(Control), cudaMemcpyHostToDevice, c->stream));
+  const bool greedy = !(m->flags & CMGB_NOTGREEDY);
+  const float ccut = hitlist ? cutoff : 3.0e38f;
+  const int cpos = (hitlist && !greedy) ? 1 : 0;
+  const float ecut = (ret_envi || ret_envj) ? env_cutoff : 3.0e38f;
+
+  CUDA_TRY(cudaEventRecord(c->ev0, c->stream));
+  if (tr) {
+    TrKParams kp;
+    std::memset(&kp, 0, sizeof(kp));
+    kp.st = (const TrStateInfo *) d_states; kp.plan = *P; kp.arena = c->d_arena;
+    kp.oesc = m->d_oesc; kp.ioesc = m->d_ioesc;
+    kp.lmesc = m->d_lmesc; kp.rmesc = m->d_rmesc; kp.ilmesc = m->d_ilmesc; kp.irmesc = m->d_irmesc;
+    kp.ilog = c->d_ilog;
+    kp.dsq = blk; kp.i0 = 1; kp.j0 = seqs_len - 2; kp.win_len = 0; kp.nwin = nseq;
+    kp.queue = &c->d_ctl->queue; kp.carry = c->d_carry; kp.ring = c->d_ring;
+    kp.cand = c->d_trcand; kp.ncand = &c->d_ctl->ncand; kp.cand_cap = kTrCandCap;
+    kp.cand_cut = ccut; kp.cand_pos = cpos; kp.env_cut = ecut;
+    kp.fill_L = fill_L; kp.fill_R = fill_R; kp.fill_T = fill_T; kp.pty_idx = pty_idx;
+    kp.vsc = nullptr; kp.winbest = reinterpret_cast<unsigned long long *>(blk + o_out); kp.wmax = nullptr;
+    kp.err = &c->d_ctl->err;
+    kp.win_s = reinterpret_cast<const long long *>(blk + o_ws); kp.win_e = reinterpret_cast<const long long *>(blk + o_we);
+    launch_tr_any(alg, gl, grid, c->threads, (size_t) P->smem_bytes, c->stream, kp);
+  } else {
+    KParams kp;
+    std::memset(&kp, 0, sizeof(kp));
+    kp.st = (const StateInfo *) d_states; kp.plan = *P; kp.rec = d_rec; kp.arena = c->d_arena;
+    kp.oesc = m->d_oesc; kp.ioesc = m->d_ioesc; kp.ilog = c->d_ilog; kp.flog = c->d_flog;
+    kp.dsq = blk; kp.i0 = 1; kp.j0 = seqs_len - 2; kp.win_len = 0; kp.nwin = nseq;
+    kp.queue = &c->d_ctl->queue; kp.carry = c->d_carry; kp.ring = c->d_ring;
+    kp.cand = c->d_cand; kp.ncand = &c->d_ctl->ncand; kp.cand_cap = kCandCap;
+    kp.cand_cut = ccut; kp.cand_pos = cpos; kp.env_cut = ecut;
+    kp.env = reinterpret_cast<long long *>(blk + o_out);
+    kp.best = reinterpret_cast<unsigned *>(blk + o_out + sizeof(long long) * 2 * nseq);
+    kp.vsc = nullptr; kp.err = &c->d_ctl->err;
+    kp.win_s = reinterpret_cast<const long long *>(blk + o_ws); kp.win_e = reinterpret_cast<const long long *>(blk + o_we);
+    launch_any(alg, gl, grid, c->threads, (size_t) P->smem_bytes, c->stream, kp);
+  }
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaEventRecord(c->ev1, c->stream));
+  std::vector<unsigned char> outv(out_bytes);
+  CUDA_TRY(cudaMemcpyAsync(h, c->d_ctl, sizeof(Control), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(outv.data(), blk + o_out, out_bytes, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  CUDA_TRY(cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1));
+  c->last_launches = 1;
+  c->last_d2h = (int64_t) (sizeof(Control) + out_bytes);
+  if (h->err & 2) ERRF(CMGB_ENODEV, "%s, a bounded device wait ran out (phase record copy)", fn);
+  if (h->err & 1) ERRF(CMGB_ERANGE, "%s, more than %d candidate root cells; raise the cutoff", fn, tr ? kTrCandCap : kCandCap);
+  auto u2f = [](unsigned u) { if (u == 0) return CMGB_IMPOSSIBLE; unsigned b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u; float f; std::memcpy(&f, &b, 4); return f; };
+
+  // per-sequence candidate lists (absolute coordinates in the buffer)
+  const int n = h->ncand;
+  std::vector<std::vector<CandHost>> per(nseq);
+  std::vector<int64_t> envi(nseq), envj(nseq);
+  for (int q = 0; q < nseq; q++) { envi[q] = offsets[q] + lengths[q] + 1; envj[q] = offsets[q]; }
+  if (tr) {
+    std::vector<TrCand> tc((size_t) n);
+    if (n > 0) CUDA_TRY(cudaMemcpy(tc.data(), c->d_trcand, sizeof(TrCand) * (size_t) n, cudaMemcpyDeviceToHost));
+    c->last_d2h += (int64_t) sizeof(TrCand) * n;
+    std::sort(tc.begin(), tc.end(), [](const TrCand &a, const TrCand &b) {
+      if (a.j != b.j) return a.j < b.j;
+      if (a.d != b.d) return a.d < b.d;
+      return a.mode > b.mode;
+    });
+    size_t q = 0;
+    while (q < tc.size()) {   // each cell registered within its own (whole-sequence) window: keep the best mode
+      size_t e = q, wq = q;
+      while (e < tc.size() && tc[e].j == tc[q].j && tc[e].d == tc[q].d) {
+        if (tc[e].f > tc[wq].f || (tc[e].f == tc[wq].f && tc[e].y < tc[wq].y)) wq = e;
+        e++;
+      }
+      const TrCand &t = tc[wq];
+      const int sq = order[t.win];
+      if (t.f >= env_cutoff) { envi[sq] = std::min<int64_t>(envi[sq], t.j - t.d + 1); envj[sq] = std::max<int64_t>(envj[sq], t.j); }
+      if (hitlist) { CandHost ch; ch.j = t.j; ch.d = t.d; ch.sc = t.f; ch.r = t.y; ch.mode = t.mode; per[sq].push_back(ch); }
+      q = e;
+    }
+    const unsigned long long *wb = reinterpret_cast<const unsigned long long *>(outv.data());
+    for (int w = 0; w < nseq; w++) {
+      const int sq = order[w];
+      const unsigned long long k = wb[w];
+      if (ret_sc) ret_sc[sq] = k ? u2f((unsigned) (k >> 32)) : CMGB_IMPOSSIBLE;
+      if (ret_mode) ret_mode[sq] = k ? 3 - (int) ((0xFFFFFFFFu - (unsigned) (k & 0xFFFFFFFFULL)) & 3u) : CMGB_TRMODE_UNKNOWN;
+    }
+  } else {
+    if (hitlist && n > 0) {
+      c->h_cand.resize((size_t) n);
+      CUDA_TRY(cudaMemcpy(c->h_cand.data(), c->d_cand, sizeof(Cand) * (size_t) n, cudaMemcpyDeviceToHost));
+      c->last_d2h += (int64_t) sizeof(Cand) * n;
+      std::vector<int> by_off(nseq);
+      for (int q = 0; q < nseq; q++) by_off[q] = q;
+      std::sort(by_off.begin(), by_off.end(), [&](int a, int b) { return offsets[a] < offsets[b]; });
+      for (const CandHost &ch : c->h_cand) {
+        int lo = 0, hi = nseq - 1;   // last sequence whose offset is below j
+        while (lo < hi) { const int mid = (lo + hi + 1) / 2; if (offsets[by_off[mid]] < ch.j) lo = mid; else hi = mid - 1; }
+        CandHost x = ch; x.mode = CMGB_TRMODE_J;
+        per[by_off[lo]].push_back(x);
+      }
+    }
+    const long long *env = reinterpret_cast<const long long *>(outv.data());
+    const unsigned *best = reinterpret_cast<const unsigned *>(outv.data() + sizeof(long long) * 2 * nseq);
+    for (int w = 0; w < nseq; w++) {
+      const int sq = order[w];
+      if (env[2 * w + 1] >= 0) { envi[sq] = env[2 * w]; envj[sq] = env[2 * w + 1]; }
+      if (ret_sc) ret_sc[sq] = u2f(best[w]);
+      if (ret_mode) ret_mode[sq] = CMGB_TRMODE_J;
+    }
+  }
+  for (int q = 0; q < nseq; q++) {
+    const int64_t off = offsets[q];
+    if (ret_envi) ret_envi[q] = envj[q] < off + 1 ? -1 : envi[q] - off;
+    if (ret_envj) ret_envj[q] = envj[q] < off + 1 ? -1 : envj[q] - off;
+    int64_t before = hitlist ? (int64_t) hitlist->h.size() : 0;
+    if (hitlist && !per[q].empty()) {
+      TruncFilter tf;
+      ResolveArgs ra;
+      ra.null = m->null.data(); ra.K = m->K; ra.null3_omega = m->null3_omega; ra.do_null3 = do_null3;
+      ra.greedy = greedy ? 1 : 0; ra.cutoff = cutoff; ra.i0 = off + 1; ra.j0 = off + lengths[q]; ra.dsq = seqs;
+      if (tr) {
+        tf.pass_idx = pass_idx; tf.local = (m->flags & CMGB_LOCAL_BEGIN) ? 1 : 0; tf.clen = m->clen;
+        tf.ndidx = m->ndidx.data(); tf.ndtype = m->ndtype.data(); tf.lpos = m->emap_lpos.data(); tf.rpos = m->emap_rpos.data();
+        ra.tr = &tf;
+      }
+      resolve_hits(per[q], ra, hitlist->h);
+      for (size_t k = (size_t) before; k < hitlist->h.size(); k++) { hitlist->h[k].start -= off; hitlist->h[k].stop -= off; }
+    }
+    if (ret_nhits) ret_nhits[q] = hitlist ? (int64_t) hitlist->h.size() - before : 0;
+  }
+  return CMGB_OK;
+}
+
 // Times candidate shapes (tile rows x arena placement) of band set qdbidx and
 // algorithm (0 CYK, 1 integer Inside, 2 float Inside) on a seeded iid sample and keeps the
 // fastest for this model; later scans that leave the shape to the library use it.

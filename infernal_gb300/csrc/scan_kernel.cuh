@@ -132,6 +132,9 @@ struct KParams {
   int *err;                   // error word: 1 candidate overflow, 2 a bounded wait ran out
   const unsigned char *rec;   // phase records (descriptor + emission row), see build_records
   float *arena;               // [grid][arena_elems] global tile arena (plans with arena_global)
+  // batched scans: window w is the whole scan [win_s[w], win_e[w]] of one
+  // sequence (no warm-up rows); env and best are then per-window arrays
+  const long long *win_s, *win_e;
 };
 
 // Order-preserving float <-> uint mapping for atomicMax.
@@ -289,11 +292,15 @@ CMGB_DEV void qdb_scan_body(const KParams &p, float *smf, int tid, int nt, int b
     CMGB_SYNC();
     const int w = *s_win;
     if (w >= p.nwin) break;
-    const long long own_s = p.i0 + (long long) w * p.win_len;
-    long long own_e = own_s + p.win_len - 1;
-    if (own_e > p.j0) own_e = p.j0;
-    long long s0 = own_s - (W - 1);
-    if (s0 < p.i0) s0 = p.i0;
+    long long own_s, own_e, s0;
+    if (p.win_s) { own_s = s0 = p.win_s[w]; own_e = p.win_e[w]; }
+    else {
+      own_s = p.i0 + (long long) w * p.win_len;
+      own_e = own_s + p.win_len - 1;
+      if (own_e > p.j0) own_e = p.j0;
+      s0 = own_s - (W - 1);
+      if (s0 < p.i0) s0 = p.i0;
+    }
     const int own_jp = (int) (own_s - s0 + 1);   // first owned row, in window coordinates
     const int last_jp = (int) (own_e - s0 + 1);
 
@@ -566,6 +573,11 @@ CMGB_DEV void qdb_scan_body(const KParams &p, float *smf, int tid, int nt, int b
         }
         CMGB_SYNC();
       }
+    }
+    if (p.win_s) {   // batched scans: envelope and best score of this sequence
+      if (envj >= 0) { CMGB_ATOMIC_MINLL(p.env + 2 * w, envi); CMGB_ATOMIC_MAXLL(p.env + 2 * w + 1, envj); }
+      if (best_root > CMGB_IMP) CMGB_ATOMIC_MAXU(p.best + w, cmgb_f2u(best_root));
+      envi = 0x7fffffffffffffffLL; envj = -1; best_root = CMGB_IMP;
     }
   }
   // every record copy was waited for by thread 0 before the barrier that followed it

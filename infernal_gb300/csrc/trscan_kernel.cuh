@@ -63,8 +63,10 @@ struct TrKParams {
   int pty_idx;                // truncation penalty index of the pass
   unsigned *vsc;              // per-state best score (order-preserving uint), NULL if not wanted
   unsigned long long *winbest;// [nwin] best root cell of each window: score << 32 | ~position
-  float *wmax;                // [nwin][4][2][acc_w] root running maxima at window end (native type)
+  float *wmax;                // [nwin][4][2][acc_w] root running maxima at window end (native type), or NULL
   int *err;                   // 1: candidate overflow
+  // batched scans: window w is the whole scan [win_s[w], win_e[w]] of one sequence (no warm-up rows)
+  const long long *win_s, *win_e;
 };
 
 template <int ALG, bool GL>
@@ -105,11 +107,15 @@ CMGB_DEV void tr_scan_body(const TrKParams &p, float *smf, int tid, int nt, int 
     CMGB_SYNC();
     const int w = *s_win;
     if (w >= p.nwin) break;
-    const long long own_s = p.i0 + (long long) w * p.win_len;
-    long long own_e = own_s + p.win_len - 1;
-    if (own_e > p.j0) own_e = p.j0;
-    long long s0 = own_s - (W - 1);
-    if (s0 < p.i0) s0 = p.i0;
+    long long own_s, own_e, s0;
+    if (p.win_s) { own_s = s0 = p.win_s[w]; own_e = p.win_e[w]; }
+    else {
+      own_s = p.i0 + (long long) w * p.win_len;
+      own_e = own_s + p.win_len - 1;
+      if (own_e > p.j0) own_e = p.j0;
+      s0 = own_s - (W - 1);
+      if (s0 < p.i0) s0 = p.i0;
+    }
     const int own_jp = (int) (own_s - s0 + 1);
     const int last_jp = (int) (own_e - s0 + 1);
 
@@ -470,8 +476,10 @@ CMGB_DEV void tr_scan_body(const TrKParams &p, float *smf, int tid, int nt, int 
       }
     }
     // window outputs: final running maxima and the best root cell
-    T *wm = reinterpret_cast<T *>(p.wmax) + (size_t) w * 8 * accw;
-    for (int q = tid; q < 8 * accw; q += nt) wm[q] = rmax[q];
+    if (p.wmax) {
+      T *wm = reinterpret_cast<T *>(p.wmax) + (size_t) w * 8 * accw;
+      for (int q = tid; q < 8 * accw; q += nt) wm[q] = rmax[q];
+    }
     if (my_best) CMGB_ATOMIC_MAXULL(p.winbest + w, my_best);
   }
 }

@@ -36,7 +36,9 @@ EXPORTS = [
     "cmgb_FastIInsideScan_dev", "cmgb_count_cells", "cmgb_autotune", "cmgb_FastCYKScan_noalloc",
     "cmgb_FastFInsideScan", "cmgb_FastFInsideScan_dev",
     "cmgb_RefTrCYKScan", "cmgb_RefITrInsideScan", "cmgb_RefTrCYKScan_dev", "cmgb_RefITrInsideScan_dev",
+    "cmgb_ScanBatch",
 ]
+BATCH_ALGOS = {"cyk": 0, "inside": 1, "finside": 2, "trcyk": 3, "trinside": 4}
 
 _SCAN_ARGS = [P, P, ctypes.c_char_p, I, P, I64, I64, F, P, I, F, P, P, P, P]
 _TR_SCAN_ARGS = [P, P, ctypes.c_char_p, I, I, P, I64, I64, F, P, I, F, P, P, P, P, P]
@@ -94,6 +96,8 @@ def bind(path: str) -> ctypes.CDLL:
         f = getattr(lib, name)
         f.argtypes = _TR_SCAN_ARGS
         f.restype = I
+    lib.cmgb_ScanBatch.argtypes = [P, P, ctypes.c_char_p, I, I, I, P, I64, P, P, I, F, P, I, F, P, P, P, P, P]
+    lib.cmgb_ScanBatch.restype = I
     lib.cmgb_autotune.argtypes = [P, P, I, I, I64, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.c_char_p]
     lib.cmgb_autotune.restype = I
     lib.cmgb_FastCYKScan_noalloc.argtypes = [P, P, ctypes.c_char_p, I, P, I64, I64, F, F, P, I, ctypes.POINTER(I),
@@ -243,6 +247,47 @@ class Scanner:
                 self.lib.cmgb_hitlist_destroy(hl)
         return ScanResult(hits, envi.value, envj.value, sc.value, vsc,
                           float(self.lib.cmgb_ctx_last_kernel_ms(self._ctx)), mode.value)
+
+    def scan_batch(self, m: cmfile.CMModel, seqs, algo: str = "cyk", qdbidx: int = 1, pass_idx: int = 4,
+                   cutoff: float = 0.0, do_null3: bool = True, env_cutoff: float = 0.0, want_hits: bool = True,
+                   notgreedy: bool = False) -> List[ScanResult]:
+        """Runs cmgb_ScanBatch over a list of digital sequences (each an Easel
+        dsq with sentinels), scanning each over [1, L]; returns one
+        ScanResult per sequence (vsc is None)."""
+        mh = self.model(m, CMGB_NOTGREEDY if notgreedy else 0)
+        parts = [np.ascontiguousarray(x, dtype=np.uint8) for x in seqs]
+        lens = np.array([len(x) - 2 for x in parts], np.int64)
+        offs = np.zeros(len(parts), np.int64)
+        if len(parts) > 1:
+            offs[1:] = np.cumsum([len(x) for x in parts[:-1]])
+        buf = np.concatenate(parts + [np.full(1, cmfile.DSQ_SENTINEL, np.uint8)])
+        nseq = len(parts)
+        nh, ei, ej = np.zeros(nseq, np.int64), np.zeros(nseq, np.int64), np.zeros(nseq, np.int64)
+        sc, mode = np.zeros(nseq, np.float32), np.zeros(nseq, np.int32)
+        hl = self.lib.cmgb_hitlist_create() if want_hits else None
+        err = ctypes.create_string_buffer(256)
+        try:
+            st = self.lib.cmgb_ScanBatch(self._ctx, mh, err, BATCH_ALGOS[algo], qdbidx, pass_idx, buf.ctypes.data,
+                                         len(buf), offs.ctypes.data, lens.ctypes.data, nseq, cutoff, hl,
+                                         int(do_null3), env_cutoff, nh.ctypes.data, ei.ctypes.data, ej.ctypes.data,
+                                         sc.ctypes.data, mode.ctypes.data)
+            if st != 0:
+                raise ScanError(st, err.value.decode())
+            allhits = []
+            if hl:
+                h = Hit()
+                for k in range(self.lib.cmgb_hitlist_count(hl)):
+                    self.lib.cmgb_hitlist_get(hl, k, ctypes.byref(h))
+                    allhits.append((h.start, h.stop, h.root, h.mode, h.score))
+        finally:
+            if hl:
+                self.lib.cmgb_hitlist_destroy(hl)
+        ms = float(self.lib.cmgb_ctx_last_kernel_ms(self._ctx))
+        out, k = [], 0
+        for q in range(nseq):
+            out.append(ScanResult(allhits[k: k + int(nh[q])], int(ei[q]), int(ej[q]), float(sc[q]), None, ms, int(mode[q])))
+            k += int(nh[q])
+        return out
 
     def autotune(self, m: cmfile.CMModel, qdbidx: int, algo: str = "cyk", sample_len: int = 0):
         """Runs cmgb_autotune for (model, band set, algorithm); returns (tile_rows, arena)."""

@@ -67,7 +67,7 @@ def test_count_cells_matches_oracle(built_lib, models):
 def test_emulated_kernel_matches_oracle(emu, models, name, algo, qdb, T, win, arena):
     m = models[name]
     rng = np.random.default_rng(11)
-    n = 400 if name == "Plant_SRP" else 600
+    n = 220 if name == "Plant_SRP" else 350
     dsq = cmfile.digitize("".join(rng.choice(list("ACGU"), n)))
     emu.set_shape(T, win, 1, 0, arena)
     r = emu.scan(m, dsq, 1, n, algo=algo, qdbidx=qdb, cutoff=-2.0, env_cutoff=1.0, want_vsc=True)
