@@ -620,7 +620,18 @@ extern "C" int cmgb_FastFInsideScan_dev(cmgb_ctx *c, cmgb_model *m, char *errbuf
 
 // ---------------------------------------------------------------------------
 // Truncated scanners (RefTrCYKScan / RefITrInsideScan).
-static const int kTrCandCap = 1 << 21;
+static const int kTrCandCap = 1 << 21;          // initial truncated candidate capacity (grows on demand)
+static const int64_t kTrCandMax = (int64_t) 1 << 27;
+
+// Capacity of the context's truncated candidate buffer, grown to at least `need` entries.
+static int tr_cand_reserve(cmgb_ctx *c, int64_t need, int *cap, char *errbuf)
+{
+  if (need > kTrCandMax) ERRF(CMGB_ERANGE, "more than %lld candidate root cells; raise the cutoff", (long long) kTrCandMax);
+  int st = grow((void **) &c->d_trcand, &c->trcand_bytes, sizeof(TrCand) * (size_t) std::max<int64_t>(need, kTrCandCap), errbuf);
+  if (st != CMGB_OK) return st;
+  *cap = (int) std::min<int64_t>((int64_t) (c->trcand_bytes / sizeof(TrCand)), kTrCandMax);
+  return CMGB_OK;
+}
 
 static int get_tr_plan(cmgb_model *m, int qdbidx, int alg, DevTrPlan **ret, char *errbuf)
 {
@@ -731,7 +742,8 @@ static int scan_tr(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, int pas
   if ((st = grow((void **) &c->d_carry, &c->carry_bytes, carry_need, errbuf)) != CMGB_OK) return st;
   if ((st = grow((void **) &c->d_ring, &c->ring_bytes, ring_need, errbuf)) != CMGB_OK) return st;
   if (gl && (st = grow((void **) &c->d_arena, &c->arena_bytes, sizeof(float) * (size_t) P.arena_elems * grid, errbuf)) != CMGB_OK) return st;
-  if ((st = grow((void **) &c->d_trcand, &c->trcand_bytes, sizeof(TrCand) * (size_t) kTrCandCap, errbuf)) != CMGB_OK) return st;
+  int cand_cap = 0;
+  if ((st = tr_cand_reserve(c, kTrCandCap, &cand_cap, errbuf)) != CMGB_OK) return st;
   if ((st = grow((void **) &c->d_winbest, &c->winbest_bytes, sizeof(unsigned long long) * (size_t) nwin, errbuf)) != CMGB_OK) return st;
   if ((st = grow((void **) &c->d_wmax, &c->wmax_bytes, sizeof(float) * 8 * (size_t) accw * nwin, errbuf)) != CMGB_OK) return st;
   if (ret_vsc && c->vsc_len < m->M) {
@@ -739,7 +751,11 @@ static int scan_tr(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, int pas
     if (cudaMalloc(&c->d_vsc, sizeof(unsigned) * m->M) != cudaSuccess) ERRF(CMGB_EMEM, "out of device memory");
     c->vsc_len = m->M;
   }
+  const bool greedy = !(m->flags & CMGB_NOTGREEDY);
   Control *h = c->h_ctl;
+  std::vector<unsigned long long> winbest((size_t) nwin);
+  std::vector<unsigned> vscu;
+  for (int attempt = 0;; attempt++) {   // a second launch only when the candidate buffer was too small
   std::memset(h, 0, sizeof(Control));
   CUDA_TRY(cudaMemcpyAsync(c->d_ctl, h, sizeof(Control), cudaMemcpyHostToDevice, c->stream));
   CUDA_TRY(cudaMemsetAsync(c->d_winbest, 0, sizeof(unsigned long long) * (size_t) nwin, c->stream));
@@ -753,8 +769,7 @@ static int scan_tr(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, int pas
   kp.ilog = c->d_ilog;
   kp.dsq = d_dsq; kp.i0 = i0; kp.j0 = j0; kp.win_len = win; kp.nwin = (int) nwin;
   kp.queue = &c->d_ctl->queue; kp.carry = c->d_carry; kp.ring = c->d_ring;
-  kp.cand = c->d_trcand; kp.ncand = &c->d_ctl->ncand; kp.cand_cap = kTrCandCap;
-  const bool greedy = !(m->flags & CMGB_NOTGREEDY);
+  kp.cand = c->d_trcand; kp.ncand = &c->d_ctl->ncand; kp.cand_cap = cand_cap;
   kp.cand_cut = cutoff; kp.cand_pos = (hitlist && !greedy) ? 1 : 0;
   if (!hitlist) { kp.cand_cut = 3.0e38f; kp.cand_pos = 0; }
   kp.env_cut = (ret_envi || ret_envj) ? env_cutoff : 3.0e38f;
@@ -768,15 +783,16 @@ static int scan_tr(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, int pas
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaEventRecord(c->ev1, c->stream));
   CUDA_TRY(cudaMemcpyAsync(h, c->d_ctl, sizeof(Control), cudaMemcpyDeviceToHost, c->stream));
-  std::vector<unsigned long long> winbest((size_t) nwin);
   CUDA_TRY(cudaMemcpyAsync(winbest.data(), c->d_winbest, sizeof(unsigned long long) * (size_t) nwin, cudaMemcpyDeviceToHost, c->stream));
-  std::vector<unsigned> vscu;
   if (ret_vsc) { vscu.resize(m->M); CUDA_TRY(cudaMemcpyAsync(vscu.data(), c->d_vsc, sizeof(unsigned) * m->M, cudaMemcpyDeviceToHost, c->stream)); }
   CUDA_TRY(cudaStreamSynchronize(c->stream));
   CUDA_TRY(cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1));
-  c->last_launches = 1;
+  c->last_launches = attempt + 1;
   c->last_d2h = (int64_t) sizeof(Control) + (int64_t) sizeof(unsigned long long) * nwin + (ret_vsc ? (int64_t) sizeof(unsigned) * m->M : 0);
-  if (h->err & 1) ERRF(CMGB_ERANGE, "%s, more than %d candidate root cells; raise the cutoff", fn, kTrCandCap);
+  if (!(h->err & 1)) break;
+  if (attempt > 0) ERRF(CMGB_ERANGE, "%s, more than %d candidate root cells; raise the cutoff", fn, cand_cap);
+  if ((st = tr_cand_reserve(c, (int64_t) h->ncand + h->ncand / 4, &cand_cap, errbuf)) != CMGB_OK) return st;
+  }
 
   auto u2f = [](unsigned u) { if (u == 0) return CMGB_IMPOSSIBLE; unsigned b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u; float f; std::memcpy(&f, &b, 4); return f; };
   // best parse over all windows: highest score, earliest window on ties
@@ -977,14 +993,18 @@ extern "C" int cmgb_ScanBatch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo
   if ((st = grow((void **) &c->d_carry, &c->carry_bytes, sizeof(float) * 2 * (size_t) P->carry_elems * grid, errbuf)) != CMGB_OK) return st;
   if ((st = grow((void **) &c->d_ring, &c->ring_bytes, sizeof(float) * (size_t) P->ring_elems * grid, errbuf)) != CMGB_OK) return st;
   if (gl && (st = grow((void **) &c->d_arena, &c->arena_bytes, sizeof(float) * (size_t) P->arena_elems * grid, errbuf)) != CMGB_OK) return st;
-  if (tr && (st = grow((void **) &c->d_trcand, &c->trcand_bytes, sizeof(TrCand) * (size_t) kTrCandCap, errbuf)) != CMGB_OK) return st;
+  int cand_cap = kCandCap;
+  if (tr && (st = tr_cand_reserve(c, kTrCandCap, &cand_cap, errbuf)) != CMGB_OK) return st;
   Control *h = c->h_ctl;
-  std::memset(h, 0, sizeof(Control));
-  CUDA_TRY(cudaMemcpyAsync(c->d_ctl, h, sizeof(Control), cudaMemcpyHostToDevice, c->stream));
+  std::vector<unsigned char> outv(out_bytes);
   const bool greedy = !(m->flags & CMGB_NOTGREEDY);
   const float ccut = hitlist ? cutoff : 3.0e38f;
   const int cpos = (hitlist && !greedy) ? 1 : 0;
   const float ecut = (ret_envi || ret_envj) ? env_cutoff : 3.0e38f;
+  for (int attempt = 0;; attempt++) {   // a second launch only when the candidate buffer was too small
+  std::memset(h, 0, sizeof(Control));
+  CUDA_TRY(cudaMemcpyAsync(c->d_ctl, h, sizeof(Control), cudaMemcpyHostToDevice, c->stream));
+  if (attempt > 0) CUDA_TRY(cudaMemcpyAsync(blk + o_out, out_init.data(), out_bytes, cudaMemcpyHostToDevice, c->stream));
 
   CUDA_TRY(cudaEventRecord(c->ev0, c->stream));
   if (tr) {
@@ -996,7 +1016,7 @@ extern "C" int cmgb_ScanBatch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo
     kp.ilog = c->d_ilog;
     kp.dsq = blk; kp.i0 = 1; kp.j0 = seqs_len - 2; kp.win_len = 0; kp.nwin = nseq;
     kp.queue = &c->d_ctl->queue; kp.carry = c->d_carry; kp.ring = c->d_ring;
-    kp.cand = c->d_trcand; kp.ncand = &c->d_ctl->ncand; kp.cand_cap = kTrCandCap;
+    kp.cand = c->d_trcand; kp.ncand = &c->d_ctl->ncand; kp.cand_cap = cand_cap;
     kp.cand_cut = ccut; kp.cand_pos = cpos; kp.env_cut = ecut;
     kp.fill_L = fill_L; kp.fill_R = fill_R; kp.fill_T = fill_T; kp.pty_idx = pty_idx;
     kp.vsc = nullptr; kp.winbest = reinterpret_cast<unsigned long long *>(blk + o_out); kp.wmax = nullptr;
@@ -1020,15 +1040,17 @@ extern "C" int cmgb_ScanBatch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo
   }
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaEventRecord(c->ev1, c->stream));
-  std::vector<unsigned char> outv(out_bytes);
   CUDA_TRY(cudaMemcpyAsync(h, c->d_ctl, sizeof(Control), cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(cudaMemcpyAsync(outv.data(), blk + o_out, out_bytes, cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(cudaStreamSynchronize(c->stream));
   CUDA_TRY(cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1));
-  c->last_launches = 1;
+  c->last_launches = attempt + 1;
   c->last_d2h = (int64_t) (sizeof(Control) + out_bytes);
   if (h->err & 2) ERRF(CMGB_ENODEV, "%s, a bounded device wait ran out (phase record copy)", fn);
-  if (h->err & 1) ERRF(CMGB_ERANGE, "%s, more than %d candidate root cells; raise the cutoff", fn, tr ? kTrCandCap : kCandCap);
+  if (!(h->err & 1)) break;
+  if (!tr || attempt > 0) ERRF(CMGB_ERANGE, "%s, more than %d candidate root cells; raise the cutoff", fn, cand_cap);
+  if ((st = tr_cand_reserve(c, (int64_t) h->ncand + h->ncand / 4, &cand_cap, errbuf)) != CMGB_OK) return st;
+  }
   auto u2f = [](unsigned u) { if (u == 0) return CMGB_IMPOSSIBLE; unsigned b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u; float f; std::memcpy(&f, &b, 4); return f; };
 
   // per-sequence candidate lists (absolute coordinates in the buffer)

@@ -69,6 +69,10 @@ struct TrKParams {
   const long long *win_s, *win_e;
 };
 
+// Child loop with a compile-time trip count: the per-child arrays (scores,
+// buffer offsets, strides) stay in registers instead of local memory.
+#define CMGB_FOR_CHILD(o, first) _Pragma("unroll") for (int o = (first); o < CMGB_MAXC; o++) if (o < cnum)
+
 template <int ALG, bool GL>
 CMGB_DEV void tr_scan_body(const TrKParams &p, float *smf, int tid, int nt, int bid)
 {
@@ -254,7 +258,7 @@ CMGB_DEV void tr_scan_body(const TrKParams &p, float *smf, int tid, int nt, int 
               if (d < 1 || d > dx) val = imp;
               else {
                 val = INIT(d);
-                for (int o = 1; o < cnum; o++)
+                CMGB_FOR_CHILD(o, 1)
                   val = R::comb(val, R::comb(R::add(CHV(o, 0, r, d), tv[o]), R::add(CHV(o, pm, r, d), tv[o]), tbl), tbl);
               }
               own[pm * mst + r * stride + d] = val;
@@ -286,7 +290,7 @@ CMGB_DEV void tr_scan_body(const TrKParams &p, float *smf, int tid, int nt, int 
                       if (m == 1 && d == 1) x = e;
                       else {
                         T s = R::comb(INIT(d - 1), R::add(x, tv[0]), tbl);
-                        for (int o = 1; o < cnum; o++) s = R::comb(s, R::add(CHV(o, m, r, d - 1), tv[o]), tbl);
+                        CMGB_FOR_CHILD(o, 1) s = R::comb(s, R::add(CHV(o, m, r, d - 1), tv[o]), tbl);
                         x = R::add(s, e);
                       }
                       row[d] = x;
@@ -321,13 +325,13 @@ CMGB_DEV void tr_scan_body(const TrKParams &p, float *smf, int tid, int nt, int 
                 else {
                   const T ej = ESC1(res[W + r - 1]);
                   T s = R::comb(INIT(d - 1), R::add(xJ, tv[0]), tbl);
-                  for (int o = 1; o < cnum; o++) s = R::comb(s, R::add(CHV(o, 0, r - 1, d - 1), tv[o]), tbl);
+                  CMGB_FOR_CHILD(o, 1) s = R::comb(s, R::add(CHV(o, 0, r - 1, d - 1), tv[o]), tbl);
                   vJ = R::add(s, ej);
                   if (fR) {
                     if (d == 1) vR = ej;
                     else {
                       T s2 = R::comb(INIT(d - 1), R::add(xR, tv[0]), tbl);
-                      for (int o = 1; o < cnum; o++) s2 = R::comb(s2, R::add(CHV(o, 2, r - 1, d - 1), tv[o]), tbl);
+                      CMGB_FOR_CHILD(o, 1) s2 = R::comb(s2, R::add(CHV(o, 2, r - 1, d - 1), tv[o]), tbl);
                       vR = R::add(s2, ej);
                     }
                   } else vR = imp;
@@ -395,7 +399,7 @@ CMGB_DEV void tr_scan_body(const TrKParams &p, float *smf, int tid, int nt, int 
             } else if (emit == 0) {
               // S, D, BEGL_S: every mode from the same mode of the children
               vJ = INIT(d); vL = vJ; vR = vJ;
-              for (int o = 0; o < cnum; o++) {
+              CMGB_FOR_CHILD(o, 0) {
                 vJ = R::comb(vJ, R::add(CHV(o, 0, r, d), tv[o]), tbl);
                 if (fL) vL = R::comb(vL, R::add(CHV(o, 1, r, d), tv[o]), tbl);
                 if (fR) vR = R::comb(vR, R::add(CHV(o, 2, r, d), tv[o]), tbl);
@@ -404,7 +408,7 @@ CMGB_DEV void tr_scan_body(const TrKParams &p, float *smf, int tid, int nt, int 
               // ML (src/cm_dpsearch_trunc.c:341-380)
               const T e = ESC1(res[W + r - d]);
               vJ = INIT(d - 1); vL = vJ;
-              for (int o = 0; o < cnum; o++) {
+              CMGB_FOR_CHILD(o, 0) {
                 vJ = R::comb(vJ, R::add(CHV(o, 0, r, d - 1), tv[o]), tbl);
                 if (fL) vL = R::comb(vL, R::add(CHV(o, 1, r, d - 1), tv[o]), tbl);
               }
@@ -412,14 +416,14 @@ CMGB_DEV void tr_scan_body(const TrKParams &p, float *smf, int tid, int nt, int 
               vL = d >= 2 ? R::add(vL, e) : e;
               if (fR) {
                 vR = INIT(d);
-                for (int o = 0; o < cnum; o++)
+                CMGB_FOR_CHILD(o, 0)
                   vR = R::comb(vR, R::comb(R::add(CHV(o, 0, r, d), tv[o]), R::add(CHV(o, 2, r, d), tv[o]), tbl), tbl);
               }
             } else if (emit == 2) {
               // MR (src/cm_dpsearch_trunc.c:381-420)
               const T ej = ESC1(res[W + r - 1]);
               vJ = INIT(d - 1); vR = vJ;
-              for (int o = 0; o < cnum; o++) {
+              CMGB_FOR_CHILD(o, 0) {
                 vJ = R::comb(vJ, R::add(CHV(o, 0, r - 1, d - 1), tv[o]), tbl);
                 if (fR) vR = R::comb(vR, R::add(CHV(o, 2, r - 1, d - 1), tv[o]), tbl);
               }
@@ -427,7 +431,7 @@ CMGB_DEV void tr_scan_body(const TrKParams &p, float *smf, int tid, int nt, int 
               vR = d >= 2 ? R::add(vR, ej) : ej;
               if (fL) {
                 vL = INIT(d);
-                for (int o = 0; o < cnum; o++)
+                CMGB_FOR_CHILD(o, 0)
                   vL = R::comb(vL, R::comb(R::add(CHV(o, 0, r, d), tv[o]), R::add(CHV(o, 1, r, d), tv[o]), tbl), tbl);
               }
             } else {
@@ -435,7 +439,7 @@ CMGB_DEV void tr_scan_body(const TrKParams &p, float *smf, int tid, int nt, int 
               const int xi = res[W + r - d], xj = res[W + r - 1];
               vJ = d >= 2 ? INIT(d - 2) : imp;
               vL = INIT(d - 1); vR = vL;
-              for (int o = 0; o < cnum; o++) {
+              CMGB_FOR_CHILD(o, 0) {
                 if (d >= 2) vJ = R::comb(vJ, R::add(CHV(o, 0, r - 1, d - 2), tv[o]), tbl);
                 if (fL) vL = R::comb(vL, MAXT(R::add(CHV(o, 0, r, d - 1), tv[o]), R::add(CHV(o, 1, r, d - 1), tv[o])), tbl);
                 if (fR) vR = R::comb(vR, MAXT(R::add(CHV(o, 0, r - 1, d - 1), tv[o]), R::add(CHV(o, 2, r - 1, d - 1), tv[o])), tbl);
@@ -486,7 +490,7 @@ CMGB_DEV void tr_scan_body(const TrKParams &p, float *smf, int tid, int nt, int 
 
 #ifndef CMGB_HOST_EMULATION
 template <int ALG, bool GL>
-__global__ void __launch_bounds__(512) tr_scan_kernel(TrKParams p)
+__global__ void __launch_bounds__(512, 1) tr_scan_kernel(TrKParams p)
 {
   extern __shared__ __align__(128) float smem_dyn[];
   tr_scan_body<ALG, GL>(p, smem_dyn, threadIdx.x, blockDim.x, blockIdx.x);

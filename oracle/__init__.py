@@ -25,7 +25,7 @@ ORACLE_SO = os.path.join(BUILD, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libinfernal_ref.so")
 
 P, I, I64, F = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_float
-ALGOS = {"cyk": 0, "inside": 1, "finside": 2}
+ALGOS = {"cyk": 0, "inside": 1, "finside": 2, "dinside": 3}
 REF_ALGOS = {"cyk": 0, "refcyk": 1, "inside": 2, "refinside": 3, "finside": 4, "reffinside": 5,
              "trcyk": 6, "trinside": 7}
 

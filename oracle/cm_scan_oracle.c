@@ -22,6 +22,8 @@
  *   report_greedy()       ReportHitsGreedily    src/cm_mx.c:7547-7628
  *   gamma_update/tback    UpdateGammaHitMx / TBackGammaHitMx src/cm_mx.c:7440-7669
  *   null3_correction()    ScoreCorrectionNull3  src/cm_parsetree.c:2352-2380
+ *   core_dinside()        FastFInsideScan's recursion in double with the exact
+ *                         log-sum (the FP64 yardstick, not a reference scanner)
  *   remove_overlaps()     cm_tophits_SortForOverlapRemoval + RemoveOrMarkOverlaps
  *                         src/cm_tophits.c:220-245, 400, 1097-1275
  *   oracle_tr_scan()      RefTrCYKScan          src/cm_dpsearch_trunc.c:79-700
@@ -46,7 +48,7 @@
 #define MAXF(a, b) (((a) > (b)) ? (a) : (b))
 #define MINF(a, b) (((a) < (b)) ? (a) : (b))
 
-enum { ORC_CYK = 0, ORC_IINS = 1, ORC_FINS = 2 };
+enum { ORC_CYK = 0, ORC_IINS = 1, ORC_FINS = 2, ORC_DINS = 3 };
 
 /* ---------------- log-sum tables (src/logsum.c) ---------------- */
 static int   ilog_tbl[LOGSUM_TBL];
@@ -248,6 +250,8 @@ static void report_j(scanctx *c, int64_t j, int64_t jp, int dn0, int dx0)
 #define ENVF(x) (x)
 #define TSC(v, o) m->tsc[(v) * MAXC + (o)]
 #define ESC(v) (m->oesc + (size_t) (v) * Kp * Kp)
+#define ESCT float
+#define EV(x) (x)
 #define BEGINSC(y) m->beginsc[y]
 #define HAS_BEGIN(y) NOT_IMP(m->beginsc[y])
 #define ENDSC(v) m->endsc[v]
@@ -263,6 +267,8 @@ static void report_j(scanctx *c, int64_t j, int64_t jp, int dn0, int dx0)
 #define ENVF(x) (x)
 #define TSC(v, o) m->tsc[(v) * MAXC + (o)]
 #define ESC(v) (m->oesc + (size_t) (v) * Kp * Kp)
+#define ESCT float
+#define EV(x) (x)
 #define BEGINSC(y) m->beginsc[y]
 #define HAS_BEGIN(y) NOT_IMP(m->beginsc[y])
 #define ENDSC(v) m->endsc[v]
@@ -278,10 +284,40 @@ static void report_j(scanctx *c, int64_t j, int64_t jp, int dn0, int dx0)
 #define ENVF(x) ((float) (x))
 #define TSC(v, o) m->itsc[(v) * MAXC + (o)]
 #define ESC(v) (m->ioesc + (size_t) (v) * Kp * Kp)
+#define ESCT int
+#define EV(x) (x)
 #define BEGINSC(y) m->ibeginsc[y]
 #define HAS_BEGIN(y) (m->ibeginsc[y] != -INFTY)
 #define ENDSC(v) m->iendsc[v]
 #define INIT_SC(v, d) ((m->iendsc[v] != -INFTY) ? m->iel_selfsc * (d) + m->iendsc[v] : -INFTY)
+#include "cm_scan_oracle_core.h"
+
+/* Double-precision Inside: the FastFInsideScan recursion in double with the
+ * exact log2(2^a + 2^b) instead of the FLogsum table, and IMPOSSIBLE scores
+ * mapped to -infinity.  Not a reference scanner: the yardstick for the
+ * table-based Inside scores. */
+static inline double dlogsum(double a, double b)
+{
+  const double mx = a > b ? a : b, mn = a < b ? a : b;
+  if (mn == -INFINITY) return mx;
+  return mx + log2(1.0 + exp2(mn - mx));
+}
+static inline double dsc(float x) { return NOT_IMP(x) ? (double) x : -INFINITY; }
+#define CORE_NAME core_dinside
+#define SCT double
+#define IMPV (-INFINITY)
+#define COMB(a, b) dlogsum((a), (b))
+#define ROOTFIRST(x) (x)
+#define SCOREF(x) ((float) (x))
+#define ENVF(x) (x)
+#define TSC(v, o) dsc(m->tsc[(v) * MAXC + (o)])
+#define ESC(v) (m->oesc + (size_t) (v) * Kp * Kp)
+#define ESCT float
+#define EV(x) dsc(x)
+#define BEGINSC(y) dsc(m->beginsc[y])
+#define HAS_BEGIN(y) NOT_IMP(m->beginsc[y])
+#define ENDSC(v) dsc(m->endsc[v])
+#define INIT_SC(v, d) (NOT_IMP(m->endsc[v]) ? (double) m->el_selfsc * (d) + (double) m->endsc[v] : -INFINITY)
 #include "cm_scan_oracle_core.h"
 
 /* One scan of dsq[i0..j0].  algo: ORC_CYK (FastCYKScan), ORC_IINS
@@ -338,6 +374,7 @@ int oracle_scan(const cmgb_model_desc *m, int algo, int qdbidx,
 
   if (algo == ORC_IINS) core_iinside(&c);
   else if (algo == ORC_FINS) core_finside(&c);
+  else if (algo == ORC_DINS) core_dinside(&c);
   else core_cyk(&c);
 
   c.vsc[0] = c.vsc_root;

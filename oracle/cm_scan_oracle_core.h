@@ -1,7 +1,8 @@
 /* cm_scan_oracle_core.h -- typed DP core of the scan oracle (TEST
  * INFRASTRUCTURE ONLY; included three times by cm_scan_oracle.c with the
  * macros CORE_NAME, SCT, IMPV, COMB, ROOTFIRST, SCOREF, ENVF, TSC, ESC,
- * BEGINSC, HAS_BEGIN, ENDSC, INIT_SC).
+ * ESCT (emission table element type), EV (emission value as SCT), BEGINSC,
+ * HAS_BEGIN, ENDSC, INIT_SC).
  *
  * Restates the j / v / d loops of FastCYKScan (src/cm_dpsearch.c:215-634),
  * FastIInsideScan (:1232-1647) and FastFInsideScan (:1851-2270): rolling
@@ -54,7 +55,7 @@ static void CORE_NAME(scanctx *c)
       const int dnv = dn[v], dxv = MINF(jr, dxW[v]);
       const int jpy = st_right(t) ? prv : cur;
       const int isbegl = (m->stid[v] == CMGB_BEGL_S);
-      const SCT *esc = (t == CMGB_B_st || t == CMGB_S_st || t == CMGB_D_st) ? NULL : ESC(v);
+      const ESCT *esc = (t == CMGB_B_st || t == CMGB_S_st || t == CMGB_D_st) ? NULL : ESC(v);
       SCT tv[MAXC];
       for (int o = 0; o < cnum && o < MAXC; o++) tv[o] = TSC(v, o);
       SCT *out = isbegl ? &BG(jrow, beglidx[v], 0) : &A(cur, v, 0);
@@ -104,9 +105,9 @@ static void CORE_NAME(scanctx *c)
                    sc = COMB(sc, ch[2][dp] + tv[2]); sc = COMB(sc, ch[1][dp] + tv[1]); sc = COMB(sc, ch[0][dp] + tv[0]); break;
           }
           const int64_t i = j - d + 1;
-          if (em == 3) sc += esc[dsq[i] * Kp + dsq[j]];
-          else if (em == 1) sc += esc[dsq[i]];
-          else if (em == 2) sc += esc[dsq[j]];
+          if (em == 3) sc += EV(esc[dsq[i] * Kp + dsq[j]]);
+          else if (em == 1) sc += EV(esc[dsq[i]]);
+          else if (em == 2) sc += EV(esc[dsq[j]]);
           out[d] = sc;   /* IL reads this cell as its own child at d+1 */
           float sf = SCOREF(sc); vbest = MAXF(vbest, sf);
         }
@@ -155,6 +156,8 @@ static void CORE_NAME(scanctx *c)
 #undef ENVF
 #undef TSC
 #undef ESC
+#undef ESCT
+#undef EV
 #undef BEGINSC
 #undef HAS_BEGIN
 #undef ENDSC
