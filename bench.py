@@ -216,6 +216,9 @@ def run_ours(args, rank, world):
     tuned = {"cyk_qdb1": sc.autotune(m, 1, "cyk"), "inside_qdb2": sc.autotune(m, 2, "inside")}
     xfer = [0, 0]
 
+    opr = {1: dp_ops_per_residue(m, 1), 2: dp_ops_per_residue(m, 2)}
+    ops_acc = [0]
+
     def step(strands, dev_ptrs):
         """One pass; returns (hits, cells, kernel_ms, launches)."""
         cells = 0
@@ -230,12 +233,14 @@ def run_ours(args, rank, world):
             kms += r.kernel_ms; launches += sc.last_launches()
             hb, db = sc.last_transfer_bytes(); xfer[0] += hb; xfer[1] += db
             cells += lib.cmgb_count_cells(ctypes.byref(desc), 1, Lres)
+            ops_acc[0] += opr[1] * Lres
             for a, b in windows_from_hits(r.hits, m.W, Lres):
                 r2 = sc.scan(m, dsq, a, b, algo="inside", qdbidx=2, cutoff=INS_CUT, env_cutoff=INS_CUT,
                              device_ptr=ptr)
                 kms += r2.kernel_ms; launches += sc.last_launches()
                 hb, db = sc.last_transfer_bytes(); xfer[0] += hb; xfer[1] += db
                 cells += lib.cmgb_count_cells(ctypes.byref(desc), 2, b - a + 1)
+                ops_acc[0] += opr[2] * (b - a + 1)
                 nh += len(r2.hits)
         return nh, cells, kms, launches
 
@@ -253,6 +258,7 @@ def run_ours(args, rank, world):
         for s in range(args.warmup):
             step(inputs[s], [t.data_ptr() for t in dev_inputs[s]] if use_dev else None)
         tot, cells, kms, launches, nh = 0.0, 0, 0.0, 0, 0
+        ops_acc[0] = 0
         for s in range(args.warmup, nsteps):
             flush.fill_(float(s))                  # evict L2 between timed steps
             barrier()
@@ -266,6 +272,7 @@ def run_ours(args, rank, world):
 
     clk = start_clock_sampler(rank)
     t_dev, cells, kms, launches, nh = timed(True)
+    ops = ops_acc[0]
     clocks = stop_clock_sampler(clk)
     t_e2e, _, _, _, _ = timed(False)
     h2d_step, d2h_step = xfer[0], xfer[1]     # transfers of the last host-buffer step
@@ -298,10 +305,56 @@ def run_ours(args, rank, world):
         "clocks": clocks,
     }
     out["roofline"] = roofline_block(cells, kms, Lres, args)
+    out["alu_roofline"] = alu_roofline(ops, kms, clocks)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(m, inputs[args.warmup][0], threads=1, seconds=args.cpu_seconds)
     sc.close()
     return out
+
+
+def dp_ops_per_residue(m, qdbidx):
+    """Algorithmic DP operations per residue once j >= W: per non-B cell,
+    cnum adds + (cnum + 1) max/log-sum combines + 1 emission add if the state
+    emits; per B cell, one add and one combine per k term (k limits of
+    src/cm_dpsearch.c:258-269)."""
+    from infernal_gb300 import cmfile
+    dmin, dmax = m.bands(qdbidx)
+    ops = 0
+    for v in range(m.M):
+        t = int(m.sttype[v])
+        if t == cmfile.E_st:
+            continue
+        lo = 2 if t == cmfile.MP_st else 1
+        if dmin is not None:
+            lo = max(int(dmin[v]), lo)
+        dn, dx = min(lo, m.W), (min(int(dmax[v]), m.W) if dmax is not None else m.W)
+        if dx < dn:
+            continue
+        if t == cmfile.B_st:
+            w, y = int(m.cfirst[v]), int(m.cnum[v])
+            for d in range(dn, dx + 1):
+                if dmin is not None:
+                    kmin = max(0, max(min(int(dmin[y]), m.W), d - min(int(dmax[w]), m.W)))
+                    kmax = min(min(int(dmax[y]), m.W), d - min(int(dmin[w]), m.W))
+                else:
+                    kmin, kmax = 0, d
+                ops += 2 * max(0, kmax - kmin + 1)
+        else:
+            c = int(m.cnum[v])
+            emits = t in (cmfile.MP_st, cmfile.ML_st, cmfile.MR_st, cmfile.IL_st, cmfile.IR_st)
+            ops += (dx - dn + 1) * (c + (c + 1) + (1 if emits else 0))
+    return ops
+
+
+def alu_roofline(ops, kms, clocks):
+    """The DP's own roof: FP32/INT32 non-tensor issue (one operation per lane
+    per clock; 152 SMs x 128 lanes)."""
+    mhz = (clocks or {}).get("sm_max_mhz") or 2070.0
+    peak = 152 * 128 * mhz * 1e6 / 1e12
+    ach = ops / (kms / 1e3) / 1e12 if kms > 0 else 0.0
+    return {"bound": "fp32/int32 non-tensor issue", "achieved": round(ach, 4), "peak": round(peak, 2),
+            "unit": "Tops/s", "frac": round(ach / peak, 5),
+            "note": "algorithmic DP operations (adds + max/log-sum combines) per kernel second"}
 
 
 def roofline_block(cells, kms, Lres, args):

@@ -547,6 +547,135 @@ def load(path: str, which: int = 0, local: bool = True) -> CMModel:
     return truncation_tables(configure(read_cm(path, which), local=local))
 
 
+# ---- query-dependent bands ---------------------------------------------------
+def _dsum_kahan(v) -> float:
+    """Easel esl_vec_DSum: compensated double sum."""
+    s, c = 0.0, 0.0
+    for x in v:
+        y = float(x) - c
+        t = s + y
+        c = (t - s) - y
+        s = t
+    return s
+
+
+def qdb_bands(m: CMModel, beta1: float = 1e-7, beta2: float = 1e-15, beta_W: float = 1e-7):
+    """Query-dependent bands and W: CalculateQueryDependentBands /
+    BandCalculationEngine (src/cm_qdband.c:45-451).
+
+    gamma[v][n] is the probability that the subtree rooted at v emits n
+    residues, computed from the leaves up in double precision over the
+    transitions before local configuration, with local begins (from pbegin)
+    into the root and local ends off.  dmin/dmax cut <= beta of probability
+    mass off each tail (beta1 -> dmin1/dmax1, beta2 -> dmin2/dmax2); W is the
+    root's right bound at beta_W.  The maximum length Z starts at 4 clen and
+    doubles until the truncated tail is negligible.  Every sum runs in the
+    reference's order, so the integer bounds agree exactly.
+    Returns (dmin1, dmax1, dmin2, dmax2, W) as int32 arrays and an int."""
+    if beta2 - beta1 > 1e-20:
+        raise ValueError("qdb_bands: beta1 must be >= beta2")
+    max_beta = max(beta_W, beta1, beta2)
+    M = m.M
+    t = m.t_global.astype(np.float64)          # float probabilities, used as doubles
+    internal = (MATP_nd, MATL_nd, MATR_nd, BIF_nd)
+    nstarts = sum(1 for nd in range(2, m.nodes) if m.ndtype[nd] in internal)
+    begin = np.zeros(M, np.float32)
+    begin[m.nodemap[1]] = f32(1.0 - float(m.pbegin))
+    pb = f32(f32(m.pbegin) / f32(nstarts))
+    for nd in range(2, m.nodes):
+        if m.ndtype[nd] in internal:
+            begin[m.nodemap[nd]] = pb
+    Z = m.clen * 4
+    while True:
+        res = _band_engine(m, Z, t, begin, beta1, beta2, beta_W, max_beta)
+        if res is not None:
+            return res
+        Z *= 2
+        if Z > m.clen * 1000:
+            raise ValueError("qdb_bands: Z got insanely large (> 1000*clen)")
+
+
+def _band_engine(m, Z, t, begin, beta1, beta2, beta_W, max_beta):
+    """One pass of BandCalculationEngine at maximum length Z; None when the
+    truncation error is not negligible (the caller doubles Z)."""
+    M = m.M
+    eps = np.finfo(np.float64).eps
+    gamma = [None] * M
+    g0 = np.zeros(Z + 1)
+    gE = np.zeros(Z + 1)
+    gE[0] = 1.0
+    dmin1, dmax1 = np.zeros(M, np.int32), np.zeros(M, np.int32)
+    dmin2, dmax2 = np.zeros(M, np.int32), np.zeros(M, np.int32)
+    W = 0
+    for v in range(M - 1, -1, -1):
+        st = int(m.sttype[v])
+        if st == E_st:
+            gamma[v] = gE
+            continue
+        if v == 0:
+            g = g0
+        else:
+            g = np.zeros(Z + 1)
+            if st == B_st:
+                gw, gy = gamma[int(m.cfirst[v])], gamma[int(m.cnum[v])]
+                for leftn in range(Z + 1):          # per n, terms added in leftn order
+                    g[leftn:] += gw[leftn] * gy[: Z + 1 - leftn]
+            else:
+                dv = 2 if st == MP_st else (1 if st in (ML_st, MR_st, IL_st, IR_st) else 0)
+                ys = [int(m.cfirst[v]) + yo for yo in range(int(m.cnum[v]))]
+                if v in ys:
+                    # an insert's self-loop reads its own density at n - dv:
+                    # sequential in n, children summed in yoffset order
+                    tv = [float(t[v, yo]) for yo in range(len(ys))]
+                    cols = [None if y == v else gamma[y].tolist() for y in ys]
+                    gl = [0.0] * (Z + 1)
+                    for n in range(dv, Z + 1):
+                        acc = 0.0
+                        for yo, y in enumerate(ys):
+                            acc += tv[yo] * (gl[n - dv] if y == v else cols[yo][n - dv])
+                        gl[n] = acc
+                    g[:] = gl
+                else:
+                    for yo, y in enumerate(ys):
+                        g[dv:] += float(t[v, yo]) * gamma[y][: Z + 1 - dv]
+            gamma[v] = g
+        pdf = float(np.cumsum(g)[-1]) if v != 0 else 0.0
+        if begin[v] > 0.0:
+            g0 += float(begin[v]) * g
+        if v == 0:
+            pdf = _dsum_kahan(g0)
+        if pdf <= 0.999 or g[Z] > max_beta * eps:
+            return None
+        if pdf > 1.0:
+            s = _dsum_kahan(g)
+            g /= s
+        c = np.cumsum(g)
+        k2 = int(np.argmax(c > beta2))
+        k1 = k2 + int(np.argmax(c[k2:] > beta1))
+        dmin2[v], dmin1[v] = k2, k1
+        r = np.cumsum(g[::-1])
+        k2 = int(np.argmax(r > beta2))
+        k1 = k2 + int(np.argmax(r[k2:] > beta1))
+        dmax2[v], dmax1[v] = Z - k2, Z - k1
+        if v == 0:
+            W = Z - int(np.argmax(r > beta_W))
+    for b in (W, int(dmax1[0]), int(dmax2[0])):
+        if not _band_truncation_negligible(g0, b, Z):
+            return None
+    return dmin1, dmax1, dmin2, dmax2, W
+
+
+def _band_truncation_negligible(density, b, Z) -> bool:
+    """BandTruncationNegligible (src/cm_qdband.c:520-545)."""
+    C = 0.0
+    for i in range(b + 1, Z + 1):
+        C += float(density[i])
+    logbeta = (math.log(density[Z]) - math.log(density[b + 1])) / (Z - b - 1)
+    beta = math.exp(logbeta)
+    D = (beta / (1.0 - beta)) * float(density[Z])
+    return D < C * np.finfo(np.float64).eps
+
+
 # ---- truncated-scan tables ----------------------------------------------------
 def emit_map(m: CMModel):
     """Consensus coordinates of every node: CreateEmitMap (src/display.c:1110).

@@ -490,6 +490,66 @@ CMGB_DEV void qdb_scan_body(const KParams &p, float *smf, int tid, int nt, int b
           if (!begl) for (int x = tid; x < hi - lo + 1; x += nt) sm[buf + x] = cin[carry + x];
 #pragma unroll
           for (int o = 0; o < CMGB_MAXC; o++) cb[o] -= sd;
+          if (kind == SK_GEN) {
+            // Two cells per iteration: their child loads and folds are
+            // independent, so each warp keeps two dependency chains in flight.
+            // Both are evaluated at a length clamped into the band (child reads
+            // stay inside the children's buffers); pad cells then take their
+            // constant value.
+            auto gval = [&](int r, int d) -> T {
+              const int crow = r - rdo;
+              T sc;
+              switch (cnum) {
+#define CH(o) R::add(sm[cb[o] + crow * cs[o] + d], tv[o])
+              case 2: sc = R::comb(CH(1), INIT(d - sd), tbl); sc = R::comb(sc, CH(0), tbl); break;
+              case 3: sc = R::comb(CH(2), CH(1), tbl); sc = R::comb(sc, INIT(d - sd), tbl); sc = R::comb(sc, CH(0), tbl); break;
+              case 4: sc = R::comb(CH(3), CH(2), tbl); sc = R::comb(sc, INIT(d - sd), tbl); sc = R::comb(sc, CH(1), tbl);
+                      sc = R::comb(sc, CH(0), tbl); break;
+              case 5: sc = R::comb(CH(4), CH(3), tbl); sc = R::comb(sc, INIT(d - sd), tbl); sc = R::comb(sc, CH(1), tbl);
+                      sc = R::comb(sc, CH(2), tbl); sc = R::comb(sc, CH(0), tbl); break;
+              default: sc = R::comb(CH(5), INIT(d - sd), tbl); sc = R::comb(sc, CH(4), tbl); sc = R::comb(sc, CH(3), tbl);
+                       sc = R::comb(sc, CH(2), tbl); sc = R::comb(sc, CH(1), tbl); sc = R::comb(sc, CH(0), tbl); break;
+#undef CH
+              }
+              if (emit == 3)      sc = R::add(sc, esc[res[W + r - d] * P.Kp + res[W + r - 1]]);
+              else if (emit == 1) sc = R::add(sc, esc[res[W + r - d]]);
+              else if (emit == 2) sc = R::add(sc, esc[res[W + r - 1]]);
+              return sc;
+            };
+            auto finish = [&](int r, int d, T val, bool in) {
+              const int jp = jp0 + r;
+              if (in) {
+                if (want_vsc && jp >= own_jp) { const float f = R::score(val); vbest = vbest > f ? vbest : f; }
+                if (has_begin && d >= rdn && d <= (jp < rdxW ? jp : rdxW)) {
+                  const T cc = R::add(val, beg);
+                  const int ai = (r - 1) * accw + d - rdn;
+                  if (cc >= acc[ai]) { acc[ai] = cc; bestr[ai] = v; }
+                }
+              }
+              sm[buf + r * stride + d - lo] = val;
+              if (r == TT) cout[carry + d - lo] = val;
+            };
+            const bool band_ok = dn <= dxW;   // uniform: an empty band has only pad cells
+            CellWalk c(tid, lo, hi, wpa, sra, sdda, inva);
+            while (c.r <= nrows) {
+              CellWalk c2 = c; c2.next();
+              const bool two = c2.r <= nrows;
+              const int r1 = c.r, d1 = c.d, r2 = two ? c2.r : c.r, d2 = two ? c2.d : c.d;
+              const int dx1 = jp0 + r1 < dxW ? jp0 + r1 : dxW, dx2 = jp0 + r2 < dxW ? jp0 + r2 : dxW;
+              const bool in1 = d1 >= dn && d1 <= dx1, in2 = d2 >= dn && d2 <= dx2;
+              T v1 = d1 == 0 ? i0v : imp, v2 = d2 == 0 ? i0v : imp;
+              if (band_ok) {
+                const int e1 = d1 < dn ? dn : (d1 > dxW ? dxW : d1), e2 = d2 < dn ? dn : (d2 > dxW ? dxW : d2);
+                const T g1 = gval(r1, e1), g2 = gval(r2, e2);
+                if (in1) v1 = g1;
+                if (in2) v2 = g2;
+              }
+              finish(r1, d1, v1, in1);
+              if (two) finish(r2, d2, v2, in2);
+              c = c2;
+              if (two) c.next();
+            }
+          } else
           for (CellWalk c(tid, lo, hi, wpa, sra, sdda, inva); c.r <= nrows; c.next()) {
             const int r = c.r, d = c.d, jp = jp0 + r;
             const int dx = jp < dxW ? jp : dxW;

@@ -131,11 +131,13 @@ CMGB_DEV void tr_scan_body(const TrKParams &p, float *smf, int tid, int nt, int 
       if (si.carry >= 0)
         for (int x = tid; x < 3 * width; x += nt) {
           const int m = x / width, d = si.lo + x - m * width;
+          if ((m == 1 && !fL) || (m == 2 && !fR)) continue;   // planes the pass does not fill are never read
           carry0[si.carry + m * si.stride + d - si.lo] = (m == 0 && d == 0) ? i0v : imp;
         }
       if (si.kind == SK_BEGL)
         for (int x = tid; x < 3 * width; x += nt) {
           const int m = x / width, d = si.lo + x - m * width;
+          if ((m == 1 && !fL) || (m == 2 && !fR)) continue;
           ringb[si.ring + m * RR * si.stride + d - si.lo] = (m == 0 && d == 0) ? i0v : imp;
         }
     }
@@ -245,6 +247,7 @@ CMGB_DEV void tr_scan_body(const TrKParams &p, float *smf, int tid, int nt, int 
         } else if (kind == SK_IL || kind == SK_IR) {
           for (int x = tid; x < 3 * (hi - lo + 1); x += nt) {
             const int m = x / (hi - lo + 1), xx = x - m * (hi - lo + 1);
+            if ((m == 1 && !fL) || (m == 2 && !fR)) continue;
             sm[buf + m * mst + xx] = cin[carry + m * stride + xx];
           }
           const bool il = kind == SK_IL;
@@ -361,6 +364,7 @@ CMGB_DEV void tr_scan_body(const TrKParams &p, float *smf, int tid, int nt, int 
           if (!begl)
             for (int x = tid; x < 3 * (hi - lo + 1); x += nt) {
               const int m = x / (hi - lo + 1), xx = x - m * (hi - lo + 1);
+              if ((m == 1 && !fL) || (m == 2 && !fR)) continue;
               sm[buf + m * mst + xx] = cin[carry + m * stride + xx];
             }
           for (CellWalk c(tid, lo, hi, wpa, sra, sdda, inva); c.r <= nrows; c.next()) {

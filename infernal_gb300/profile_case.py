@@ -1,11 +1,15 @@
 """One scan of a stored model on a seeded synthetic target, for profiling.
 
-    python -m infernal_gb300.profile_case <model> <length> <cyk|inside> [tile_rows arena]
+    python -m infernal_gb300.profile_case <model> <length> <cyk|inside|finside> [tile_rows arena]
+    python -m infernal_gb300.profile_case <model> <nreads> <trcyk|trinside> [tile_rows arena]
 
 <model> is a configured model under tests/golden (tRNA, Vault, Plant_SRP).
-Runs the scan twice (the first builds the plan) and prints the kernel time.
-With tile_rows/arena the launch shape is fixed (arena 1 shared, 2 global);
-without them the autotuner picks it first.
+The standard scanners scan one target of <length> residues; the truncated
+scanners scan a batch of <nreads> reads of 100-400 nt (cmgb_ScanBatch, pass 4:
+5' and 3' truncation).  Runs the scan twice (the first builds the plan) and
+prints the kernel time.  With tile_rows/arena the launch shape is fixed
+(arena 1 shared, 2 global); without them the standard scanners let the
+autotuner pick it and the truncated scanners use the default shape.
 """
 from __future__ import annotations
 
@@ -24,19 +28,29 @@ def main(argv):
     name = argv[1] if len(argv) > 1 else "Plant_SRP"
     L = int(argv[2]) if len(argv) > 2 else 30000
     algo = argv[3] if len(argv) > 3 else "cyk"
-    q = 1 if algo == "cyk" else 2
+    q = 1 if algo in ("cyk", "trcyk") else 2
     m = cmfile.load_npz(os.path.join(ROOT, "tests", "golden", f"{name}.model.npz"))
-    dsq, _ = emit.make_target(np.random.default_rng(1), L, 0.40, [])
+    rng = np.random.default_rng(1)
     sc = lib.Scanner(0)
+    shape = None
     if len(argv) > 5:
         sc.set_shape(int(argv[4]), 0, 0, 0, int(argv[5]))
         shape = (int(argv[4]), int(argv[5]))
+    if algo.startswith("tr"):
+        reads = [cmfile.digitize("".join(rng.choice(list("ACGU"), int(rng.integers(100, 401))))) for _ in range(L)]
+        for _ in range(2):
+            t = time.time()
+            rs = sc.scan_batch(m, reads, algo=algo, qdbidx=q, pass_idx=4, cutoff=10.0)
+            print(f"{name} reads={L} {algo} shape={shape} kernel_ms={rs[0].kernel_ms:.2f} wall_s={time.time() - t:.2f} "
+                  f"hits={sum(len(r.hits) for r in rs)}")
     else:
-        shape = sc.autotune(m, q, algo)
-    for _ in range(2):
-        t = time.time()
-        r = sc.scan(m, dsq, 1, L, algo=algo, qdbidx=q, cutoff=10.0)
-        print(f"{name} L={L} {algo} shape={shape} kernel_ms={r.kernel_ms:.2f} wall_s={time.time() - t:.2f} hits={len(r.hits)}")
+        dsq, _ = emit.make_target(rng, L, 0.40, [])
+        if shape is None:
+            shape = sc.autotune(m, q, algo)
+        for _ in range(2):
+            t = time.time()
+            r = sc.scan(m, dsq, 1, L, algo=algo, qdbidx=q, cutoff=10.0)
+            print(f"{name} L={L} {algo} shape={shape} kernel_ms={r.kernel_ms:.2f} wall_s={time.time() - t:.2f} hits={len(r.hits)}")
     sc.close()
 
 

@@ -69,6 +69,10 @@ def _load(path):
         if hasattr(lib, "refh_tr_penalties"):
             lib.refh_tr_penalties.argtypes = [I, I, I] + [P] * 10 + [F] + [P] * 7
             lib.refh_tr_penalties.restype = I
+        if hasattr(lib, "refh_qdb_bands"):
+            lib.refh_qdb_bands.argtypes = [I, I, I] + [P] * 8 + [F, ctypes.c_double, ctypes.c_double,
+                                                                 ctypes.c_double] + [P] * 6
+            lib.refh_qdb_bands.restype = I
         if hasattr(lib, "refh_scan"):
             lib.refh_scan.argtypes = [P, I, I, I, P, I64, I64, F, I, F, I, I, P, I64, P, P, P, P, P, P, P]
             lib.refh_scan.restype = I
@@ -163,3 +167,25 @@ def ref_tr_penalties(m):
     if st != 0:
         raise RuntimeError(f"refh_tr_penalties status {st}: {err.value.decode()}")
     return lp, rp, g.reshape(3, M), l.reshape(3, M), ig.reshape(3, M), il.reshape(3, M)
+
+
+def ref_qdb_bands(m, beta1=1e-7, beta2=1e-15, beta_W=1e-7):
+    """Bands and W by the reference's own CalculateQueryDependentBands
+    (oracle/_ref); returns (dmin1, dmax1, dmin2, dmax2, W)."""
+    lib = _load(REF_SO)
+    keep = []
+
+    def c(a, dt):
+        x = np.ascontiguousarray(a, dt)
+        keep.append(x)
+        return x.ctypes.data
+    out = [np.zeros(m.M, np.int32) for _ in range(4)]
+    W = I()
+    err = ctypes.create_string_buffer(256)
+    st = lib.refh_qdb_bands(m.M, m.nodes, m.clen, c(m.sttype, np.int8), c(m.stid, np.int8), c(m.cfirst, np.int32),
+                            c(m.cnum, np.int32), c(m.pnum, np.int32), c(m.ndtype, np.int8), c(m.nodemap, np.int32),
+                            c(m.t_global, np.float32), float(m.pbegin), beta1, beta2, beta_W,
+                            *[o.ctypes.data for o in out], ctypes.byref(W), err)
+    if st != 0:
+        raise RuntimeError(f"refh_qdb_bands status {st}: {err.value.decode()}")
+    return out[0], out[1], out[2], out[3], W.value

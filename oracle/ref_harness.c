@@ -145,13 +145,32 @@ int cm_TrFillFromMode(char mode, int *fl, int *fr, int *ft)
   return eslOK;
 }
 
-/* Easel's integer push-down stack (esl_stack.c), used by CreateEmitMap. */
-struct esl_stack_s { int *idata; int n, nalloc; };
+/* Easel's push-down stacks (esl_stack.c): integers for CreateEmitMap,
+ * pointers for BandCalculationEngine's reusable beams. */
+struct esl_stack_s { int *idata; void **pdata; int n, nalloc; };
 ESL_STACK *esl_stack_ICreate(void)
 {
   ESL_STACK *s = calloc(1, sizeof(ESL_STACK));
   s->nalloc = 128; s->idata = malloc(sizeof(int) * s->nalloc);
   return s;
+}
+ESL_STACK *esl_stack_PCreate(void)
+{
+  ESL_STACK *s = calloc(1, sizeof(ESL_STACK));
+  s->nalloc = 128; s->pdata = malloc(sizeof(void *) * s->nalloc);
+  return s;
+}
+int esl_stack_PPush(ESL_STACK *s, void *p)
+{
+  if (s->n == s->nalloc) { s->nalloc *= 2; s->pdata = realloc(s->pdata, sizeof(void *) * s->nalloc); }
+  s->pdata[s->n++] = p;
+  return eslOK;
+}
+int esl_stack_PPop(ESL_STACK *s, void **ret_p)
+{
+  if (s->n == 0) { *ret_p = NULL; return eslEOD; }
+  *ret_p = s->pdata[--s->n];
+  return eslOK;
 }
 int esl_stack_IPush(ESL_STACK *s, int x)
 {
@@ -165,7 +184,7 @@ int esl_stack_IPop(ESL_STACK *s, int *ret_x)
   *ret_x = s->idata[--s->n];
   return eslOK;
 }
-void esl_stack_Destroy(ESL_STACK *s) { if (s) { free(s->idata); free(s); } }
+void esl_stack_Destroy(ESL_STACK *s) { if (s) { free(s->idata); free(s->pdata); free(s); } }
 
 /* src/cm.c:4897 */
 void InsertsGivenNodeIndex(CM_t *cm, int nd, int *ret_i1, int *ret_i2)
@@ -410,4 +429,39 @@ int refh_tr_penalties(int M, int nodes, int clen, const int8_t *sttype, const in
       ig_out[p * M + v] = trp->ig_ptyAA[p][v]; il_out[p * M + v] = trp->il_ptyAA[p][v];
     }
   return eslOK;
+}
+
+/* Query-dependent bands and W computed by the reference's own
+ * CalculateQueryDependentBands / BandCalculationEngine (src/cm_qdband.c:45,
+ * 163) on the renormalised global transition probabilities t[M*6], with
+ * local begin probabilities from pbegin (cm_CalculateLocalBeginProbs,
+ * compiled from src/cm_modelconfig.c).  Outputs dmin1/dmax1/dmin2/dmax2[M]
+ * and *ret_W. */
+int refh_qdb_bands(int M, int nodes, int clen, const int8_t *sttype, const int8_t *stid, const int *cfirst,
+                   const int *cnum, const int *pnum, const int8_t *ndtype, const int *nodemap, const float *t,
+                   float pbegin, double beta1, double beta2, double beta_W,
+                   int *dmin1, int *dmax1, int *dmin2, int *dmax2, int *ret_W, char *errbuf)
+{
+  CM_t *cm = calloc(1, sizeof(CM_t));
+  cm->M = M; cm->nodes = nodes; cm->clen = clen; cm->pbegin = pbegin;
+  cm->sttype = malloc(M + 1); cm->stid = malloc(M + 1);
+  cm->cfirst = malloc(sizeof(int) * M); cm->cnum = malloc(sizeof(int) * M); cm->pnum = malloc(sizeof(int) * M);
+  cm->ndtype = malloc(nodes + 1); cm->nodemap = malloc(sizeof(int) * nodes);
+  cm->t = malloc(sizeof(float *) * M);
+  cm->t[0] = malloc(sizeof(float) * M * MAXCONNECT);
+  cm->begin = calloc(M, sizeof(float));
+  for (int v = 0; v < M; v++) {
+    cm->sttype[v] = sttype[v]; cm->stid[v] = stid[v];
+    cm->cfirst[v] = cfirst[v]; cm->cnum[v] = cnum[v]; cm->pnum[v] = pnum[v];
+    cm->t[v] = cm->t[0] + (size_t) v * MAXCONNECT;
+    for (int x = 0; x < MAXCONNECT; x++) cm->t[v][x] = t[(size_t) v * MAXCONNECT + x];
+  }
+  cm->sttype[M] = cm->stid[M] = -1;
+  for (int nd = 0; nd < nodes; nd++) { cm->ndtype[nd] = ndtype[nd]; cm->nodemap[nd] = nodemap[nd]; }
+  cm->ndtype[nodes] = -1;
+  CM_QDBINFO *q = calloc(1, sizeof(CM_QDBINFO));
+  q->M = M; q->beta1 = beta1; q->beta2 = beta2;
+  q->dmin1 = dmin1; q->dmax1 = dmax1; q->dmin2 = dmin2; q->dmax2 = dmax2;
+  int status = CalculateQueryDependentBands(cm, errbuf, q, beta_W, ret_W, NULL, NULL, NULL);
+  return status;
 }

@@ -18,7 +18,6 @@ OFFPATH(cm_alidisplay_Print) OFFPATH(cm_alidisplay_TruncString) OFFPATH(cm_pli_T
 OFFPATH(cm_pli_TargetReportable) OFFPATH(esl_DCompare_old) OFFPATH(esl_getcwd) OFFPATH(esl_keyhash_Get)
 OFFPATH(esl_keyhash_GetNumber) OFFPATH(esl_msa_Destroy) OFFPATH(esl_opt_SpoofCmdline)
 OFFPATH(esl_randomness_CreateTimeseeded) OFFPATH(esl_randomness_Destroy) OFFPATH(esl_sq_Destroy)
-OFFPATH(esl_stack_PCreate) OFFPATH(esl_stack_PPop) OFFPATH(esl_stack_PPush)
 OFFPATH(AllocCP9Bands) OFFPATH(CMLogoddsify) OFFPATH(CP9Logoddsify) OFFPATH(CreateCP9Matrix)
 OFFPATH(DegeneratePairScore) OFFPATH(SubCMLogoddsify) OFFPATH(build_cp9_hmm) OFFPATH(cm_Validate)
 OFFPATH(cm_cp9_to_p7) OFFPATH(cm_nonconfigured_Verify) OFFPATH(cp9_Clone) OFFPATH(esl_abc_FAvgScore)
