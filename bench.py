@@ -193,6 +193,123 @@ def run_trunc(args, rank, world):
     return out
 
 
+def _overlap(a, b):
+    return max(0, min(a[1], b[1]) - max(a[0], b[0]) + 1)
+
+
+def run_learned(args, rank, world):
+    """Learned pre-filter + batched CYK -> Inside on the kept regions, against
+    the plain scan of everything on the same targets (the hit-loss judge)."""
+    import torch
+    from infernal_gb300 import cmfile, lib as L, prefilter
+    m = cmfile.load_npz(os.path.join(ROOT, "tests", "golden", "Plant_SRP.model.npz"))
+    wts = prefilter.load(os.path.join(ROOT, "infernal_gb300", "filters", "Plant_SRP.filter.npz"))
+    torch.cuda.set_device(0)
+    sc = L.Scanner(0)
+    filt = prefilter.Prefilter(sc, wts, m.W)
+    nsteps = args.warmup + args.steps
+    inputs = [make_step_input(m, 500000 + s, args.mb) for s in range(nsteps)]
+    Lres = len(inputs[0][0]) - 2
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    sc.autotune(m, 1, "cyk"); sc.autotune(m, 2, "inside")
+
+    def regions_scan(dsq, regs, algo, qdb, cut):
+        """Batched scan of sub-ranges [a, b] of one strand; hits in strand coordinates."""
+        if not regs:
+            return [], 0.0
+        buf = np.ascontiguousarray(dsq, np.uint8)
+        offs = np.array([a - 1 for a, b in regs], np.int64)
+        lens = np.array([b - a + 1 for a, b in regs], np.int64)
+        import ctypes
+        nh = np.zeros(len(regs), np.int64)
+        hl = sc.lib.cmgb_hitlist_create()
+        err = ctypes.create_string_buffer(256)
+        st = sc.lib.cmgb_ScanBatch(sc._ctx, sc.model(m), err, L.BATCH_ALGOS[algo], qdb, 0, buf.ctypes.data, len(buf),
+                                   offs.ctypes.data, lens.ctypes.data, len(regs), cut, hl, 1, cut, nh.ctypes.data,
+                                   None, None, None, None)
+        if st != 0:
+            raise L.ScanError(st, err.value.decode())
+        hits, h, k = [], L.Hit(), 0
+        for q in range(len(regs)):
+            for _ in range(int(nh[q])):
+                sc.lib.cmgb_hitlist_get(hl, k, ctypes.byref(h)); k += 1
+                hits.append((h.start + int(offs[q]), h.stop + int(offs[q]), h.score))
+        sc.lib.cmgb_hitlist_destroy(hl)
+        return hits, float(sc.lib.cmgb_ctx_last_kernel_ms(sc._ctx))
+
+    def filtered_step(strands, dptrs):
+        out, ms, kept = [], 0.0, 0
+        for dsq, ptr in zip(strands, dptrs):
+            logit, fms = filt.logits(ptr, 1, Lres)
+            ms += fms
+            regs = filt.regions(logit, 1, Lres)
+            kept += sum(b - a + 1 for a, b in regs)
+            cyk, k1 = regions_scan(dsq, regs, "cyk", 1, CYK_CUT)
+            wins = windows_from_hits([(h[0], h[1]) for h in cyk], m.W, Lres)
+            ins, k2 = regions_scan(dsq, wins, "inside", 2, INS_CUT)
+            ms += k1 + k2
+            out.append(ins)
+        return out, ms, kept
+
+    def plain_step(strands, dptrs):
+        out = []
+        for dsq, ptr in zip(strands, dptrs):
+            r = sc.scan(m, dsq, 1, Lres, algo="cyk", qdbidx=1, cutoff=CYK_CUT, env_cutoff=CYK_CUT, device_ptr=ptr)
+            ins = []
+            for a, b in windows_from_hits(r.hits, m.W, Lres):
+                r2 = sc.scan(m, dsq, a, b, algo="inside", qdbidx=2, cutoff=INS_CUT, env_cutoff=INS_CUT, device_ptr=ptr)
+                ins += [(h[0], h[1], h[4]) for h in r2.hits]
+            out.append(ins)
+        return out
+
+    dev = [[torch.from_numpy(x).to("cuda") for x in inp] for inp in inputs]
+    torch.cuda.synchronize()
+    for s in range(args.warmup):
+        filtered_step(inputs[s], [t.data_ptr() for t in dev[s]])
+    clk = start_clock_sampler(rank)
+    tot, kms, kept, fhits = 0.0, 0.0, 0, []
+    for s in range(args.warmup, nsteps):
+        flush.fill_(float(s))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        h, k, kp = filtered_step(inputs[s], [t.data_ptr() for t in dev[s]])
+        torch.cuda.synchronize()
+        tot += time.perf_counter() - t0
+        kms += k; kept += kp; fhits.append(h)
+    clocks = stop_clock_sampler(clk)
+    # the judge: the plain scan of everything on the same steps (timed too)
+    t0 = time.perf_counter()
+    phits = [plain_step(inputs[s], [t.data_ptr() for t in dev[s]]) for s in range(args.warmup, nsteps)]
+    t_plain = time.perf_counter() - t0
+    nplain = nfound = 0
+    for ph, fh in zip(phits, fhits):
+        for sp, sf in zip(ph, fh):
+            for h in sp:
+                nplain += 1
+                if any(_overlap(h, g) >= 0.5 * (h[1] - h[0] + 1) for g in sf):
+                    nfound += 1
+    res = 2 * Lres * args.steps
+    value = res / tot / 1e6
+    out = {
+        "metric": "Mres/s scanned (both strands): learned pre-filter + batched QDB-CYK + Inside vs the plain GPU scan",
+        "value": round(value, 3), "unit": "Mres/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1000 * tot / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16 (filter) + f32 (CYK) + int32 (Inside)", "data": "synthetic",
+        "config": {"workload": f"Plant_SRP CM stand-in, {args.mb} Mb x 2 strands per step, GC 0.40; filter threshold "
+                               f"{filt.thr:.3f}; kept regions scanned by CYK QDB1 ({CYK_CUT} bits) -> Inside QDB2 ({INS_CUT} bits)",
+                   "l2": "flushed between timed steps (256 MB write)", "parallelism": "1 GPU"},
+        "plain_mres_s": round(res / t_plain / 1e6, 3),
+        "speedup_vs_plain": round(t_plain / tot, 2),
+        "fraction_scanned": round(kept / res, 4),
+        "hits_plain": nplain, "hits_found": nfound,
+        "hit_loss": round(1.0 - nfound / nplain, 4) if nplain else None,
+        "kernel_ms_per_step": round(kms / args.steps, 3),
+        "clocks": clocks,
+    }
+    filt.close(); sc.close()
+    return out
+
+
 # ----------------------------------------------------------------------------
 def run_ours(args, rank, world):
     import torch
@@ -507,8 +624,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="plain", choices=["plain", "trunc"],
-                    help="plain: the single-large-CM scan (default); trunc: the truncated-mode read batch")
+    ap.add_argument("--workload", default="plain", choices=["plain", "trunc", "learned"],
+                    help="plain: the single-large-CM scan (default); trunc: the truncated-mode read batch; "
+                         "learned: the pre-filtered pipeline against the plain scan")
     ap.add_argument("--reads", type=int, default=5000, help="reads per step of the trunc workload")
     args = ap.parse_args()
     world = _env_int("WORLD_SIZE", 1)
@@ -521,7 +639,12 @@ def main():
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl")
-    out = run_trunc(args, rank, world) if args.workload == "trunc" else run_ours(args, rank, world)
+    if args.workload == "trunc":
+        out = run_trunc(args, rank, world)
+    elif args.workload == "learned":
+        out = run_learned(args, rank, world)
+    else:
+        out = run_ours(args, rank, world)
     if rank == 0:
         print(json.dumps(out))
     if world > 1:

@@ -296,6 +296,26 @@ int cmgb_ScanBatch(cmgb_ctx *ctx, cmgb_model *model, char *errbuf, int algo, int
                    int nseq, float cutoff, cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
                    int64_t *ret_nhits, int64_t *ret_envi, int64_t *ret_envj, float *ret_sc, int *ret_mode);
 
+/* ---- learned window pre-filter ----
+ * No reference counterpart: a learned screen placed before the CYK stage.
+ * Windows of 2W residues at stride W over [i0, j0] (window k starts at
+ * i0 + kW, so every hit of length <= W lies inside the window where it
+ * starts in the first half) are scored by a dilated 1-D convolution network
+ * (one-hot ACGU; six convolutions of kernel 9, dilations 1..32, 4 -> 128 ->
+ * 128 channels, ReLU; max over positions; linear read-out), BF16 weights and
+ * activations, FP32 accumulation, on the tensor cores.  Weights: w0
+ * [9 taps][4][128] f32 (first layer), w [5][9][128 out][128 in] BF16 bit
+ * patterns (layers 2-6), bias [6][128] f32, wout [129] f32 (read-out
+ * weights then bias).  cmgb_filter_windows takes residues in device memory
+ * (indexed like dsq) and writes one logit per window to ret_logits (host,
+ * max_windows entries); *ret_ms receives the device time. */
+typedef struct cmgb_filter_s cmgb_filter;
+int  cmgb_filter_create(cmgb_ctx *ctx, int W, const float *w0, const uint16_t *w, const float *bias,
+                        const float *wout, cmgb_filter **ret_filter, char *errbuf);
+void cmgb_filter_destroy(cmgb_filter *filter);
+int  cmgb_filter_windows(cmgb_ctx *ctx, cmgb_filter *filter, const uint8_t *d_dsq, int64_t i0, int64_t j0,
+                         float *ret_logits, int64_t max_windows, int64_t *ret_nwin, float *ret_ms, char *errbuf);
+
 /* ---- allocation-free CYK scan ----
  * This entry point has no counterpart in the reference.  It exists for
  * callers that must not allocate device memory while they scan: code that

@@ -214,7 +214,7 @@ struct cmgb_ctx_s {
   float *d_carry = nullptr; size_t carry_bytes = 0;
   float *d_ring = nullptr; size_t ring_bytes = 0;
   unsigned char *d_dsq = nullptr; size_t dsq_bytes = 0;
-  Cand *d_cand = nullptr;
+  Cand *d_cand = nullptr; int cand_cap = 0;   // standard candidate buffer (grown by batched scans)
   Control *d_ctl = nullptr;
   unsigned *d_vsc = nullptr; int vsc_len = 0;
   int *d_ilog = nullptr;
@@ -258,6 +258,7 @@ extern "C" int cmgb_ctx_create(int device, cmgb_ctx **ret, char *errbuf)
   CUDA_TRY(cudaEventCreate(&c->ev0));
   CUDA_TRY(cudaEventCreate(&c->ev1));
   CUDA_TRY(cudaMalloc(&c->d_cand, sizeof(Cand) * (size_t) kCandCap));
+  c->cand_cap = kCandCap;
   CUDA_TRY(cudaMalloc(&c->d_ctl, sizeof(Control)));
   CUDA_TRY(cudaMallocHost(&c->h_ctl, sizeof(Control)));
   const int *ilog;
@@ -518,7 +519,7 @@ static int scan_std(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, int al
   kp.oesc = m->d_oesc; kp.ioesc = m->d_ioesc; kp.ilog = c->d_ilog; kp.flog = c->d_flog;
   kp.dsq = d_dsq; kp.i0 = i0; kp.j0 = j0; kp.win_len = win; kp.nwin = (int) nwin;
   kp.queue = &c->d_ctl->queue; kp.carry = c->d_carry; kp.ring = c->d_ring;
-  kp.cand = c->d_cand; kp.ncand = &c->d_ctl->ncand; kp.cand_cap = kCandCap;
+  kp.cand = c->d_cand; kp.ncand = &c->d_ctl->ncand; kp.cand_cap = c->cand_cap;
   const bool greedy = !(m->flags & CMGB_NOTGREEDY);
   kp.cand_cut = cutoff; kp.cand_pos = (hitlist && !greedy) ? 1 : 0;
   if (!hitlist) { kp.cand_cut = 3.0e38f; kp.cand_pos = 0; }
@@ -543,7 +544,7 @@ static int scan_std(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, int al
   CUDA_TRY(cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1));
   c->last_launches = 1;
   if (h->err & 2) ERRF(CMGB_ENODEV, "%s, a bounded device wait ran out (phase record copy)", fn);
-  if (h->err & 1) ERRF(CMGB_ERANGE, "%s, more than %d candidate hit cells; raise the cutoff", fn, kCandCap);
+  if (h->err & 1) ERRF(CMGB_ERANGE, "%s, more than %d candidate hit cells; raise the cutoff", fn, c->cand_cap);
 
   auto u2f = [](unsigned u) { if (u == 0) return CMGB_IMPOSSIBLE; unsigned b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u; float f; std::memcpy(&f, &b, 4); return f; };
   const float best = u2f(h->best);
@@ -954,28 +955,48 @@ extern "C" int cmgb_ScanBatch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo
   if (tr) { DevTrPlan *dp; if ((st = get_tr_plan(m, qdbidx, alg, &dp, errbuf)) != CMGB_OK) return st; P = &dp->plan; d_states = dp->d_states; }
   else { DevPlan *dp; if ((st = get_plan(m, qdbidx, alg, &dp, errbuf)) != CMGB_OK) return st; P = &dp->plan; d_states = dp->d_states; d_rec = dp->d_rec; }
 
-  // work items, longest sequence first (band area grows with length)
-  std::vector<int> order(nseq);
-  for (int q = 0; q < nseq; q++) order[q] = q;
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return lengths[a] > lengths[b]; });
-  std::vector<long long> ws(nseq), we(nseq);
-  for (int w = 0; w < nseq; w++) { ws[w] = offsets[order[w]] + 1; we[w] = offsets[order[w]] + lengths[order[w]]; }
+  // work items: one per sequence for the truncated scanners; the standard
+  // scanners cut sequences longer than a window into windows that start W-1
+  // rows early (as the single-sequence scan does).  Longest first.
+  const int64_t wlen = std::max<int64_t>(8LL * m->W, 2048);
+  std::vector<int> wseq;                 // sequence of each window
+  std::vector<long long> ws, we, ws0;
+  for (int q = 0; q < nseq; q++) {
+    const int64_t a = offsets[q] + 1, b = offsets[q] + lengths[q];
+    if (tr || lengths[q] <= wlen) { wseq.push_back(q); ws.push_back(a); we.push_back(b); ws0.push_back(a); continue; }
+    for (int64_t s = a; s <= b; s += wlen) {
+      wseq.push_back(q); ws.push_back(s); we.push_back(std::min<int64_t>(b, s + wlen - 1));
+      ws0.push_back(std::max<int64_t>(a, s - (m->W - 1)));
+    }
+  }
+  if (wseq.size() > (size_t) (1 << 24)) ERRF(CMGB_ERANGE, "%s, too many windows", fn);
+  const int nw = (int) wseq.size();
+  std::vector<int> order(nw);
+  for (int w = 0; w < nw; w++) order[w] = w;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return we[a] - ws0[a] > we[b] - ws0[b]; });
+  {
+    std::vector<long long> a(nw), b(nw), c(nw); std::vector<int> sq(nw);
+    for (int w = 0; w < nw; w++) { a[w] = ws[order[w]]; b[w] = we[order[w]]; c[w] = ws0[order[w]]; sq[w] = wseq[order[w]]; }
+    ws.swap(a); we.swap(b); ws0.swap(c); wseq.swap(sq);
+  }
   // one device block: residues, window ranges, per-window outputs
   auto al = [](size_t x) { return (x + 255) & ~(size_t) 255; };
-  const size_t o_ws = al((size_t) seqs_len), o_we = o_ws + al(sizeof(long long) * nseq), o_out = o_we + al(sizeof(long long) * nseq);
-  const size_t out_bytes = tr ? sizeof(unsigned long long) * nseq : sizeof(long long) * 2 * nseq + sizeof(unsigned) * nseq;
+  const size_t o_ws = al((size_t) seqs_len), o_we = o_ws + al(sizeof(long long) * nw), o_ws0 = o_we + al(sizeof(long long) * nw);
+  const size_t o_out = o_ws0 + al(sizeof(long long) * nw);
+  const size_t out_bytes = tr ? sizeof(unsigned long long) * nw : sizeof(long long) * 2 * nw + sizeof(unsigned) * nw;
   if ((st = grow((void **) &c->d_dsq, &c->dsq_bytes, o_out + al(out_bytes), errbuf)) != CMGB_OK) return st;
   unsigned char *blk = c->d_dsq;
   std::vector<unsigned char> out_init(out_bytes, 0);
   if (!tr) {
     long long *env = reinterpret_cast<long long *>(out_init.data());
-    for (int w = 0; w < nseq; w++) { env[2 * w] = LLONG_MAX; env[2 * w + 1] = -1; }
+    for (int w = 0; w < nw; w++) { env[2 * w] = LLONG_MAX; env[2 * w + 1] = -1; }
   }
   CUDA_TRY(cudaMemcpyAsync(blk, seqs, (size_t) seqs_len, cudaMemcpyHostToDevice, c->stream));
-  CUDA_TRY(cudaMemcpyAsync(blk + o_ws, ws.data(), sizeof(long long) * nseq, cudaMemcpyHostToDevice, c->stream));
-  CUDA_TRY(cudaMemcpyAsync(blk + o_we, we.data(), sizeof(long long) * nseq, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(blk + o_ws, ws.data(), sizeof(long long) * nw, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(blk + o_we, we.data(), sizeof(long long) * nw, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaMemcpyAsync(blk + o_ws0, ws0.data(), sizeof(long long) * nw, cudaMemcpyHostToDevice, c->stream));
   CUDA_TRY(cudaMemcpyAsync(blk + o_out, out_init.data(), out_bytes, cudaMemcpyHostToDevice, c->stream));
-  c->last_h2d = seqs_len + (int64_t) (2 * sizeof(long long) * nseq + out_bytes + sizeof(Control));
+  c->last_h2d = seqs_len + (int64_t) (3 * sizeof(long long) * nw + out_bytes + sizeof(Control));
 
   const bool gl = P->arena_global != 0;
   int cps = c->ctas_per_sm;
@@ -989,11 +1010,11 @@ extern "C" int cmgb_ScanBatch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo
     cps = 1;
 #endif
   }
-  const int grid = std::min(nseq, c->nsm * cps);
+  const int grid = std::min(nw, c->nsm * cps);
   if ((st = grow((void **) &c->d_carry, &c->carry_bytes, sizeof(float) * 2 * (size_t) P->carry_elems * grid, errbuf)) != CMGB_OK) return st;
   if ((st = grow((void **) &c->d_ring, &c->ring_bytes, sizeof(float) * (size_t) P->ring_elems * grid, errbuf)) != CMGB_OK) return st;
   if (gl && (st = grow((void **) &c->d_arena, &c->arena_bytes, sizeof(float) * (size_t) P->arena_elems * grid, errbuf)) != CMGB_OK) return st;
-  int cand_cap = kCandCap;
+  int cand_cap = c->cand_cap;
   if (tr && (st = tr_cand_reserve(c, kTrCandCap, &cand_cap, errbuf)) != CMGB_OK) return st;
   Control *h = c->h_ctl;
   std::vector<unsigned char> outv(out_bytes);
@@ -1014,7 +1035,7 @@ extern "C" int cmgb_ScanBatch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo
     kp.oesc = m->d_oesc; kp.ioesc = m->d_ioesc;
     kp.lmesc = m->d_lmesc; kp.rmesc = m->d_rmesc; kp.ilmesc = m->d_ilmesc; kp.irmesc = m->d_irmesc;
     kp.ilog = c->d_ilog;
-    kp.dsq = blk; kp.i0 = 1; kp.j0 = seqs_len - 2; kp.win_len = 0; kp.nwin = nseq;
+    kp.dsq = blk; kp.i0 = 1; kp.j0 = seqs_len - 2; kp.win_len = 0; kp.nwin = nw;
     kp.queue = &c->d_ctl->queue; kp.carry = c->d_carry; kp.ring = c->d_ring;
     kp.cand = c->d_trcand; kp.ncand = &c->d_ctl->ncand; kp.cand_cap = cand_cap;
     kp.cand_cut = ccut; kp.cand_pos = cpos; kp.env_cut = ecut;
@@ -1028,14 +1049,15 @@ extern "C" int cmgb_ScanBatch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo
     std::memset(&kp, 0, sizeof(kp));
     kp.st = (const StateInfo *) d_states; kp.plan = *P; kp.rec = d_rec; kp.arena = c->d_arena;
     kp.oesc = m->d_oesc; kp.ioesc = m->d_ioesc; kp.ilog = c->d_ilog; kp.flog = c->d_flog;
-    kp.dsq = blk; kp.i0 = 1; kp.j0 = seqs_len - 2; kp.win_len = 0; kp.nwin = nseq;
+    kp.dsq = blk; kp.i0 = 1; kp.j0 = seqs_len - 2; kp.win_len = 0; kp.nwin = nw;
     kp.queue = &c->d_ctl->queue; kp.carry = c->d_carry; kp.ring = c->d_ring;
-    kp.cand = c->d_cand; kp.ncand = &c->d_ctl->ncand; kp.cand_cap = kCandCap;
+    kp.cand = c->d_cand; kp.ncand = &c->d_ctl->ncand; kp.cand_cap = cand_cap;
     kp.cand_cut = ccut; kp.cand_pos = cpos; kp.env_cut = ecut;
     kp.env = reinterpret_cast<long long *>(blk + o_out);
-    kp.best = reinterpret_cast<unsigned *>(blk + o_out + sizeof(long long) * 2 * nseq);
+    kp.best = reinterpret_cast<unsigned *>(blk + o_out + sizeof(long long) * 2 * nw);
     kp.vsc = nullptr; kp.err = &c->d_ctl->err;
     kp.win_s = reinterpret_cast<const long long *>(blk + o_ws); kp.win_e = reinterpret_cast<const long long *>(blk + o_we);
+    kp.win_s0 = reinterpret_cast<const long long *>(blk + o_ws0);
     launch_any(alg, gl, grid, c->threads, (size_t) P->smem_bytes, c->stream, kp);
   }
   CUDA_TRY(cudaGetLastError());
@@ -1048,8 +1070,15 @@ extern "C" int cmgb_ScanBatch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo
   c->last_d2h = (int64_t) (sizeof(Control) + out_bytes);
   if (h->err & 2) ERRF(CMGB_ENODEV, "%s, a bounded device wait ran out (phase record copy)", fn);
   if (!(h->err & 1)) break;
-  if (!tr || attempt > 0) ERRF(CMGB_ERANGE, "%s, more than %d candidate root cells; raise the cutoff", fn, cand_cap);
-  if ((st = tr_cand_reserve(c, (int64_t) h->ncand + h->ncand / 4, &cand_cap, errbuf)) != CMGB_OK) return st;
+  if (attempt > 0) ERRF(CMGB_ERANGE, "%s, more than %d candidate root cells; raise the cutoff", fn, cand_cap);
+  const int64_t need = (int64_t) h->ncand + h->ncand / 4;
+  if (tr) { if ((st = tr_cand_reserve(c, need, &cand_cap, errbuf)) != CMGB_OK) return st; }
+  else {   // grow the standard candidate buffer (kept for later calls)
+    if (need > kTrCandMax) ERRF(CMGB_ERANGE, "%s, more than %lld candidate root cells; raise the cutoff", fn, (long long) kTrCandMax);
+    cudaFree(c->d_cand); c->d_cand = nullptr; c->cand_cap = 0;
+    if (cudaMalloc(&c->d_cand, sizeof(Cand) * (size_t) need) != cudaSuccess) ERRF(CMGB_EMEM, "%s, out of device memory for candidates", fn);
+    c->cand_cap = cand_cap = (int) need;
+  }
   }
   auto u2f = [](unsigned u) { if (u == 0) return CMGB_IMPOSSIBLE; unsigned b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u; float f; std::memcpy(&f, &b, 4); return f; };
 
@@ -1075,14 +1104,14 @@ extern "C" int cmgb_ScanBatch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo
         e++;
       }
       const TrCand &t = tc[wq];
-      const int sq = order[t.win];
+      const int sq = wseq[t.win];
       if (t.f >= env_cutoff) { envi[sq] = std::min<int64_t>(envi[sq], t.j - t.d + 1); envj[sq] = std::max<int64_t>(envj[sq], t.j); }
       if (hitlist) { CandHost ch; ch.j = t.j; ch.d = t.d; ch.sc = t.f; ch.r = t.y; ch.mode = t.mode; per[sq].push_back(ch); }
       q = e;
     }
     const unsigned long long *wb = reinterpret_cast<const unsigned long long *>(outv.data());
-    for (int w = 0; w < nseq; w++) {
-      const int sq = order[w];
+    for (int w = 0; w < nw; w++) {
+      const int sq = wseq[w];
       const unsigned long long k = wb[w];
       if (ret_sc) ret_sc[sq] = k ? u2f((unsigned) (k >> 32)) : CMGB_IMPOSSIBLE;
       if (ret_mode) ret_mode[sq] = k ? 3 - (int) ((0xFFFFFFFFu - (unsigned) (k & 0xFFFFFFFFULL)) & 3u) : CMGB_TRMODE_UNKNOWN;
@@ -1103,12 +1132,16 @@ extern "C" int cmgb_ScanBatch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo
       }
     }
     const long long *env = reinterpret_cast<const long long *>(outv.data());
-    const unsigned *best = reinterpret_cast<const unsigned *>(outv.data() + sizeof(long long) * 2 * nseq);
-    for (int w = 0; w < nseq; w++) {
-      const int sq = order[w];
-      if (env[2 * w + 1] >= 0) { envi[sq] = env[2 * w]; envj[sq] = env[2 * w + 1]; }
-      if (ret_sc) ret_sc[sq] = u2f(best[w]);
-      if (ret_mode) ret_mode[sq] = CMGB_TRMODE_J;
+    const unsigned *best = reinterpret_cast<const unsigned *>(outv.data() + sizeof(long long) * 2 * nw);
+    std::vector<unsigned> bestq(nseq, 0u);
+    for (int w = 0; w < nw; w++) {   // a long sequence's windows: union of envelopes, best of scores
+      const int sq = wseq[w];
+      if (env[2 * w + 1] >= 0) { envi[sq] = std::min<int64_t>(envi[sq], env[2 * w]); envj[sq] = std::max<int64_t>(envj[sq], env[2 * w + 1]); }
+      bestq[sq] = std::max(bestq[sq], best[w]);
+    }
+    for (int q = 0; q < nseq; q++) {
+      if (ret_sc) ret_sc[q] = u2f(bestq[q]);
+      if (ret_mode) ret_mode[q] = CMGB_TRMODE_J;
     }
   }
   for (int q = 0; q < nseq; q++) {

@@ -132,9 +132,11 @@ struct KParams {
   int *err;                   // error word: 1 candidate overflow, 2 a bounded wait ran out
   const unsigned char *rec;   // phase records (descriptor + emission row), see build_records
   float *arena;               // [grid][arena_elems] global tile arena (plans with arena_global)
-  // batched scans: window w is the whole scan [win_s[w], win_e[w]] of one
-  // sequence (no warm-up rows); env and best are then per-window arrays
-  const long long *win_s, *win_e;
+  // batched scans: window w owns end positions [win_s[w], win_e[w]] and
+  // starts computing at win_s0[w] (its sequence's start, or W-1 rows before
+  // win_s for a later window of a long sequence); env and best are then
+  // per-window arrays
+  const long long *win_s, *win_e, *win_s0;
 };
 
 // Order-preserving float <-> uint mapping for atomicMax.
@@ -293,7 +295,7 @@ CMGB_DEV void qdb_scan_body(const KParams &p, float *smf, int tid, int nt, int b
     const int w = *s_win;
     if (w >= p.nwin) break;
     long long own_s, own_e, s0;
-    if (p.win_s) { own_s = s0 = p.win_s[w]; own_e = p.win_e[w]; }
+    if (p.win_s) { own_s = p.win_s[w]; own_e = p.win_e[w]; s0 = p.win_s0 ? p.win_s0[w] : own_s; }
     else {
       own_s = p.i0 + (long long) w * p.win_len;
       own_e = own_s + p.win_len - 1;

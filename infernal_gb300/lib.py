@@ -36,7 +36,7 @@ EXPORTS = [
     "cmgb_FastIInsideScan_dev", "cmgb_count_cells", "cmgb_autotune", "cmgb_FastCYKScan_noalloc",
     "cmgb_FastFInsideScan", "cmgb_FastFInsideScan_dev",
     "cmgb_RefTrCYKScan", "cmgb_RefITrInsideScan", "cmgb_RefTrCYKScan_dev", "cmgb_RefITrInsideScan_dev",
-    "cmgb_ScanBatch",
+    "cmgb_ScanBatch", "cmgb_filter_create", "cmgb_filter_destroy", "cmgb_filter_windows",
 ]
 BATCH_ALGOS = {"cyk": 0, "inside": 1, "finside": 2, "trcyk": 3, "trinside": 4}
 
@@ -98,6 +98,11 @@ def bind(path: str) -> ctypes.CDLL:
         f.restype = I
     lib.cmgb_ScanBatch.argtypes = [P, P, ctypes.c_char_p, I, I, I, P, I64, P, P, I, F, P, I, F, P, P, P, P, P]
     lib.cmgb_ScanBatch.restype = I
+    lib.cmgb_filter_create.argtypes = [P, I, P, P, P, P, ctypes.POINTER(P), ctypes.c_char_p]
+    lib.cmgb_filter_create.restype = I
+    lib.cmgb_filter_destroy.argtypes = [P]
+    lib.cmgb_filter_windows.argtypes = [P, P, P, I64, I64, P, I64, ctypes.POINTER(I64), ctypes.POINTER(F), ctypes.c_char_p]
+    lib.cmgb_filter_windows.restype = I
     lib.cmgb_autotune.argtypes = [P, P, I, I, I64, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.c_char_p]
     lib.cmgb_autotune.restype = I
     lib.cmgb_FastCYKScan_noalloc.argtypes = [P, P, ctypes.c_char_p, I, P, I64, I64, F, F, P, I, ctypes.POINTER(I),

@@ -1,0 +1,347 @@
+"""Learned window pre-filter ahead of the QDB-CYK stage.
+
+The network (scored on the GPU by the hand-written kernels of
+``csrc/filter.cu`` through ``cmgb_filter_windows``): windows of 2W residues at
+stride W, one-hot ACGU, six dilated convolutions (kernel 9, dilations
+1..32, 4 -> 128 -> 128 channels, ReLU), max over positions, linear read-out.
+Weights and activations are BF16 with FP32 accumulation.
+
+Training data come from the plain scanner itself: windows are labelled
+positive when the plain QDB-CYK scan (cutoff ``CYK_CUT``) followed by the
+QDB2 Inside scan (cutoff ``INS_CUT``) reports a hit in them.  Positives are windows holding sequences emitted by the CM (whole or
+cut at random points) in background of varying GC; negatives are iid
+background and dinucleotide-shuffled positives (the Altschul-Erickson
+doublet-preserving shuffle, restated here).  PyTorch fits the weights
+(``train``); only the exported arrays are used at scan time.
+
+``filtered_scan`` is the pipeline: filter all windows of both strands, keep
+those above the threshold, merge them into regions and run the plain
+CYK -> Inside scan on the regions only.  The plain scan on everything stays
+the judge of what the filter misses.
+
+    python -m infernal_gb300.prefilter train <model> <out.npz> [n_windows] [steps]
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import sys
+import time
+from typing import List, Optional, Tuple
+
+import numpy as np
+
+from . import cmfile, emit, lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CYK_CUT = 10.0
+INS_CUT = 15.0
+CH, KT, DIL = 128, 9, (1, 2, 4, 8, 16, 32)
+
+
+# ---------------------------------------------------------------------------
+# sequences
+def dinuc_shuffle(seq: str, rng: np.random.Generator) -> str:
+    """Doublet-preserving shuffle (Altschul & Erickson 1985): a random Euler
+    path through the multigraph of the sequence's dinucleotides that starts
+    and ends where the sequence does.  Last exit edges of every vertex but
+    the final one form a random tree towards the final vertex; the other
+    edges leave each vertex in random order."""
+    if len(seq) < 3:
+        return seq
+    edges = {}
+    for a, b in zip(seq[:-1], seq[1:]):
+        edges.setdefault(a, []).append(b)
+    last = seq[-1]
+    verts = list(edges.keys())
+    # random last-exit tree: for each vertex, pick a random exit such that
+    # following last exits reaches `last` (Wilson-style loop-erased walks)
+    in_tree = {last: True}
+    last_exit = {}
+    for v in verts:
+        u = v
+        path = {}
+        while u not in in_tree:
+            nxt = edges[u][int(rng.integers(len(edges[u])))]
+            path[u] = nxt
+            u = nxt
+        u = v
+        while u not in in_tree:
+            last_exit[u] = path[u]
+            in_tree[u] = True
+            u = path[u]
+    order = {}
+    for v, outs in edges.items():
+        outs = list(outs)
+        if v in last_exit:
+            outs.remove(last_exit[v])
+            rng.shuffle(outs)
+            outs.append(last_exit[v])
+        else:
+            rng.shuffle(outs)
+        order[v] = outs[::-1]          # pop from the end
+    out = [seq[0]]
+    u = seq[0]
+    while order.get(u):
+        u = order[u].pop()
+        out.append(u)
+    return "".join(out)
+
+
+def background(rng: np.random.Generator, n: int, gc: float) -> str:
+    p = [(1 - gc) / 2, gc / 2, gc / 2, (1 - gc) / 2]
+    return "".join(rng.choice(list("ACGU"), n, p=p))
+
+
+def make_windows(m: cmfile.CMModel, n: int, rng: np.random.Generator) -> List[np.ndarray]:
+    """n training windows of 2W residues: a third with an emitted sequence
+    (whole or cut at random 5'/3' points) at a random offset, a third iid
+    background and a third dinucleotide-shuffled emitted-sequence windows;
+    GC drawn from 0.35-0.60 per window."""
+    W2 = 2 * m.W
+    pool = [emit.sample(m, rng) for _ in range(min(n, 1500))]   # emitted sequences, reused with random cuts
+    out = []
+    for k in range(n):
+        gc = float(rng.uniform(0.35, 0.60))
+        kind = k % 3
+        if kind == 1:
+            s = background(rng, W2, gc)
+        else:
+            e = pool[int(rng.integers(len(pool)))]
+            if rng.random() < 0.15 and len(e) > 40:
+                a, b = sorted(int(x) for x in rng.integers(0, len(e) + 1, 2))
+                e = e[a:b] if b - a >= 20 else e
+            if rng.random() < 0.5:
+                e = emit.revcomp(e)
+            e = e[:W2]
+            bg = background(rng, W2, gc)
+            pos = int(rng.integers(0, W2 - len(e) + 1))
+            s = bg[:pos] + e + bg[pos + len(e):]
+            if kind == 2:
+                s = dinuc_shuffle(s, rng)
+        out.append(cmfile.digitize(s[:W2]))
+    return out
+
+
+def label_windows(sc: "lib.Scanner", m: cmfile.CMModel, wins: List[np.ndarray], chunk: int = 2000) -> np.ndarray:
+    """1 where the plain pipeline reports a final hit in the window: a
+    QDB-CYK survivor (>= CYK_CUT) that the QDB2 Inside scan keeps (>= INS_CUT),
+    i.e. the hits the filter must not lose."""
+    lab = np.zeros(len(wins), np.float32)
+    for a in range(0, len(wins), chunk):
+        rs = sc.scan_batch(m, wins[a:a + chunk], algo="cyk", qdbidx=1, cutoff=CYK_CUT, env_cutoff=CYK_CUT,
+                           do_null3=True)
+        surv = [a + q for q, r in enumerate(rs) if r.hits]
+        if surv:
+            r2 = sc.scan_batch(m, [wins[k] for k in surv], algo="inside", qdbidx=2, cutoff=INS_CUT,
+                               env_cutoff=INS_CUT, do_null3=True)
+            for k, r in zip(surv, r2):
+                lab[k] = 1.0 if r.hits else 0.0
+    return lab
+
+
+def onehot(wins: List[np.ndarray]):
+    import torch
+    X = np.zeros((len(wins), 4, len(wins[0]) - 2), np.float32)
+    for k, d in enumerate(wins):
+        body = d[1:-1]
+        ok = body < 4
+        X[k, body[ok], np.nonzero(ok)[0]] = 1.0
+    return torch.from_numpy(X)
+
+
+# ---------------------------------------------------------------------------
+# network (training only)
+def make_net():
+    import torch
+    import torch.nn as nn
+
+    class FilterNet(nn.Module):
+        """Convolution -> batch norm -> ReLU per layer; the batch norms are
+        folded into the convolutions' weights and biases at export."""
+        def __init__(self):
+            super().__init__()
+            self.convs = nn.ModuleList()
+            self.norms = nn.ModuleList()
+            cin = 4
+            for d in DIL:
+                self.convs.append(nn.Conv1d(cin, CH, KT, dilation=d, padding=4 * d))
+                self.norms.append(nn.BatchNorm1d(CH))
+                cin = CH
+            self.out = nn.Linear(CH, 1)
+
+        def forward(self, x):
+            for c, n in zip(self.convs, self.norms):
+                x = torch.relu(n(c(x)))
+            return self.out(x.amax(dim=2)).squeeze(1)
+    return FilterNet()
+
+
+def _folded(net, l):
+    """Layer l's convolution with its (eval-mode) batch norm folded in:
+    weight [co, ci, 9] and bias [co], float32."""
+    c, n = net.convs[l], net.norms[l]
+    scale = (n.weight / (n.running_var + n.eps).sqrt()).detach().float()
+    w = c.weight.detach().float() * scale[:, None, None]
+    b = (c.bias.detach().float() - n.running_mean.float()) * scale + n.bias.detach().float()
+    return w.cpu(), b.cpu()
+
+
+def export(net) -> dict:
+    """Weights in the kernel layout (csrc/filter.cu)."""
+    import torch
+    net = net.eval()
+    w0, b0 = _folded(net, 0)
+    w0k = np.ascontiguousarray(w0.numpy().transpose(2, 1, 0))  # [9][4][128]
+    ws, bs = [], [b0.numpy()]
+    for l in range(1, 6):
+        w, b = _folded(net, l)                                # [co, ci, 9]
+        w = w.permute(2, 0, 1).contiguous().to(torch.bfloat16)  # [9][co][ci]
+        ws.append(w.view(torch.int16).numpy().view(np.uint16))
+        bs.append(b.numpy())
+    wb = np.ascontiguousarray(np.stack(ws))                    # [5][9][128][128]
+    bias = np.stack(bs).astype(np.float32)
+    wout = np.concatenate([net.out.weight.detach().float().cpu().numpy().ravel(),
+                           net.out.bias.detach().float().cpu().numpy().ravel()]).astype(np.float32)
+    return {"w0": w0k.astype(np.float32), "w": wb, "bias": bias, "wout": wout}
+
+
+def reference_logits(weights: dict, wins: List[np.ndarray]) -> np.ndarray:
+    """The network in PyTorch FP32 on the exported weights, with the kernel's
+    BF16 rounding points (weights of layers 2-6, every layer's output)."""
+    import torch
+    import torch.nn.functional as F
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    x = onehot(wins).to(dev)
+    w0 = torch.from_numpy(weights["w0"]).to(dev).permute(2, 1, 0).contiguous()   # [128, 4, 9]
+    b = torch.from_numpy(weights["bias"]).to(dev)
+    bf = lambda t: t.to(torch.bfloat16).float()
+    x = bf(torch.relu(F.conv1d(x, w0, b[0], padding=4, dilation=1)))
+    wb = torch.from_numpy(weights["w"].view(np.int16)).to(dev).view(torch.bfloat16).float()   # [5][9][co][ci]
+    for l in range(1, 6):
+        w = wb[l - 1].permute(1, 2, 0).contiguous()            # [co, ci, 9]
+        x = bf(torch.relu(F.conv1d(x, w, b[l], padding=4 * DIL[l], dilation=DIL[l])))
+    wo = torch.from_numpy(weights["wout"]).to(dev)
+    return (x.amax(dim=2) @ wo[:CH] + wo[CH]).cpu().numpy()
+
+
+def train(net, X, y, steps: int = 3000, batch: int = 256, lr: float = 1e-3, seed: int = 0):
+    import torch
+    torch.manual_seed(seed)
+    dev = "cuda"
+    net = net.to(dev)
+    opt = torch.optim.AdamW(net.parameters(), lr=lr, weight_decay=1e-4)
+    sched = torch.optim.lr_scheduler.OneCycleLR(opt, max_lr=lr, total_steps=steps, pct_start=0.1)
+    pos_w = torch.tensor(max(1.0, float((y == 0).sum()) / max(1.0, float((y == 1).sum()))), device=dev)
+    lossf = torch.nn.BCEWithLogitsLoss(pos_weight=pos_w)
+    Xd, yd = X.to(dev), torch.from_numpy(y).to(dev)
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    for it in range(steps):
+        idx = torch.randint(0, len(yd), (batch,), generator=g).to(dev)
+        with torch.autocast("cuda", dtype=torch.bfloat16):
+            out = net(Xd[idx])
+        loss = lossf(out.float(), yd[idx])
+        opt.zero_grad(set_to_none=True)
+        loss.backward()
+        torch.nn.utils.clip_grad_norm_(net.parameters(), 1.0)
+        opt.step()
+        sched.step()
+        if it % 500 == 0:
+            print(f"step {it} loss {loss.item():.4f}", flush=True)
+    return net
+
+
+def save(weights: dict, path: str, **meta) -> None:
+    np.savez_compressed(path, **weights, **{k: np.asarray(v) for k, v in meta.items()})
+
+
+def load(path: str) -> dict:
+    z = np.load(path)
+    return {k: z[k] for k in z.files}
+
+
+# ---------------------------------------------------------------------------
+# scan-time use
+class Prefilter:
+    """The network on one device context (cmgb_filter_*)."""
+
+    def __init__(self, scanner: "lib.Scanner", weights: dict, W: int):
+        self.sc, self.lib = scanner, scanner.lib
+        self.W = W
+        self.thr = float(weights.get("threshold", 0.0))
+        self._keep = [np.ascontiguousarray(weights["w0"], np.float32), np.ascontiguousarray(weights["w"], np.uint16),
+                      np.ascontiguousarray(weights["bias"], np.float32), np.ascontiguousarray(weights["wout"], np.float32)]
+        self._f = ctypes.c_void_p()
+        err = ctypes.create_string_buffer(256)
+        st = self.lib.cmgb_filter_create(scanner._ctx, W, *[a.ctypes.data for a in self._keep], ctypes.byref(self._f), err)
+        if st != 0:
+            raise lib.ScanError(st, err.value.decode())
+
+    def close(self):
+        if self._f:
+            self.lib.cmgb_filter_destroy(self._f)
+            self._f = ctypes.c_void_p()
+
+    def logits(self, d_dsq_ptr: int, i0: int, j0: int) -> Tuple[np.ndarray, float]:
+        """Window logits over [i0, j0] of device-resident residues, and the device ms."""
+        n = (j0 - i0 + 1 + self.W - 1) // self.W
+        out = np.zeros(n, np.float32)
+        nw, ms = ctypes.c_int64(), ctypes.c_float()
+        err = ctypes.create_string_buffer(256)
+        st = self.lib.cmgb_filter_windows(self.sc._ctx, self._f, d_dsq_ptr, i0, j0, out.ctypes.data, n,
+                                          ctypes.byref(nw), ctypes.byref(ms), err)
+        if st != 0:
+            raise lib.ScanError(st, err.value.decode())
+        return out[: nw.value], float(ms.value)
+
+    def regions(self, logits: np.ndarray, i0: int, j0: int, thr: Optional[float] = None) -> List[Tuple[int, int]]:
+        """Kept windows (logit > thr) merged into scan regions [a, b]."""
+        thr = self.thr if thr is None else thr
+        regs: List[List[int]] = []
+        for k in np.nonzero(logits > thr)[0]:
+            a, b = i0 + int(k) * self.W, min(j0, i0 + int(k) * self.W + 2 * self.W - 1)
+            if regs and a <= regs[-1][1] + 1:
+                regs[-1][1] = max(regs[-1][1], b)
+            else:
+                regs.append([a, b])
+        return [(a, b) for a, b in regs]
+
+
+def main(argv):
+    if len(argv) < 4 or argv[1] != "train":
+        print(__doc__)
+        return 2
+    import torch
+    name, out = argv[2], argv[3]
+    nwin = int(argv[4]) if len(argv) > 4 else 60000
+    steps = int(argv[5]) if len(argv) > 5 else 4000
+    m = cmfile.load_npz(os.path.join(ROOT, "tests", "golden", f"{name}.model.npz"))
+    rng = np.random.default_rng(20261205)
+    t0 = time.time()
+    wins = make_windows(m, nwin, rng)
+    sc = lib.Scanner(0)
+    y = label_windows(sc, m, wins)
+    print(f"{nwin} windows, {int(y.sum())} positive, made+labelled in {time.time() - t0:.0f}s", flush=True)
+    ntr = int(0.85 * nwin)
+    X = onehot(wins)
+    net = train(make_net(), X[:ntr], y[:ntr], steps=steps)
+    wts = export(net.float())
+    # threshold: keep >= 99.5% of the validation positives
+    val = reference_logits(wts, wins[ntr:])
+    pos = np.sort(val[y[ntr:] == 1])
+    thr = float(pos[int(0.005 * len(pos))] - 1e-3) if len(pos) else 0.0
+    kept_neg = float((val[y[ntr:] == 0] > thr).mean())
+    print(f"threshold {thr:.3f}: validation positives kept {(val[y[ntr:] == 1] > thr).mean():.4f}, "
+          f"negatives kept {kept_neg:.4f}", flush=True)
+    bg = np.array([k % 3 == 1 for k in range(ntr, nwin)])      # pure background windows
+    print(f"  background windows kept {float((val[bg] > thr).mean()):.4f}", flush=True)
+    for q in (0.9, 0.95, 0.98, 0.99, 0.999):
+        t = float(pos[int((1 - q) * len(pos))] - 1e-3) if len(pos) else 0.0
+        print(f"  recall {q}: threshold {t:.3f}, negatives kept {float((val[y[ntr:] == 0] > t).mean()):.4f}", flush=True)
+    save(wts, out, threshold=thr, W=m.W, trained_windows=ntr)
+    sc.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main(sys.argv))
