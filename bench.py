@@ -56,11 +56,11 @@ def _env_int(k, d):
         return d
 
 
-def make_step_input(model_glob, step, mb, seed=20261203):
+def make_step_input(model_glob, step, mb, seed=20261203, hits_per_mb=2.0):
     from infernal_gb300 import emit
     rng = np.random.default_rng([seed, step])
     L = int(mb * 1_000_000)
-    nhits = max(1, int(round(20 * mb / 10)))     # 200 hits per 100 Mb
+    nhits = max(1, int(round(hits_per_mb * mb)))     # default: 200 hits per 100 Mb
     ins = [emit.sample(model_glob, rng) for _ in range(nhits)]
     dsq, spans = emit.make_target(rng, L, 0.40, ins)
     return dsq, emit.revcomp_dsq(dsq)
@@ -208,7 +208,7 @@ def run_learned(args, rank, world):
     sc = L.Scanner(0)
     filt = prefilter.Prefilter(sc, wts, m.W)
     nsteps = args.warmup + args.steps
-    inputs = [make_step_input(m, 500000 + s, args.mb) for s in range(nsteps)]
+    inputs = [make_step_input(m, 500000 + s, args.mb, hits_per_mb=args.hits_per_mb) for s in range(nsteps)]
     Lres = len(inputs[0][0]) - 2
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     sc.autotune(m, 1, "cyk"); sc.autotune(m, 2, "inside")
@@ -281,13 +281,19 @@ def run_learned(args, rank, world):
     t0 = time.perf_counter()
     phits = [plain_step(inputs[s], [t.data_ptr() for t in dev[s]]) for s in range(args.warmup, nsteps)]
     t_plain = time.perf_counter() - t0
-    nplain = nfound = 0
+    # E <= 0.01 at this search size from the CM's local Inside calibration
+    # (ECMLI line of Plant_SRP.c.cm: lambda, mu_extrap, calibration db size,
+    # random hits): E = nrandhits * Z / dbsize * exp(-lambda (S - mu)), Z = residues per step
+    lam, mu, cdb, nrand = 0.70748, -9.17856, 1600000.0, 519142.0
+    e_bits = mu - np.log(0.01 / (nrand * (2 * Lres) / cdb)) / lam
+    nplain = nfound = ne = nef = 0
     for ph, fh in zip(phits, fhits):
         for sp, sf in zip(ph, fh):
             for h in sp:
-                nplain += 1
-                if any(_overlap(h, g) >= 0.5 * (h[1] - h[0] + 1) for g in sf):
-                    nfound += 1
+                found = any(_overlap(h, g) >= 0.5 * (h[1] - h[0] + 1) for g in sf)
+                nplain += 1; nfound += found
+                if h[2] >= e_bits:
+                    ne += 1; nef += found
     res = 2 * Lres * args.steps
     value = res / tot / 1e6
     out = {
@@ -295,7 +301,8 @@ def run_learned(args, rank, world):
         "value": round(value, 3), "unit": "Mres/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1000 * tot / args.steps, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "bf16 (filter) + f32 (CYK) + int32 (Inside)", "data": "synthetic",
-        "config": {"workload": f"Plant_SRP CM stand-in, {args.mb} Mb x 2 strands per step, GC 0.40; filter threshold "
+        "config": {"workload": f"Plant_SRP CM stand-in, {args.mb} Mb x 2 strands per step, GC 0.40, "
+                               f"{args.hits_per_mb} emitted hits per Mb; filter threshold "
                                f"{filt.thr:.3f}; kept regions scanned by CYK QDB1 ({CYK_CUT} bits) -> Inside QDB2 ({INS_CUT} bits)",
                    "l2": "flushed between timed steps (256 MB write)", "parallelism": "1 GPU"},
         "plain_mres_s": round(res / t_plain / 1e6, 3),
@@ -303,6 +310,8 @@ def run_learned(args, rank, world):
         "fraction_scanned": round(kept / res, 4),
         "hits_plain": nplain, "hits_found": nfound,
         "hit_loss": round(1.0 - nfound / nplain, 4) if nplain else None,
+        "e001_bits": round(float(e_bits), 2), "e001_hits_plain": ne, "e001_hits_found": nef,
+        "e001_hit_loss": round(1.0 - nef / ne, 4) if ne else None,
         "kernel_ms_per_step": round(kms / args.steps, 3),
         "clocks": clocks,
     }
@@ -628,6 +637,7 @@ def main():
                     help="plain: the single-large-CM scan (default); trunc: the truncated-mode read batch; "
                          "learned: the pre-filtered pipeline against the plain scan")
     ap.add_argument("--reads", type=int, default=5000, help="reads per step of the trunc workload")
+    ap.add_argument("--hits-per-mb", type=float, default=2.0, help="embedded hits per Mb (learned workload)")
     args = ap.parse_args()
     world = _env_int("WORLD_SIZE", 1)
     rank = _env_int("RANK", 0)

@@ -2,6 +2,7 @@
 
     python -m infernal_gb300.profile_case <model> <length> <cyk|inside|finside> [tile_rows arena]
     python -m infernal_gb300.profile_case <model> <nreads> <trcyk|trinside> [tile_rows arena]
+    python -m infernal_gb300.profile_case <model> <length> filter
 
 <model> is a configured model under tests/golden (tRNA, Vault, Plant_SRP).
 The standard scanners scan one target of <length> residues; the truncated
@@ -36,7 +37,20 @@ def main(argv):
     if len(argv) > 5:
         sc.set_shape(int(argv[4]), 0, 0, 0, int(argv[5]))
         shape = (int(argv[4]), int(argv[5]))
-    if algo.startswith("tr"):
+    if algo == "filter":
+        import torch
+        from . import prefilter
+        wts = prefilter.load(os.path.join(ROOT, "infernal_gb300", "filters", f"{name}.filter.npz"))
+        dsq, _ = emit.make_target(rng, L, 0.40, [])
+        d = torch.from_numpy(dsq).cuda()
+        f = prefilter.Prefilter(sc, wts, m.W)
+        for _ in range(2):
+            t = time.time()
+            lg, ms = f.logits(d.data_ptr(), 1, L)
+            print(f"{name} L={L} filter windows={len(lg)} kept={(lg > f.thr).mean():.4f} kernel_ms={ms:.2f} "
+                  f"wall_s={time.time() - t:.2f}")
+        f.close()
+    elif algo.startswith("tr"):
         reads = [cmfile.digitize("".join(rng.choice(list("ACGU"), int(rng.integers(100, 401))))) for _ in range(L)]
         for _ in range(2):
             t = time.time()
