@@ -15,10 +15,10 @@
 // bf16, biases [6][128] f32, read-out [128] + 1 f32.
 //
 // Layers 1-5 are implicit GEMMs (M = window positions, N = 128 output
-// channels, K = 9 taps x 128 input channels) on the tensor cores with
-// mma.sync m16n8k16 BF16 -> FP32: a CTA computes a 128 x 128 output tile; its
-// input rows for all nine taps (128 + 8 d rows) are staged once in shared
-// memory, the tap's weights per tap.
+// channels, K = 9 taps x 128 input channels) on the fifth-generation tensor
+// cores (tcgen05.mma, BF16 x BF16 -> FP32 in TMEM): a CTA computes a 128 x 128
+// output tile; its input rows for all nine taps (128 + 8 d rows) are staged
+// once in shared memory, the tap's weights per tap.
 #ifdef CMGB_HOST_EMULATION
 #include "cmgb_emu.h"
 #endif
@@ -39,7 +39,6 @@ constexpr int CH = 128;      // channels
 constexpr int KT = 9;        // kernel taps
 constexpr int NL = 6;        // layers
 constexpr int TILE = 128;    // positions per CTA tile
-constexpr int SROW = CH + 8; // padded shared-memory row (bf16 elements): conflict-free fragment loads
 constexpr int DIL[NL] = {1, 2, 4, 8, 16, 32};
 }
 
@@ -52,6 +51,7 @@ struct cmgb_filter_s {
   unsigned short *d_act[2] = {nullptr, nullptr};
   size_t act_rows = 0;
   float *d_logit = nullptr; size_t logit_n = 0;
+  int *d_err = nullptr;               // set by a tensor-core wait that ran out
 };
 
 #ifndef CMGB_HOST_EMULATION
@@ -88,95 +88,119 @@ __global__ void filter_layer0(const unsigned char *dsq, long long i0, long long 
   }
 }
 
-__device__ __forceinline__ void mma_bf16(float *c, const unsigned *a, const unsigned *bq)
+// ---- layers 1-5 on tcgen05 ------------------------------------------------
+// One CTA (4 warps) computes a 128-position x 128-channel tile with
+// tcgen05.mma (cta_group::1, kind::f16, BF16 x BF16 -> FP32, M = N = 128,
+// K = 16 per instruction) accumulating in 128 TMEM columns.  Operands sit in
+// shared memory in the K-major, non-swizzled canonical layout: 8-row x
+// 16-byte core matrices, chunk c (8 input channels) of row r at
+// (c * rows + r) * 16 bytes, so a tap's shift by (t * dil) rows is a 16-byte
+// multiple of the start address.  Descriptors: leading (K) byte offset =
+// one chunk plane, stride (M/N) byte offset = 128 bytes between 8-row core
+// matrices.  Thread 0 issues the 8 MMAs of a tap and commits them to an
+// mbarrier; every wait is bounded and sets *err on expiry.
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned) __cvta_generic_to_shared(p); }
+__device__ __forceinline__ unsigned long long umma_desc(unsigned saddr, unsigned lbo, unsigned sbo)
 {
-  asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
-               : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-               : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(bq[0]), "r"(bq[1]));
+  return (unsigned long long) ((saddr >> 4) & 0x3FFFu) | ((unsigned long long) ((lbo >> 4) & 0x3FFFu) << 16) |
+         ((unsigned long long) ((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);   // version 1, no swizzle
+}
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *mb, unsigned parity)
+{
+  for (int it = 0; it < (1 << 24); it++) {
+    unsigned ok;
+    asm volatile("{\n .reg .pred P1;\n mbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n selp.b32 %0, 1, 0, P1;\n}"
+                 : "=r"(ok) : "r"(smem_u32(mb)), "r"(parity) : "memory");
+    if (ok) return true;
+  }
+  return false;
 }
 
-// Layers 1-5: out[w][i][co] = relu(b[co] + sum_t sum_ci in[w][i + (t-4) d][ci] * wt[t][co][ci]).
-// Grid: (LP / 128 tiles, nwin); 256 threads = 8 warps, warp (wm, wn) owns
-// rows 32 wm .. +32 and columns 64 wn .. +64 of the tile.
-__global__ void __launch_bounds__(256) filter_conv(const unsigned short *in, unsigned short *out, int LP, int W2, int dil,
-                                                   const unsigned short *wt, const float *bias)
+__global__ void __launch_bounds__(128, 1) filter_conv_tc(const unsigned short *in, unsigned short *out, int LP, int W2, int dil,
+                                                         const unsigned short *wt, const float *bias, int *err)
 {
-  extern __shared__ __align__(16) unsigned short fsm[];
-  const int rows = TILE + 8 * dil;             // staged input rows: tile plus the taps' reach
-  unsigned short *sA = fsm;                    // [rows][SROW]
-  unsigned short *sB = fsm + (size_t) rows * SROW;   // [128 co][SROW]
+  extern __shared__ __align__(1024) unsigned char tsm[];
+  const int rows = TILE + 8 * dil;
+  unsigned char *sA = tsm;                                    // [16 chunks][rows][16 B]
+  unsigned char *sB = tsm + (size_t) 16 * rows * 16;          // [16 chunks][128][16 B]
+  unsigned long long *mbar = reinterpret_cast<unsigned long long *>(sB + 16 * CH * 16);
+  unsigned *tslot = reinterpret_cast<unsigned *>(mbar + 1);
   const int tile = blockIdx.x, win = blockIdx.y;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int wm = warp & 3, wn = warp >> 2;
-  const int g = lane >> 2, tg = lane & 3;
-  const int p0 = tile * TILE - 4 * dil;        // window position of staged row 0
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" :: "r"(smem_u32(tslot)), "r"(128) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(mbar)), "r"(1) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  const int p0 = tile * TILE - 4 * dil;
   const unsigned short *inw = in + (size_t) win * LP * CH;
-  // stage the input rows (16-byte chunks); rows outside [0, LP) are zero
-  for (int x = tid; x < rows * (CH / 8); x += blockDim.x) {
-    const int r = x / (CH / 8), c8 = x - r * (CH / 8);
+  for (int x = tid; x < rows * 16; x += blockDim.x) {
+    const int r = x >> 4, c = x & 15;
     const int p = p0 + r;
     uint4 v = make_uint4(0, 0, 0, 0);
-    if (p >= 0 && p < LP) v = *reinterpret_cast<const uint4 *>(inw + (size_t) p * CH + c8 * 8);
-    *reinterpret_cast<uint4 *>(sA + (size_t) r * SROW + c8 * 8) = v;
+    if (p >= 0 && p < LP) v = *reinterpret_cast<const uint4 *>(inw + (size_t) p * CH + c * 8);
+    *reinterpret_cast<uint4 *>(sA + ((size_t) c * rows + r) * 16) = v;
   }
-  float acc[2][8][4];
-#pragma unroll
-  for (int a = 0; a < 2; a++)
-#pragma unroll
-    for (int n = 0; n < 8; n++)
-#pragma unroll
-      for (int q = 0; q < 4; q++) acc[a][n][q] = 0.f;
-
-  for (int t = 0; t < KT; t++) {
-    __syncthreads();   // previous tap's B fully consumed (and, at t = 0, A staged)
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const unsigned taddr = *tslot;
+  // instruction descriptor: D f32, A/B bf16, both K-major, N = 128, M = 128
+  const unsigned idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned) (CH >> 3) << 17) | ((unsigned) (TILE >> 4) << 24);
+  bool ok = true;
+  for (int t = 0; t < KT && ok; t++) {
     const unsigned short *wtt = wt + (size_t) t * CH * CH;
-    for (int x = tid; x < CH * (CH / 8); x += blockDim.x) {
-      const int r = x / (CH / 8), c8 = x - r * (CH / 8);
-      *reinterpret_cast<uint4 *>(sB + (size_t) r * SROW + c8 * 8) = *reinterpret_cast<const uint4 *>(wtt + (size_t) r * CH + c8 * 8);
+    for (int x = tid; x < CH * 16; x += blockDim.x) {
+      const int co = x >> 4, c = x & 15;
+      *reinterpret_cast<uint4 *>(sB + ((size_t) c * CH + co) * 16) = *reinterpret_cast<const uint4 *>(wtt + (size_t) co * CH + c * 8);
     }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // generic-proxy stores -> tensor-core reads
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    const int rbase = t * dil;                 // staged row of tile row 0 for this tap
-#pragma unroll 2
-    for (int k0 = 0; k0 < CH; k0 += 16) {
-      unsigned af[2][4];
-#pragma unroll
-      for (int a = 0; a < 2; a++) {
-        const int r = rbase + 32 * wm + 16 * a + g;
-        const unsigned short *p = sA + (size_t) r * SROW + k0 + 2 * tg;
-        af[a][0] = *reinterpret_cast<const unsigned *>(p);
-        af[a][1] = *reinterpret_cast<const unsigned *>(p + 8 * SROW);
-        af[a][2] = *reinterpret_cast<const unsigned *>(p + 8);
-        af[a][3] = *reinterpret_cast<const unsigned *>(p + 8 * SROW + 8);
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      for (int kb = 0; kb < CH / 16; kb++) {
+        const unsigned long long ad = umma_desc(smem_u32(sA + ((size_t) (2 * kb) * rows + t * dil) * 16), rows * 16, 128);
+        const unsigned long long bd = umma_desc(smem_u32(sB + (size_t) (2 * kb) * CH * 16), CH * 16, 128);
+        const unsigned acc = (t > 0 || kb > 0) ? 1u : 0u;
+        asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
+                     :: "r"(taddr), "l"(ad), "l"(bd), "r"(idesc), "r"(acc) : "memory");
       }
-#pragma unroll
-      for (int n = 0; n < 8; n++) {
-        const unsigned short *p = sB + (size_t) (64 * wn + 8 * n + g) * SROW + k0 + 2 * tg;
-        unsigned bq[2];
-        bq[0] = *reinterpret_cast<const unsigned *>(p);
-        bq[1] = *reinterpret_cast<const unsigned *>(p + 8);
-        mma_bf16(acc[0][n], af[0], bq);
-        mma_bf16(acc[1][n], af[1], bq);
-      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(smem_u32(mbar)) : "memory");
     }
+    // the tap's MMAs must finish reading sB before it is overwritten
+    if (!mbar_wait_bounded(mbar, (unsigned) (t & 1))) { ok = false; if (tid == 0) atomicOr(err, 1); }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   }
-  // epilogue: bias, ReLU, BF16; rows at or beyond the window length are zero
+  // epilogue: warp w holds tile rows 32 w .. 32 w + 31 (TMEM lanes), 16 columns per load
   unsigned short *outw = out + (size_t) win * LP * CH;
+  const int row = tile * TILE + 32 * warp + lane;
+  for (int cb = 0; cb < CH / 16; cb++) {
+    unsigned r[16];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr + ((unsigned) (32 * warp) << 16) + (unsigned) (cb * 16)));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    unsigned pk[8];
 #pragma unroll
-  for (int a = 0; a < 2; a++)
-#pragma unroll
-    for (int n = 0; n < 8; n++) {
-      const int col = 64 * wn + 8 * n + 2 * tg;
-      const float b0 = bias[col], b1 = bias[col + 1];
-#pragma unroll
-      for (int h = 0; h < 2; h++) {
-        const int row = tile * TILE + 32 * wm + 16 * a + g + 8 * h;
-        float v0 = acc[a][n][2 * h] + b0, v1 = acc[a][n][2 * h + 1] + b1;
-        v0 = v0 > 0.f ? v0 : 0.f; v1 = v1 > 0.f ? v1 : 0.f;
-        if (row >= W2) v0 = v1 = 0.f;
-        const unsigned pk = (unsigned) f2bf(v0) | ((unsigned) f2bf(v1) << 16);
-        *reinterpret_cast<unsigned *>(outw + (size_t) row * CH + col) = pk;
-      }
+    for (int j = 0; j < 8; j++) {
+      const int co = cb * 16 + 2 * j;
+      float v0 = __uint_as_float(r[2 * j]) + bias[co], v1 = __uint_as_float(r[2 * j + 1]) + bias[co + 1];
+      v0 = v0 > 0.f ? v0 : 0.f; v1 = v1 > 0.f ? v1 : 0.f;
+      if (row >= W2 || !ok) v0 = v1 = 0.f;
+      pk[j] = (unsigned) f2bf(v0) | ((unsigned) f2bf(v1) << 16);
     }
+    uint4 *dst = reinterpret_cast<uint4 *>(outw + (size_t) row * CH + cb * 16);
+    dst[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    dst[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(taddr), "r"(128) : "memory");
 }
 
 // Read-out: max over the window's positions per channel, then the linear layer.
@@ -215,8 +239,10 @@ extern "C" int cmgb_filter_create(cmgb_ctx *ctx, int W, const float *w0, const u
   FCUDA(cudaMemcpy(f->d_w, w, sizeof(unsigned short) * 5 * KT * CH * CH, cudaMemcpyHostToDevice));
   FCUDA(cudaMemcpy(f->d_b, bias, sizeof(float) * NL * CH, cudaMemcpyHostToDevice));
   FCUDA(cudaMemcpy(f->d_out, wout, sizeof(float) * (CH + 1), cudaMemcpyHostToDevice));
-  int maxsm = (TILE + 8 * DIL[NL - 1]) * SROW * 2 + CH * SROW * 2;
-  FCUDA(cudaFuncSetAttribute(filter_conv, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm));
+  FCUDA(cudaMalloc(&f->d_err, sizeof(int)));
+  FCUDA(cudaMemset(f->d_err, 0, sizeof(int)));
+  const int maxsm = 16 * (TILE + 8 * DIL[NL - 1]) * 16 + 16 * CH * 16 + 64;
+  FCUDA(cudaFuncSetAttribute(filter_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm));
   *ret = f.release();
   return CMGB_OK;
 #endif
@@ -227,7 +253,7 @@ extern "C" void cmgb_filter_destroy(cmgb_filter *f)
   if (!f) return;
 #ifndef CMGB_HOST_EMULATION
   cudaFree(f->d_w0); cudaFree(f->d_w); cudaFree(f->d_b); cudaFree(f->d_out);
-  cudaFree(f->d_act[0]); cudaFree(f->d_act[1]); cudaFree(f->d_logit);
+  cudaFree(f->d_act[0]); cudaFree(f->d_act[1]); cudaFree(f->d_logit); cudaFree(f->d_err);
 #endif
   delete f;
 }
@@ -267,9 +293,9 @@ extern "C" int cmgb_filter_windows(cmgb_ctx *ctx, cmgb_filter *f, const uint8_t 
   int cur = 0;
   for (int l = 1; l < NL; l++) {
     const int d = DIL[l];
-    const size_t sm = (size_t) (TILE + 8 * d) * SROW * 2 + (size_t) CH * SROW * 2;
-    filter_conv<<<dim3(f->LP / TILE, nwin), 256, sm>>>(f->d_act[cur], f->d_act[cur ^ 1], f->LP, (int) (2 * W), d,
-                                                       f->d_w + (size_t) (l - 1) * KT * CH * CH, f->d_b + l * CH);
+    const size_t sm = (size_t) 16 * (TILE + 8 * d) * 16 + (size_t) 16 * CH * 16 + 64;
+    filter_conv_tc<<<dim3(f->LP / TILE, nwin), 128, sm>>>(f->d_act[cur], f->d_act[cur ^ 1], f->LP, (int) (2 * W), d,
+                                                          f->d_w + (size_t) (l - 1) * KT * CH * CH, f->d_b + l * CH, f->d_err);
     FCUDA(cudaGetLastError());
     cur ^= 1;
   }
@@ -277,6 +303,9 @@ extern "C" int cmgb_filter_windows(cmgb_ctx *ctx, cmgb_filter *f, const uint8_t 
   FCUDA(cudaGetLastError());
   FCUDA(cudaEventRecord(e1));
   FCUDA(cudaMemcpy(ret_logits, f->d_logit, sizeof(float) * nwin, cudaMemcpyDeviceToHost));
+  int herr = 0;
+  FCUDA(cudaMemcpy(&herr, f->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (herr) FERR(CMGB_ENODEV, "filter: a bounded tensor-core wait ran out");
   float ms = 0.f;
   FCUDA(cudaEventElapsedTime(&ms, e0, e1));
   cudaEventDestroy(e0); cudaEventDestroy(e1);
