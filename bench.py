@@ -25,6 +25,14 @@ CM-emitted sequences cut at a random 5' and/or 3' point, the rest iid ACGU at
 (cmgb_ScanBatch, one launch per pass), and reads with a CYK survivor rescanned
 by RefITrInsideScan (QDB2) for that pass.  Residues count once per pass.
 
+`--workload multi` runs the uneven multi-model batch: a panel of the
+reference's calibrated CMs (clen 71-307; --cm-slots repeats them up to a
+larger count) against --seqs sequences per step (log-uniform 100-5,000 nt,
+45% GC, 5% carrying an emitted hit, both strands), every (CM, sequence) pair
+by FastCYKScan QDB1 in one multi-model persistent launch (cmgb_ScanMulti),
+timed beside one cmgb_ScanBatch launch per CM over the same sequences.
+Residues count once per (CM, sequence) pair.
+
 `--impl reference` times the reference's scanner on the host cores instead:
 the reference's own FastCYKScan/FastIInsideScan compiled from source
 (oracle/_ref) where that library exists, otherwise the C restatement of them
@@ -316,6 +324,125 @@ def run_learned(args, rank, world):
         "clocks": clocks,
     }
     filt.close(); sc.close()
+    return out
+
+
+PANEL = ["tRNA", "Vault", "Plant_SRP", "tRNA1415G", "snR75", "tRNA-Sec", "srp-euk", "rnaseP-eubact",
+         "5S_rRNA", "Cobalamin", "tRNA5", "tRNA5-hand"]
+
+
+def load_panel():
+    from infernal_gb300 import cmfile
+    out = []
+    for n in PANEL:
+        p = os.path.join(ROOT, "tests", "golden", f"{n}.model.npz")
+        if not os.path.exists(p):
+            p = os.path.join(ROOT, "tests", "golden", "panel", f"{n}.model.npz")
+        out.append(cmfile.load_npz(p))
+    return out
+
+
+def make_multi_seqs(models, step, nseq, seed=20261205):
+    """Sequences of the uneven multi-model workload: lengths log-uniform
+    100-5,000 nt, iid at 45% GC, 5% carrying an emitted hit of a random
+    panel model; returned with their reverse complements (both strands)."""
+    from infernal_gb300 import cmfile, emit
+    rng = np.random.default_rng([seed, step])
+    p = [0.275, 0.225, 0.225, 0.275]
+    top = []
+    for k in range(nseq):
+        n = int(np.exp(rng.uniform(np.log(100), np.log(5000))))
+        seq = "".join(rng.choice(list("ACGU"), n, p=p))
+        if rng.random() < 0.05:
+            h = emit.sample(models[int(rng.integers(len(models)))], rng)
+            pos = int(rng.integers(0, max(1, n - len(h))))
+            seq = (seq[:pos] + h + seq[pos + len(h):])[:max(n, len(h))]
+        top.append(cmfile.digitize(seq))
+    return top + [emit.revcomp_dsq(d) for d in top]
+
+
+def run_multi(args, rank, world):
+    """Uneven multi-model batch: every panel model x every sequence (both
+    strands) by CYK QDB1 in one multi-model persistent launch per step,
+    against one cmgb_ScanBatch launch per model over the same sequences."""
+    import ctypes
+    import torch
+    from infernal_gb300 import cmfile, lib as L
+    torch.cuda.set_device(0)
+    sc = L.Scanner(0)
+    models = load_panel()
+    nslots = args.cm_slots or len(models)
+    slots = [models[k % len(models)] for k in range(nslots)]
+    nsteps = args.warmup + args.steps
+    inputs = [make_multi_seqs(models, s, args.seqs) for s in range(nsteps)]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    tuned = {n: sc.autotune(m, 1, "cyk") for n, m in zip(PANEL, models)}
+    keep = []
+    descs = [cmfile.make_desc(m, keep=keep) for m in models]
+    cut = [CYK_CUT] * nslots
+
+    def work(seqs):
+        res = sum(len(d) - 2 for d in seqs) * nslots
+        cells = 0
+        for k in range(nslots):
+            dk = descs[k % len(models)]
+            cells += sum(sc.lib.cmgb_count_cells(ctypes.byref(dk), 1, len(d) - 2) for d in seqs)
+        return res, cells
+
+    for s in range(args.warmup):
+        sc.scan_multi(slots, inputs[s], algo="cyk", qdbidx=1, cutoffs=cut, env_cutoff=CYK_CUT)
+    clk = start_clock_sampler(rank)
+    tot = kms = 0.0
+    res = cells = launches = nh = 0
+    h2d = d2h = 0
+    for s in range(args.warmup, nsteps):
+        flush.fill_(float(s))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rs = sc.scan_multi(slots, inputs[s], algo="cyk", qdbidx=1, cutoffs=cut, env_cutoff=CYK_CUT)
+        tot += time.perf_counter() - t0
+        kms += rs[0].kernel_ms
+        launches += sc.last_launches()
+        h2d, d2h = sc.last_transfer_bytes()
+        nh += sum(len(r.hits) for r in rs)
+        r_, c_ = work(inputs[s]); res += r_; cells += c_
+    clocks = stop_clock_sampler(clk)
+    # the same jobs as one batched launch per model
+    t_per = kms_per = 0.0
+    for s in range(args.warmup, nsteps):
+        flush.fill_(float(s))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for m in slots:
+            r = sc.scan_batch(m, inputs[s], algo="cyk", qdbidx=1, cutoff=CYK_CUT, env_cutoff=CYK_CUT)
+            kms_per += r[0].kernel_ms
+        t_per += time.perf_counter() - t0
+    value = res / (kms / 1e3) / 1e6
+    nlen = [len(d) - 2 for d in inputs[args.warmup]]
+    out = {
+        "metric": "Mres/s scanned (model x residue pairs, both strands), multi-model batched QDB-CYK in one persistent launch",
+        "value": round(value, 3), "unit": "Mres/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(kms / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{nslots} CM slots over a {len(models)}-CM panel of the reference's calibrated CMs "
+                               f"(clen 71-307), {args.seqs} sequences x 2 strands per step, length log-uniform "
+                               f"100-5000 (mean {np.mean(nlen):.0f}), GC 0.45, 5% with an emitted hit; "
+                               f"CYK QDB1 cutoff {CYK_CUT} bits, NULL3, greedy; autotuned shapes per CM",
+                   "model_residues_per_step": res // args.steps, "l2": "flushed between timed steps (256 MB write)",
+                   "parallelism": "1 GPU"},
+        "gcups": round(cells / (kms / 1e3) / 1e9, 2),
+        "e2e": {"value": round(res / tot / 1e6, 3), "unit": "Mres/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "per_model_batches": {"value": round(res / (kms_per / 1e3) / 1e6, 3), "unit": "Mres/s",
+                              "wall_mres_s": round(res / t_per / 1e6, 3), "launches_per_step": nslots,
+                              "note": "one cmgb_ScanBatch launch per CM over the same sequences"},
+        "speedup_vs_per_model": round(kms_per / kms, 3) if kms > 0 else None,
+        "gpu_launches": launches,
+        "hits_per_step": nh / args.steps,
+        "tuned_shapes": {k: {"tile_rows": v[0], "arena": "global" if v[1] == 2 else "shared"} for k, v in tuned.items()},
+        "clocks": clocks,
+    }
+    sc.close()
     return out
 
 
@@ -633,9 +760,12 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="plain", choices=["plain", "trunc", "learned"],
+    ap.add_argument("--workload", default="plain", choices=["plain", "trunc", "learned", "multi"],
                     help="plain: the single-large-CM scan (default); trunc: the truncated-mode read batch; "
-                         "learned: the pre-filtered pipeline against the plain scan")
+                         "learned: the pre-filtered pipeline against the plain scan; multi: the uneven "
+                         "multi-model batch")
+    ap.add_argument("--seqs", type=int, default=300, help="sequences per step of the multi workload (x 2 strands)")
+    ap.add_argument("--cm-slots", type=int, default=0, help="CM slots of the multi workload (default: the panel)")
     ap.add_argument("--reads", type=int, default=5000, help="reads per step of the trunc workload")
     ap.add_argument("--hits-per-mb", type=float, default=2.0, help="embedded hits per Mb (learned workload)")
     args = ap.parse_args()
@@ -653,6 +783,8 @@ def main():
         out = run_trunc(args, rank, world)
     elif args.workload == "learned":
         out = run_learned(args, rank, world)
+    elif args.workload == "multi":
+        out = run_multi(args, rank, world)
     else:
         out = run_ours(args, rank, world)
     if rank == 0:

@@ -296,6 +296,29 @@ int cmgb_ScanBatch(cmgb_ctx *ctx, cmgb_model *model, char *errbuf, int algo, int
                    int nseq, float cutoff, cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
                    int64_t *ret_nhits, int64_t *ret_envi, int64_t *ret_envj, float *ret_sc, int *ret_mode);
 
+/* ---- multi-model batched scans ----
+ * Runs njobs (model, sequence) scans of several models in one persistent
+ * launch (one launch per tile placement when the models' plans mix shared-
+ * memory and global-memory arenas): what cmsearch / cmscan do when they
+ * loop over models and sequences (src/cmscan.c, src/cmsearch.c: one
+ * pli_dispatch_cm_search per model and window).  Job k scans sequence
+ * job_seq[k] (laid out as in cmgb_ScanBatch) with models[job_model[k]] and
+ * that model's cutoff cutoffs[job_model[k]]; (model, sequence) pairs must be
+ * distinct.  Long sequences are cut into windows as in cmgb_ScanBatch, and
+ * every window of every job enters one work queue, largest band area
+ * (model cells per residue x window rows) first.  algo is one of the
+ * standard scanners (CMGB_ALGO_CYK, _IINSIDE, _FINSIDE).  Each job's results
+ * equal those of cmgb_ScanBatch with that model over that sequence.
+ * Outputs per job (arrays of njobs, each may be NULL): ret_nhits (hits it
+ * added to hitlist, which receives job 0's hits, then job 1's, ..., local
+ * coordinates), ret_envi/ret_envj (local, -1 if none), ret_sc (best score).
+ * All models must belong to ctx. */
+int cmgb_ScanMulti(cmgb_ctx *ctx, cmgb_model *const *models, int nmodels, const float *cutoffs, char *errbuf,
+                   int algo, int qdbidx, const uint8_t *seqs, int64_t seqs_len, const int64_t *offsets,
+                   const int64_t *lengths, int nseq, const int *job_model, const int *job_seq, int njobs,
+                   cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
+                   int64_t *ret_nhits, int64_t *ret_envi, int64_t *ret_envj, float *ret_sc);
+
 /* ---- learned window pre-filter ----
  * No reference counterpart: a learned screen placed before the CYK stage.
  * Windows of 2W residues at stride W over [i0, j0] (window k starts at

@@ -31,7 +31,7 @@ using namespace cmgb;
 
 #ifdef CMGB_HOST_EMULATION
 static const int kDefaultThreads = CMGB_EMU_THREADS;
-template <int ALG, bool GL>
+template <int ALG, bool GL, bool MULTI = false>
 static void launch_qdb(int grid, int nt, size_t smem, cudaStream_t, const KParams &kp)
 {
   std::vector<std::vector<float>> sm(grid, std::vector<float>(smem / 4 + 16));
@@ -44,7 +44,7 @@ static void launch_qdb(int grid, int nt, size_t smem, cudaStream_t, const KParam
     for (int t = 0; t < nt; t++)
       th.emplace_back([&, b, t] {
         cmgb_emu_bar = bars[b]; cmgb_emu_warp = warps[b * (nt / 32) + t / 32]; cmgb_emu_lane = t & 31;
-        qdb_scan_body<ALG, GL>(kp, sm[b].data(), t, nt, b);
+        qdb_scan_body<ALG, GL, MULTI>(kp, sm[b].data(), t, nt, b);
       });
   for (auto &x : th) x.join();
   for (auto *b : bars) delete b;
@@ -83,44 +83,56 @@ static cudaError_t prepare_tr(int nt, int smem, int *blocks_per_sm)
   if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, tr_scan_kernel<ALG, GL>, nt, smem);
 }
-template <int ALG, bool GL>
+template <int ALG, bool GL, bool MULTI = false>
 static void launch_qdb(int grid, int nt, size_t smem, cudaStream_t s, const KParams &kp)
 {
-  qdb_scan_kernel<ALG, GL><<<grid, nt, smem, s>>>(kp);
+  qdb_scan_kernel<ALG, GL, MULTI><<<grid, nt, smem, s>>>(kp);
 }
-template <int ALG, bool GL>
+template <int ALG, bool GL, bool MULTI = false>
 static cudaError_t prepare_qdb(int nt, int smem, int *blocks_per_sm)
 {
-  cudaError_t e = cudaFuncSetAttribute(qdb_scan_kernel<ALG, GL>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaError_t e = cudaFuncSetAttribute(qdb_scan_kernel<ALG, GL, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, qdb_scan_kernel<ALG, GL>, nt, smem);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, qdb_scan_kernel<ALG, GL, MULTI>, nt, smem);
 }
 #endif
 static const int kCandCap = 1 << 22;
 
-// Runtime dispatch over (algorithm, tile placement) to the kernel instantiations.
+// Runtime dispatch over (algorithm, tile placement, multi-model) to the kernel instantiations.
 #ifndef CMGB_HOST_EMULATION
-static cudaError_t prepare_any(int alg, bool gl, int nt, int smem, int *nb)
+static cudaError_t prepare_any(int alg, bool gl, int nt, int smem, int *nb, bool multi = false)
 {
-  switch (alg * 2 + (gl ? 1 : 0)) {
-  case 0: return prepare_qdb<0, false>(nt, smem, nb);
-  case 1: return prepare_qdb<0, true>(nt, smem, nb);
-  case 2: return prepare_qdb<1, false>(nt, smem, nb);
-  case 3: return prepare_qdb<1, true>(nt, smem, nb);
-  case 4: return prepare_qdb<2, false>(nt, smem, nb);
-  default: return prepare_qdb<2, true>(nt, smem, nb);
+  switch (alg * 4 + (gl ? 2 : 0) + (multi ? 1 : 0)) {
+  case 0: return prepare_qdb<0, false, false>(nt, smem, nb);
+  case 1: return prepare_qdb<0, false, true>(nt, smem, nb);
+  case 2: return prepare_qdb<0, true, false>(nt, smem, nb);
+  case 3: return prepare_qdb<0, true, true>(nt, smem, nb);
+  case 4: return prepare_qdb<1, false, false>(nt, smem, nb);
+  case 5: return prepare_qdb<1, false, true>(nt, smem, nb);
+  case 6: return prepare_qdb<1, true, false>(nt, smem, nb);
+  case 7: return prepare_qdb<1, true, true>(nt, smem, nb);
+  case 8: return prepare_qdb<2, false, false>(nt, smem, nb);
+  case 9: return prepare_qdb<2, false, true>(nt, smem, nb);
+  case 10: return prepare_qdb<2, true, false>(nt, smem, nb);
+  default: return prepare_qdb<2, true, true>(nt, smem, nb);
   }
 }
 #endif
-static void launch_any(int alg, bool gl, int grid, int nt, size_t smem, cudaStream_t s, const KParams &kp)
+static void launch_any(int alg, bool gl, int grid, int nt, size_t smem, cudaStream_t s, const KParams &kp, bool multi = false)
 {
-  switch (alg * 2 + (gl ? 1 : 0)) {
-  case 0: launch_qdb<0, false>(grid, nt, smem, s, kp); break;
-  case 1: launch_qdb<0, true>(grid, nt, smem, s, kp); break;
-  case 2: launch_qdb<1, false>(grid, nt, smem, s, kp); break;
-  case 3: launch_qdb<1, true>(grid, nt, smem, s, kp); break;
-  case 4: launch_qdb<2, false>(grid, nt, smem, s, kp); break;
-  default: launch_qdb<2, true>(grid, nt, smem, s, kp); break;
+  switch (alg * 4 + (gl ? 2 : 0) + (multi ? 1 : 0)) {
+  case 0: launch_qdb<0, false, false>(grid, nt, smem, s, kp); break;
+  case 1: launch_qdb<0, false, true>(grid, nt, smem, s, kp); break;
+  case 2: launch_qdb<0, true, false>(grid, nt, smem, s, kp); break;
+  case 3: launch_qdb<0, true, true>(grid, nt, smem, s, kp); break;
+  case 4: launch_qdb<1, false, false>(grid, nt, smem, s, kp); break;
+  case 5: launch_qdb<1, false, true>(grid, nt, smem, s, kp); break;
+  case 6: launch_qdb<1, true, false>(grid, nt, smem, s, kp); break;
+  case 7: launch_qdb<1, true, true>(grid, nt, smem, s, kp); break;
+  case 8: launch_qdb<2, false, false>(grid, nt, smem, s, kp); break;
+  case 9: launch_qdb<2, false, true>(grid, nt, smem, s, kp); break;
+  case 10: launch_qdb<2, true, false>(grid, nt, smem, s, kp); break;
+  default: launch_qdb<2, true, true>(grid, nt, smem, s, kp); break;
   }
 }
 
@@ -1163,6 +1175,249 @@ extern "C" int cmgb_ScanBatch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo
       for (size_t k = (size_t) before; k < hitlist->h.size(); k++) { hitlist->h[k].start -= off; hitlist->h[k].stop -= off; }
     }
     if (ret_nhits) ret_nhits[q] = hitlist ? (int64_t) hitlist->h.size() - before : 0;
+  }
+  return CMGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Multi-model batched scans: the windows of every (model, sequence) job in
+// one work queue, one persistent launch per tile placement.
+extern "C" int cmgb_ScanMulti(cmgb_ctx *c, cmgb_model *const *models, int nmodels, const float *cutoffs, char *errbuf,
+                              int algo, int qdbidx, const uint8_t *seqs, int64_t seqs_len, const int64_t *offsets,
+                              const int64_t *lengths, int nseq, const int *job_model, const int *job_seq, int njobs,
+                              cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
+                              int64_t *ret_nhits, int64_t *ret_envi, int64_t *ret_envj, float *ret_sc)
+{
+  static const char *fn = "ScanMulti";
+  if (!c || !models || nmodels < 1 || !cutoffs) ERRF(CMGB_EINVAL, "%s, NULL context, models or cutoffs", fn);
+  if (algo < CMGB_ALGO_CYK || algo > CMGB_ALGO_FINSIDE) ERRF(CMGB_EINVAL, "%s, algorithm %d is not a standard scanner", fn, algo);
+  if (qdbidx < 0 || qdbidx > 2) ERRF(CMGB_EINCOMPAT, "%s, qdbidx is invalid", fn);
+  if (!seqs || !offsets || !lengths || nseq < 1 || !job_model || !job_seq || njobs < 1) ERRF(CMGB_EINCOMPAT, "%s, no jobs", fn);
+  for (int k = 0; k < nmodels; k++)
+    if (!models[k] || models[k]->ctx != c) ERRF(CMGB_EINCOMPAT, "%s, model %d is NULL or belongs to another context", fn, k);
+  for (int q = 0; q < nseq; q++)
+    if (!(lengths[q] >= 1 && offsets[q] >= 0 && offsets[q] + lengths[q] + 1 <= seqs_len - 1))
+      ERRF(CMGB_EINCOMPAT, "%s, sequence %d lies outside the buffer", fn, q);
+  std::vector<int64_t> keys((size_t) njobs);
+  for (int k = 0; k < njobs; k++) {
+    if (job_model[k] < 0 || job_model[k] >= nmodels || job_seq[k] < 0 || job_seq[k] >= nseq)
+      ERRF(CMGB_EINCOMPAT, "%s, job %d names model %d / sequence %d out of range", fn, k, job_model[k], job_seq[k]);
+    keys[k] = (int64_t) job_model[k] * nseq + job_seq[k];
+  }
+  std::vector<int> by_key((size_t) njobs);
+  for (int k = 0; k < njobs; k++) by_key[k] = k;
+  std::sort(by_key.begin(), by_key.end(), [&](int a, int b) { return keys[a] < keys[b]; });
+  for (int k = 1; k < njobs; k++)
+    if (keys[by_key[k]] == keys[by_key[k - 1]]) ERRF(CMGB_EINCOMPAT, "%s, jobs %d and %d repeat a (model, sequence) pair", fn, by_key[k - 1], by_key[k]);
+  auto job_of = [&](int mi, int q) {   // job index of (model, sequence)
+    const int64_t key = (int64_t) mi * nseq + q;
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) { const int mid = (lo + hi) / 2; if (keys[by_key[mid]] < key) lo = mid + 1; else hi = mid; }
+    return keys[by_key[lo]] == key ? by_key[lo] : -1;
+  };
+  const int alg = algo;
+  int st;
+  CUDA_TRY(cudaSetDevice(c->device));
+  std::vector<DevPlan *> plan((size_t) nmodels, nullptr);
+  std::vector<double> rate((size_t) nmodels, 0.0);   // cells per residue of a full-length row
+  std::vector<char> used((size_t) nmodels, 0);
+  for (int k = 0; k < njobs; k++) used[job_model[k]] = 1;
+  for (int mi = 0; mi < nmodels; mi++) {
+    if (!used[mi]) continue;
+    if ((st = get_plan(models[mi], qdbidx, alg, &plan[mi], errbuf)) != CMGB_OK) return st;
+    const cmgb_model_desc *d = &models[mi]->desc;
+    rate[mi] = (double) (cmgb_count_cells(d, qdbidx, d->W) - cmgb_count_cells(d, qdbidx, d->W - 1));
+  }
+
+  // windows of every job (as cmgb_ScanBatch cuts a sequence), with their cost
+  struct Win { int job; long long s, e, s0; double cost; };
+  std::vector<Win> all;
+  for (int k = 0; k < njobs; k++) {
+    const int mi = job_model[k], q = job_seq[k];
+    const int Wm = models[mi]->W;
+    const int64_t wlen = std::max<int64_t>(8LL * Wm, 2048);
+    const int64_t a = offsets[q] + 1, b = offsets[q] + lengths[q];
+    for (int64_t s0w = a; s0w <= b; s0w += wlen) {
+      Win x; x.job = k; x.s = s0w; x.e = std::min<int64_t>(b, s0w + wlen - 1);
+      x.s0 = s0w == a ? a : std::max<int64_t>(a, s0w - (Wm - 1));
+      x.cost = rate[mi] * (double) (x.e - x.s0 + 1);
+      all.push_back(x);
+    }
+  }
+  if (all.size() > (size_t) (1 << 24)) ERRF(CMGB_ERANGE, "%s, too many windows", fn);
+
+  std::vector<std::vector<CandHost>> per((size_t) njobs);
+  std::vector<int64_t> envi((size_t) njobs), envj((size_t) njobs);
+  std::vector<unsigned> bestj((size_t) njobs, 0u);
+  for (int k = 0; k < njobs; k++) { const int q = job_seq[k]; envi[k] = offsets[q] + lengths[q] + 1; envj[k] = offsets[q]; }
+  float total_ms = 0.f;
+  int launches = 0;
+  int64_t h2d = 0, d2h = 0;
+  const float ecut = (ret_envi || ret_envj) ? env_cutoff : 3.0e38f;
+
+  for (int glp = 0; glp < 2; glp++) {   // one launch per tile placement (shared, then global arena)
+    std::vector<Win> wv;
+    for (const Win &x : all) if ((plan[job_model[x.job]]->plan.arena_global != 0) == (glp == 1)) wv.push_back(x);
+    if (wv.empty()) continue;
+    std::stable_sort(wv.begin(), wv.end(), [](const Win &a, const Win &b) { return a.cost > b.cost; });
+    const int nw = (int) wv.size();
+    const bool gl = glp == 1;
+    // the common per-CTA strides of this launch: largest over its models
+    int max_elems = 0, max_carry = 0, max_ring = 0, max_arena = 0, smem = 0;
+    std::vector<int> gmodels;
+    for (int mi = 0; mi < nmodels; mi++) {
+      if (!plan[mi] || (plan[mi]->plan.arena_global != 0) != gl) continue;
+      bool has = false;
+      for (const Win &x : wv) if (job_model[x.job] == mi) { has = true; break; }
+      if (!has) continue;
+      const ScanPlan &P = plan[mi]->plan;
+      gmodels.push_back(mi);
+      max_elems = std::max(max_elems, P.smem_elems); max_carry = std::max(max_carry, P.carry_elems);
+      max_ring = std::max(max_ring, P.ring_elems); max_arena = std::max(max_arena, P.arena_elems);
+    }
+    smem = max_elems * 4 + 32;
+    if (smem + 64 > c->max_smem_optin) ERRF(CMGB_ERANGE, "%s, %d bytes of shared memory per CTA exceed the device", fn, smem);
+
+    auto al = [](size_t x) { return (x + 255) & ~(size_t) 255; };
+    const size_t o_ws = al((size_t) seqs_len), o_we = o_ws + al(sizeof(long long) * nw), o_ws0 = o_we + al(sizeof(long long) * nw);
+    const size_t o_cm = o_ws0 + al(sizeof(long long) * nw), o_kp = o_cm + al(sizeof(int) * nw);
+    const size_t o_out = o_kp + al(sizeof(KParams) * (size_t) nmodels);
+    const size_t out_bytes = sizeof(long long) * 2 * nw + sizeof(unsigned) * nw;
+    if ((st = grow((void **) &c->d_dsq, &c->dsq_bytes, o_out + al(out_bytes), errbuf)) != CMGB_OK) return st;
+    unsigned char *blk = c->d_dsq;
+    std::vector<long long> ws(nw), we(nw), ws0(nw);
+    std::vector<int> icm(nw);
+    for (int w = 0; w < nw; w++) { ws[w] = wv[w].s; we[w] = wv[w].e; ws0[w] = wv[w].s0; icm[w] = job_model[wv[w].job]; }
+    std::vector<unsigned char> out_init(out_bytes, 0);
+    {
+      long long *env = reinterpret_cast<long long *>(out_init.data());
+      for (int w = 0; w < nw; w++) { env[2 * w] = LLONG_MAX; env[2 * w + 1] = -1; }
+    }
+    int cps = c->ctas_per_sm;
+    if (cps == 0) {
+#ifndef CMGB_HOST_EMULATION
+      int nb = 1;
+      CUDA_TRY(prepare_any(alg, gl, c->threads, smem, &nb, true));
+      cps = nb < 1 ? 1 : nb;
+#else
+      cps = 1;
+#endif
+    }
+    const int grid = std::min(nw, c->nsm * cps);
+    if ((st = grow((void **) &c->d_carry, &c->carry_bytes, sizeof(float) * 2 * (size_t) max_carry * grid, errbuf)) != CMGB_OK) return st;
+    if ((st = grow((void **) &c->d_ring, &c->ring_bytes, sizeof(float) * (size_t) max_ring * grid, errbuf)) != CMGB_OK) return st;
+    if (gl && (st = grow((void **) &c->d_arena, &c->arena_bytes, sizeof(float) * (size_t) max_arena * grid, errbuf)) != CMGB_OK) return st;
+    if (c->cand_cap == 0) {
+      if (cudaMalloc(&c->d_cand, sizeof(Cand) * (size_t) kCandCap) != cudaSuccess) ERRF(CMGB_EMEM, "%s, out of device memory for candidates", fn);
+      c->cand_cap = kCandCap;
+    }
+    Control *h = c->h_ctl;
+    std::vector<unsigned char> outv(out_bytes);
+    std::vector<KParams> kps((size_t) nmodels);
+    for (int attempt = 0;; attempt++) {   // a second launch only when the candidate buffer was too small
+      std::memset(kps.data(), 0, sizeof(KParams) * kps.size());
+      for (int mi : gmodels) {
+        cmgb_model *m = models[mi];
+        KParams &kp = kps[mi];
+        const bool greedy = !(m->flags & CMGB_NOTGREEDY);
+        kp.st = plan[mi]->d_states; kp.plan = plan[mi]->plan; kp.rec = plan[mi]->d_rec; kp.arena = c->d_arena;
+        kp.plan.smem_elems = max_elems; kp.plan.carry_elems = max_carry; kp.plan.ring_elems = max_ring; kp.plan.arena_elems = max_arena;
+        kp.oesc = m->d_oesc; kp.ioesc = m->d_ioesc; kp.ilog = c->d_ilog; kp.flog = c->d_flog;
+        kp.dsq = blk; kp.i0 = 1; kp.j0 = seqs_len - 2; kp.nwin = nw;
+        kp.queue = &c->d_ctl->queue; kp.carry = c->d_carry; kp.ring = c->d_ring;
+        kp.cand = c->d_cand; kp.ncand = &c->d_ctl->ncand; kp.cand_cap = c->cand_cap;
+        kp.cand_cut = hitlist ? cutoffs[mi] : 3.0e38f; kp.cand_pos = (hitlist && !greedy) ? 1 : 0; kp.env_cut = ecut;
+        kp.env = reinterpret_cast<long long *>(blk + o_out);
+        kp.best = reinterpret_cast<unsigned *>(blk + o_out + sizeof(long long) * 2 * nw);
+        kp.err = &c->d_ctl->err;
+        kp.win_s = reinterpret_cast<const long long *>(blk + o_ws); kp.win_e = reinterpret_cast<const long long *>(blk + o_we);
+        kp.win_s0 = reinterpret_cast<const long long *>(blk + o_ws0);
+        kp.cand_tag = mi;
+      }
+      // launch parameters: the first model of the launch supplies the queue,
+      // the window count and the common shared-memory layout
+      KParams k0 = kps[gmodels[0]];
+      k0.multi = reinterpret_cast<const KParams *>(blk + o_kp);
+      k0.item_cm = reinterpret_cast<const int *>(blk + o_cm);
+      std::memset(h, 0, sizeof(Control));
+      CUDA_TRY(cudaMemcpyAsync(blk, seqs, (size_t) seqs_len, cudaMemcpyHostToDevice, c->stream));
+      CUDA_TRY(cudaMemcpyAsync(blk + o_ws, ws.data(), sizeof(long long) * nw, cudaMemcpyHostToDevice, c->stream));
+      CUDA_TRY(cudaMemcpyAsync(blk + o_we, we.data(), sizeof(long long) * nw, cudaMemcpyHostToDevice, c->stream));
+      CUDA_TRY(cudaMemcpyAsync(blk + o_ws0, ws0.data(), sizeof(long long) * nw, cudaMemcpyHostToDevice, c->stream));
+      CUDA_TRY(cudaMemcpyAsync(blk + o_cm, icm.data(), sizeof(int) * nw, cudaMemcpyHostToDevice, c->stream));
+      CUDA_TRY(cudaMemcpyAsync(blk + o_kp, kps.data(), sizeof(KParams) * kps.size(), cudaMemcpyHostToDevice, c->stream));
+      CUDA_TRY(cudaMemcpyAsync(blk + o_out, out_init.data(), out_bytes, cudaMemcpyHostToDevice, c->stream));
+      CUDA_TRY(cudaMemcpyAsync(c->d_ctl, h, sizeof(Control), cudaMemcpyHostToDevice, c->stream));
+      h2d += seqs_len + (int64_t) (3 * sizeof(long long) * nw + sizeof(int) * nw + sizeof(KParams) * kps.size() + out_bytes + sizeof(Control));
+      CUDA_TRY(cudaEventRecord(c->ev0, c->stream));
+      launch_any(alg, gl, grid, c->threads, (size_t) smem, c->stream, k0, true);
+      CUDA_TRY(cudaGetLastError());
+      CUDA_TRY(cudaEventRecord(c->ev1, c->stream));
+      CUDA_TRY(cudaMemcpyAsync(h, c->d_ctl, sizeof(Control), cudaMemcpyDeviceToHost, c->stream));
+      CUDA_TRY(cudaMemcpyAsync(outv.data(), blk + o_out, out_bytes, cudaMemcpyDeviceToHost, c->stream));
+      CUDA_TRY(cudaStreamSynchronize(c->stream));
+      float ms = 0.f;
+      CUDA_TRY(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+      total_ms += ms;
+      launches++;
+      d2h += (int64_t) (sizeof(Control) + out_bytes);
+      if (h->err & 2) ERRF(CMGB_ENODEV, "%s, a bounded device wait ran out (phase record copy)", fn);
+      if (!(h->err & 1)) break;
+      if (attempt > 0) ERRF(CMGB_ERANGE, "%s, more than %d candidate root cells; raise the cutoffs", fn, c->cand_cap);
+      const int64_t need = (int64_t) h->ncand + h->ncand / 4;
+      if (need > kTrCandMax) ERRF(CMGB_ERANGE, "%s, more than %lld candidate root cells; raise the cutoffs", fn, (long long) kTrCandMax);
+      cudaFree(c->d_cand); c->d_cand = nullptr; c->cand_cap = 0;
+      if (cudaMalloc(&c->d_cand, sizeof(Cand) * (size_t) need) != cudaSuccess) ERRF(CMGB_EMEM, "%s, out of device memory for candidates", fn);
+      c->cand_cap = (int) need;
+    }
+    // candidates -> jobs: model from the tag, sequence from the position
+    const int n = h->ncand;
+    if (hitlist && n > 0) {
+      d2h += (int64_t) sizeof(Cand) * n;
+      std::vector<Cand> raw((size_t) n);
+      CUDA_TRY(cudaMemcpy(raw.data(), c->d_cand, sizeof(Cand) * (size_t) n, cudaMemcpyDeviceToHost));
+      std::vector<int> by_off(nseq);
+      for (int q = 0; q < nseq; q++) by_off[q] = q;
+      std::sort(by_off.begin(), by_off.end(), [&](int a, int b) { return offsets[a] < offsets[b]; });
+      for (int i = 0; i < n; i++) {
+        const Cand &cc = raw[i];
+        int lo = 0, hi = nseq - 1;   // last sequence whose offset is below j
+        while (lo < hi) { const int mid = (lo + hi + 1) / 2; if (offsets[by_off[mid]] < cc.j) lo = mid; else hi = mid - 1; }
+        const int k = job_of(cc.pad, by_off[lo]);
+        if (k < 0) ERRF(CMGB_EINCOMPAT, "%s, a candidate cell matches no job", fn);
+        CandHost x; x.j = cc.j; x.d = cc.d; x.sc = cc.sc; x.r = cc.r; x.mode = CMGB_TRMODE_J;
+        per[k].push_back(x);
+      }
+    }
+    const long long *env = reinterpret_cast<const long long *>(outv.data());
+    const unsigned *best = reinterpret_cast<const unsigned *>(outv.data() + sizeof(long long) * 2 * nw);
+    for (int w = 0; w < nw; w++) {
+      const int k = wv[w].job;
+      if (env[2 * w + 1] >= 0) { envi[k] = std::min<int64_t>(envi[k], env[2 * w]); envj[k] = std::max<int64_t>(envj[k], env[2 * w + 1]); }
+      bestj[k] = std::max(bestj[k], best[w]);
+    }
+  }
+  c->last_ms = total_ms;
+  c->last_launches = launches;
+  c->last_h2d = h2d; c->last_d2h = d2h;
+  auto u2f = [](unsigned u) { if (u == 0) return CMGB_IMPOSSIBLE; unsigned b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u; float f; std::memcpy(&f, &b, 4); return f; };
+  for (int k = 0; k < njobs; k++) {
+    const int q = job_seq[k];
+    cmgb_model *m = models[job_model[k]];
+    const int64_t off = offsets[q];
+    if (ret_sc) ret_sc[k] = u2f(bestj[k]);
+    if (ret_envi) ret_envi[k] = envj[k] < off + 1 ? -1 : envi[k] - off;
+    if (ret_envj) ret_envj[k] = envj[k] < off + 1 ? -1 : envj[k] - off;
+    const int64_t before = hitlist ? (int64_t) hitlist->h.size() : 0;
+    if (hitlist && !per[k].empty()) {
+      ResolveArgs ra;
+      ra.null = m->null.data(); ra.K = m->K; ra.null3_omega = m->null3_omega; ra.do_null3 = do_null3;
+      ra.greedy = (m->flags & CMGB_NOTGREEDY) ? 0 : 1; ra.cutoff = cutoffs[job_model[k]];
+      ra.i0 = off + 1; ra.j0 = off + lengths[q]; ra.dsq = seqs;
+      resolve_hits(per[k], ra, hitlist->h);
+      for (size_t x = (size_t) before; x < hitlist->h.size(); x++) { hitlist->h[x].start -= off; hitlist->h[x].stop -= off; }
+    }
+    if (ret_nhits) ret_nhits[k] = hitlist ? (int64_t) hitlist->h.size() - before : 0;
   }
   return CMGB_OK;
 }

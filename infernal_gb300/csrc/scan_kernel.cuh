@@ -137,6 +137,12 @@ struct KParams {
   // win_s for a later window of a long sequence); env and best are then
   // per-window arrays
   const long long *win_s, *win_e, *win_s0;
+  // multi-model launches: window w belongs to model item_cm[w], whose
+  // parameters are multi[item_cm[w]]; cand_tag (the model index) is stored
+  // with each candidate cell
+  const KParams *multi;
+  const int *item_cm;
+  int cand_tag;
 };
 
 // Order-preserving float <-> uint mapping for atomicMax.
@@ -240,60 +246,72 @@ struct CellWalk {
   CMGB_DEV void next() { d += sdd; r += sr; if (d > hi) { d -= wp; r++; } }
 };
 
-template <int ALG, bool GL>
-CMGB_DEV void qdb_scan_body(const KParams &p, float *smf, int tid, int nt, int bid)
+template <int ALG, bool GL, bool MULTI>
+CMGB_DEV void qdb_scan_body(const KParams &p0, float *smf, int tid, int nt, int bid)
 {
   typedef Sr<ALG> R;
   typedef typename R::T T;
   constexpr bool INS = ALG == 1;
-  const ScanPlan &P = p.plan;
-  const int W = P.W, TT = P.T, NP = P.nphase;
   const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
-  // sm: base of the tile buffers, constant row, accumulator and insert scratch
-  // (shared memory, or this CTA's slice of the global arena when GL)
-  T *sm = GL ? reinterpret_cast<T *>(p.arena) + (size_t) bid * P.arena_elems : reinterpret_cast<T *>(smf);
-  T *acc = sm + P.acc_off;
-  int *bestr = reinterpret_cast<int *>(sm) + P.bestr_off;
-  T *tmp = sm + P.tmp_off;
-  unsigned char *res = reinterpret_cast<unsigned char *>(smf + P.res_off);
-  int *sdesc = reinterpret_cast<int *>(smf) + P.desc_off;
-  int *s_win = reinterpret_cast<int *>(smf) + P.smem_elems;   // one shared int past the plan's arena
-  T *carry0 = reinterpret_cast<T *>(p.carry) + (size_t) bid * 2 * P.carry_elems;
-  T *ringb = reinterpret_cast<T *>(p.ring) + (size_t) bid * P.ring_elems;
-  const unsigned short *tbl = ALG == 2 ? reinterpret_cast<const unsigned short *>(p.flog)
-                                        : reinterpret_cast<const unsigned short *>(smf + P.ltbl_off);
-  if (INS) {
-    unsigned short *t16 = reinterpret_cast<unsigned short *>(smf + P.ltbl_off);
-    for (int q = tid; q < CMGB_LTBL; q += nt) t16[q] = (unsigned short) CMGB_LDG(p.ilog + q);
-  }
-  const float el = P.el_selfsc;
-  const int iel = P.iel_selfsc;
-  const int accw = P.acc_w, rdn = P.root_dn, rdxW = P.root_dxW, RR = P.ring_rows, tstr = P.tmp_stride;
-  const bool want_vsc = p.vsc != nullptr;
-
+  // the work-queue slot and the two record barriers sit past the plan's arena
+  // (a multi-model launch gives every plan the largest smem_elems)
+  int *s_win = reinterpret_cast<int *>(smf) + p0.plan.smem_elems;
+  unsigned long long *mbar = reinterpret_cast<unsigned long long *>(reinterpret_cast<char *>(smf) + p0.plan.smem_elems * 4 + 16);
   // Phase records stream into two shared-memory slots by TMA, one phase
   // ahead: slot g&1 holds the record of the g-th phase this CTA runs.
-  unsigned long long *mbar = reinterpret_cast<unsigned long long *>(reinterpret_cast<char *>(smf) + P.smem_elems * 4 + 16);
-  const int slot_words = P.rec_max_bytes / 4;
-  unsigned use0 = 1, use1 = 0;   // completed waits per slot (parity source); slot 0 waited above
+  unsigned use0 = 0, use1 = 0;   // completed waits per slot (parity source)
   long long g = 0;               // phases run by this CTA
-  if (tid == 0) {
-    cmgb_mbar_init(mbar); cmgb_mbar_init(mbar + 1);
-    cmgb_tma_load(sdesc, p.rec, (unsigned) P.rec0_bytes, mbar);
-    if (!cmgb_mbar_wait(mbar, 0)) CMGB_ATOMIC_OR(p.err, 2);
-  }
-  for (int d = tid; d < P.const_row_len; d += nt) sm[P.const_row + d] = d == 0 ? (T) 0 : R::imp();
-  CMGB_SYNC();
+  if (tid == 0) { cmgb_mbar_init(mbar); cmgb_mbar_init(mbar + 1); }
 
   long long envi = 0x7fffffffffffffffLL, envj = -1;
   float best_root = CMGB_IMP;
+  int cur = -1;                  // model whose constants are staged
 
   for (;;) {
     CMGB_SYNC();
-    if (tid == 0) *s_win = CMGB_ATOMIC_ADD(p.queue, 1);
+    if (tid == 0) *s_win = CMGB_ATOMIC_ADD(p0.queue, 1);
     CMGB_SYNC();
     const int w = *s_win;
-    if (w >= p.nwin) break;
+    if (w >= p0.nwin) break;
+    const int cm = MULTI ? p0.item_cm[w] : 0;
+    const KParams &p = MULTI ? p0.multi[cm] : p0;
+    const ScanPlan &P = p.plan;
+    const int W = P.W, TT = P.T, NP = P.nphase, Kp = P.Kp;
+    // sm: base of the tile buffers, constant row, accumulator and insert scratch
+    // (shared memory, or this CTA's slice of the global arena when GL)
+    T *sm = GL ? reinterpret_cast<T *>(p.arena) + (size_t) bid * P.arena_elems : reinterpret_cast<T *>(smf);
+    T *acc = sm + P.acc_off;
+    int *bestr = reinterpret_cast<int *>(sm) + P.bestr_off;
+    T *tmp = sm + P.tmp_off;
+    unsigned char *res = reinterpret_cast<unsigned char *>(smf + P.res_off);
+    int *sdesc = reinterpret_cast<int *>(smf) + P.desc_off;
+    T *carry0 = reinterpret_cast<T *>(p.carry) + (size_t) bid * 2 * P.carry_elems;
+    T *ringb = reinterpret_cast<T *>(p.ring) + (size_t) bid * P.ring_elems;
+    const unsigned short *tbl = ALG == 2 ? reinterpret_cast<const unsigned short *>(p.flog)
+                                          : reinterpret_cast<const unsigned short *>(smf + P.ltbl_off);
+    const float el = P.el_selfsc;
+    const int iel = P.iel_selfsc;
+    const int accw = P.acc_w, rdn = P.root_dn, rdxW = P.root_dxW, RR = P.ring_rows, tstr = P.tmp_stride;
+    const bool want_vsc = p.vsc != nullptr;
+    const int slot_words = P.rec_max_bytes / 4;
+    if (cm != cur) {
+      // this model's constants: the ILogsum table, the constant E row and the
+      // record of phase 0 (later windows of the same model find it prefetched
+      // by their predecessor's last phase)
+      if (INS) {
+        unsigned short *t16 = reinterpret_cast<unsigned short *>(smf + P.ltbl_off);
+        for (int q = tid; q < CMGB_LTBL; q += nt) t16[q] = (unsigned short) CMGB_LDG(p.ilog + q);
+      }
+      for (int d = tid; d < P.const_row_len; d += nt) sm[P.const_row + d] = d == 0 ? (T) 0 : R::imp();
+      if (tid == 0) {
+        const int sl = (int) (g & 1);
+        cmgb_tma_load(sdesc + sl * slot_words, p.rec, (unsigned) P.rec0_bytes, mbar + sl);
+        if (!cmgb_mbar_wait(mbar + sl, sl ? (use1 & 1) : (use0 & 1))) CMGB_ATOMIC_OR(p.err, 2);
+        if (sl) use1++; else use0++;
+      }
+      CMGB_SYNC();
+      cur = cm;
+    }
     long long own_s, own_e, s0;
     if (p.win_s) { own_s = p.win_s[w]; own_e = p.win_e[w]; s0 = p.win_s0 ? p.win_s0[w] : own_s; }
     else {
@@ -330,7 +348,7 @@ CMGB_DEV void qdb_scan_body(const KParams &p, float *smf, int tid, int nt, int b
       for (int k = tid; k < P.res_len; k += nt) {
         const long long q = rbase + k;
         unsigned char x = (q >= 0 && q <= p.j0 + 1) ? p.dsq[q] : (unsigned char) 0;
-        res[k] = x < P.Kp ? x : (unsigned char) (P.Kp - 1);   // codes outside the alphabet read as missing data
+        res[k] = x < Kp ? x : (unsigned char) (Kp - 1);   // codes outside the alphabet read as missing data
       }
       for (int k = tid; k < TT * accw; k += nt) { acc[k] = R::acc_init(); bestr[k] = -1; }
       CMGB_SYNC();
@@ -384,7 +402,7 @@ CMGB_DEV void qdb_scan_body(const KParams &p, float *smf, int tid, int nt, int b
             }
             if (d >= 1 && CMGB_NOT_IMP(f) && (p.cand_pos ? (f > 0.0f) : (f >= p.cand_cut))) {
               const int sl = CMGB_ATOMIC_ADD(p.ncand, 1);
-              if (sl < p.cand_cap) { Cand cc; cc.j = j; cc.d = d; cc.sc = f; cc.r = br; cc.pad = 0; p.cand[sl] = cc; }
+              if (sl < p.cand_cap) { Cand cc; cc.j = j; cc.d = d; cc.sc = f; cc.r = br; cc.pad = p.cand_tag; p.cand[sl] = cc; }
               else CMGB_ATOMIC_OR(p.err, 1);
             }
           }
@@ -513,7 +531,7 @@ CMGB_DEV void qdb_scan_body(const KParams &p, float *smf, int tid, int nt, int b
                        sc = R::comb(sc, CH(2), tbl); sc = R::comb(sc, CH(1), tbl); sc = R::comb(sc, CH(0), tbl); break;
 #undef CH
               }
-              if (emit == 3)      sc = R::add(sc, esc[res[W + r - d] * P.Kp + res[W + r - 1]]);
+              if (emit == 3)      sc = R::add(sc, esc[res[W + r - d] * Kp + res[W + r - 1]]);
               else if (emit == 1) sc = R::add(sc, esc[res[W + r - d]]);
               else if (emit == 2) sc = R::add(sc, esc[res[W + r - 1]]);
               return sc;
@@ -607,7 +625,7 @@ CMGB_DEV void qdb_scan_body(const KParams &p, float *smf, int tid, int nt, int b
                          sc = R::comb(sc, CH(2), tbl); sc = R::comb(sc, CH(1), tbl); sc = R::comb(sc, CH(0), tbl); break;
 #undef CH
                 }
-                if (emit == 3)      sc = R::add(sc, esc[res[W + r - d] * P.Kp + res[W + r - 1]]);
+                if (emit == 3)      sc = R::add(sc, esc[res[W + r - d] * Kp + res[W + r - 1]]);
                 else if (emit == 1) sc = R::add(sc, esc[res[W + r - d]]);
                 else if (emit == 2) sc = R::add(sc, esc[res[W + r - 1]]);
                 val = sc;
@@ -643,15 +661,15 @@ CMGB_DEV void qdb_scan_body(const KParams &p, float *smf, int tid, int nt, int b
     }
   }
   // every record copy was waited for by thread 0 before the barrier that followed it
-  if (envj >= 0) { CMGB_ATOMIC_MINLL(p.env, envi); CMGB_ATOMIC_MAXLL(p.env + 1, envj); }
-  if (best_root > CMGB_IMP) CMGB_ATOMIC_MAXU(p.best, cmgb_f2u(best_root));
+  if (envj >= 0) { CMGB_ATOMIC_MINLL(p0.env, envi); CMGB_ATOMIC_MAXLL(p0.env + 1, envj); }
+  if (best_root > CMGB_IMP) CMGB_ATOMIC_MAXU(p0.best, cmgb_f2u(best_root));
 }
 
 #ifndef CMGB_HOST_EMULATION
-template <int ALG, bool GL>
+template <int ALG, bool GL, bool MULTI>
 __global__ void __launch_bounds__(512) qdb_scan_kernel(KParams p)
 {
   extern __shared__ __align__(128) float smem_dyn[];
-  qdb_scan_body<ALG, GL>(p, smem_dyn, threadIdx.x, blockDim.x, blockIdx.x);
+  qdb_scan_body<ALG, GL, MULTI>(p, smem_dyn, threadIdx.x, blockDim.x, blockIdx.x);
 }
 #endif

@@ -36,7 +36,7 @@ EXPORTS = [
     "cmgb_FastIInsideScan_dev", "cmgb_count_cells", "cmgb_autotune", "cmgb_FastCYKScan_noalloc",
     "cmgb_FastFInsideScan", "cmgb_FastFInsideScan_dev",
     "cmgb_RefTrCYKScan", "cmgb_RefITrInsideScan", "cmgb_RefTrCYKScan_dev", "cmgb_RefITrInsideScan_dev",
-    "cmgb_ScanBatch", "cmgb_filter_create", "cmgb_filter_destroy", "cmgb_filter_windows",
+    "cmgb_ScanBatch", "cmgb_ScanMulti", "cmgb_filter_create", "cmgb_filter_destroy", "cmgb_filter_windows",
 ]
 BATCH_ALGOS = {"cyk": 0, "inside": 1, "finside": 2, "trcyk": 3, "trinside": 4}
 
@@ -98,6 +98,8 @@ def bind(path: str) -> ctypes.CDLL:
         f.restype = I
     lib.cmgb_ScanBatch.argtypes = [P, P, ctypes.c_char_p, I, I, I, P, I64, P, P, I, F, P, I, F, P, P, P, P, P]
     lib.cmgb_ScanBatch.restype = I
+    lib.cmgb_ScanMulti.argtypes = [P, P, I, P, ctypes.c_char_p, I, I, P, I64, P, P, I, P, P, I, P, I, F, P, P, P, P]
+    lib.cmgb_ScanMulti.restype = I
     lib.cmgb_filter_create.argtypes = [P, I, P, P, P, P, ctypes.POINTER(P), ctypes.c_char_p]
     lib.cmgb_filter_create.restype = I
     lib.cmgb_filter_destroy.argtypes = [P]
@@ -291,6 +293,56 @@ class Scanner:
         out, k = [], 0
         for q in range(nseq):
             out.append(ScanResult(allhits[k: k + int(nh[q])], int(ei[q]), int(ej[q]), float(sc[q]), None, ms, int(mode[q])))
+            k += int(nh[q])
+        return out
+
+    def scan_multi(self, models, seqs, jobs=None, algo: str = "cyk", qdbidx: int = 1, cutoffs=None,
+                   do_null3: bool = True, env_cutoff: float = 0.0, want_hits: bool = True) -> List[ScanResult]:
+        """Runs cmgb_ScanMulti: every (model index, sequence index) pair of
+        jobs (default: all models x all sequences) in one persistent launch per
+        tile placement; returns one ScanResult per job, in job order."""
+        if algo not in ("cyk", "inside", "finside"):
+            raise ValueError("scan_multi runs the standard scanners only")
+        mhs = [self.model(m, 0) for m in models]
+        nm = len(models)
+        parts = [np.ascontiguousarray(x, dtype=np.uint8) for x in seqs]
+        lens = np.array([len(x) - 2 for x in parts], np.int64)
+        offs = np.zeros(len(parts), np.int64)
+        if len(parts) > 1:
+            offs[1:] = np.cumsum([len(x) for x in parts[:-1]])
+        buf = np.concatenate(parts + [np.full(1, cmfile.DSQ_SENTINEL, np.uint8)])
+        nseq = len(parts)
+        if jobs is None:
+            jobs = [(a, b) for a in range(nm) for b in range(nseq)]
+        jm = np.array([a for a, _ in jobs], np.int32)
+        js = np.array([b for _, b in jobs], np.int32)
+        nj = len(jobs)
+        cut = np.asarray(cutoffs if cutoffs is not None else [0.0] * nm, np.float32)
+        harr = (ctypes.c_void_p * nm)(*[h.value for h in mhs])
+        nh, ei, ej = np.zeros(nj, np.int64), np.zeros(nj, np.int64), np.zeros(nj, np.int64)
+        sc = np.zeros(nj, np.float32)
+        hl = self.lib.cmgb_hitlist_create() if want_hits else None
+        err = ctypes.create_string_buffer(256)
+        try:
+            st = self.lib.cmgb_ScanMulti(self._ctx, harr, nm, cut.ctypes.data, err, BATCH_ALGOS[algo], qdbidx,
+                                         buf.ctypes.data, len(buf), offs.ctypes.data, lens.ctypes.data, nseq,
+                                         jm.ctypes.data, js.ctypes.data, nj, hl, int(do_null3), env_cutoff,
+                                         nh.ctypes.data, ei.ctypes.data, ej.ctypes.data, sc.ctypes.data)
+            if st != 0:
+                raise ScanError(st, err.value.decode())
+            allhits = []
+            if hl:
+                h = Hit()
+                for k in range(self.lib.cmgb_hitlist_count(hl)):
+                    self.lib.cmgb_hitlist_get(hl, k, ctypes.byref(h))
+                    allhits.append((h.start, h.stop, h.root, h.mode, h.score))
+        finally:
+            if hl:
+                self.lib.cmgb_hitlist_destroy(hl)
+        ms = float(self.lib.cmgb_ctx_last_kernel_ms(self._ctx))
+        out, k = [], 0
+        for q in range(nj):
+            out.append(ScanResult(allhits[k: k + int(nh[q])], int(ei[q]), int(ej[q]), float(sc[q]), None, ms, 0))
             k += int(nh[q])
         return out
 

@@ -44,9 +44,10 @@ def test_table_inside_error_vs_fp64(models, name):
 @pytest.mark.parametrize("name", ["tRNA", "Vault", "Plant_SRP"])
 def test_gpu_inside_error_vs_fp64(models, name):
     m = models[name]
-    dsq = _case(m, name, 4)
+    dsq = _case(m, name, 5)      # seed 5: the FP64 scan reports at least one hit for every model
     n = len(dsq) - 2
     ref = oracle.scan(m, dsq, 1, n, algo="dinside", qdbidx=2, cutoff=0.0, env_cutoff=5.0)
+    assert len(ref[0]) >= 1
     s = L.Scanner(0)
     try:
         for algo, bound in (("inside", 0.1), ("finside", 0.01)):

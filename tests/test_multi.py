@@ -1,0 +1,103 @@
+"""Multi-model batched scans (cmgb_ScanMulti): every (model, sequence) job of
+one launch gets exactly the result cmgb_ScanBatch gives for that model over
+that sequence -- hits (local coordinates), envelope and best score.  The CPU
+tests run the kernel source in the host emulation on small cases; the GPU
+tests mix three models (shared-memory and global-memory plans) over sequences
+of uneven length."""
+import numpy as np
+import pytest
+
+from infernal_gb300 import cmfile, emit, lib as L
+
+
+def _seqs(models, rng, n, lo, hi, frac_hit=0.4):
+    out = []
+    for k in range(n):
+        L_ = int(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+        bg = "".join(rng.choice(list("ACGU"), L_))
+        if rng.random() < frac_hit:
+            s = emit.sample(models[int(rng.integers(len(models)))], rng)
+            pos = int(rng.integers(0, max(1, L_ - len(s))))
+            bg = (bg[:pos] + s + bg[pos + len(s):])[:max(L_, len(s))]
+        out.append(cmfile.digitize(bg))
+    return out
+
+
+def _check(sc, ms, seqs, jobs, algo, qdb, cutoffs):
+    rs = sc.scan_multi(ms, seqs, jobs=jobs, algo=algo, qdbidx=qdb, cutoffs=cutoffs, env_cutoff=2.0)
+    assert len(rs) == len(jobs)
+    want = {}
+    for mi, m in enumerate(ms):
+        qs = sorted({q for a, q in jobs if a == mi})
+        if not qs:
+            continue
+        bs = sc.scan_batch(m, [seqs[q] for q in qs], algo=algo, qdbidx=qdb, cutoff=cutoffs[mi], env_cutoff=2.0)
+        for q, b in zip(qs, bs):
+            want[(mi, q)] = b
+    nh = 0
+    for r, job in zip(rs, jobs):
+        b = want[job]
+        assert r.hits == b.hits, job
+        assert (r.envi, r.envj) == (b.envi, b.envj), job
+        assert np.float32(r.sc) == np.float32(b.sc), job
+        nh += len(r.hits)
+    return nh
+
+
+def test_multi_equals_batch_emulated(emu, models):
+    ms = [models["tRNA"], models["Vault"]]
+    rng = np.random.default_rng(31)
+    seqs = _seqs(ms, rng, 2, 80, 160)
+    jobs = [(a, q) for a in range(2) for q in range(2)]
+    _check(emu, ms, seqs, jobs, "cyk", 1, [0.0, 2.0])
+
+
+def test_multi_sparse_jobs_inside_emulated(emu, models):
+    ms = [models["tRNA"], models["Vault"]]
+    rng = np.random.default_rng(32)
+    seqs = _seqs(ms, rng, 3, 60, 120)
+    _check(emu, ms, seqs, [(1, 2), (0, 0)], "inside", 2, [0.0, 0.0])
+
+
+def test_multi_rejects_repeated_pairs(emu, models):
+    ms = [models["tRNA"]]
+    seqs = [cmfile.digitize("ACGU" * 30)]
+    with pytest.raises(L.ScanError):
+        emu.scan_multi(ms, seqs, jobs=[(0, 0), (0, 0)], algo="cyk", qdbidx=1)
+    with pytest.raises(ValueError):
+        emu.scan_multi(ms, seqs, algo="trcyk")
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    s = L.Scanner(0)
+    yield s
+    s.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("algo,qdb", [("cyk", 1), ("inside", 2), ("finside", 2)])
+def test_multi_equals_batch_gpu(gpu, models, algo, qdb):
+    ms = [models["tRNA"], models["Vault"], models["Plant_SRP"]]
+    rng = np.random.default_rng(hash(("multi", algo)) & 0xffff)
+    seqs = _seqs(ms, rng, 40, 100, 5000)
+    gpu.set_shape(0, 0, 0)
+    jobs = [(a, q) for a in range(3) for q in range(40)]
+    nh = _check(gpu, ms, seqs, jobs, algo, qdb, [0.0, 0.0, 0.0])
+    assert nh > 0
+    assert gpu.last_launches() >= 1
+    # a job subset in shuffled order
+    sub = [jobs[k] for k in rng.permutation(len(jobs))[:50]]
+    _check(gpu, ms, seqs, sub, algo, qdb, [3.0, 0.0, 5.0])
+
+
+@pytest.mark.gpu
+def test_multi_autotuned_shapes_gpu(gpu, models):
+    """Models tuned to different tile shapes and placements share a launch."""
+    ms = [models["tRNA"], models["Vault"], models["Plant_SRP"]]
+    for m in ms:
+        gpu.autotune(m, 1, "cyk", sample_len=60000)
+    rng = np.random.default_rng(77)
+    seqs = _seqs(ms, rng, 30, 200, 4000)
+    jobs = [(a, q) for a in range(3) for q in range(30)]
+    _check(gpu, ms, seqs, jobs, "cyk", 1, [0.0, 0.0, 0.0])
