@@ -519,8 +519,8 @@ CMGB_DEV void qdb_scan_body(const KParams &p0, float *smf, int tid, int nt, int 
             auto gval = [&](int r, int d) -> T {
               const int crow = r - rdo;
               T sc;
-              switch (cnum) {
 #define CH(o) R::add(sm[cb[o] + crow * cs[o] + d], tv[o])
+              switch (cnum) {
               case 2: sc = R::comb(CH(1), INIT(d - sd), tbl); sc = R::comb(sc, CH(0), tbl); break;
               case 3: sc = R::comb(CH(2), CH(1), tbl); sc = R::comb(sc, INIT(d - sd), tbl); sc = R::comb(sc, CH(0), tbl); break;
               case 4: sc = R::comb(CH(3), CH(2), tbl); sc = R::comb(sc, INIT(d - sd), tbl); sc = R::comb(sc, CH(1), tbl);
@@ -529,8 +529,8 @@ CMGB_DEV void qdb_scan_body(const KParams &p0, float *smf, int tid, int nt, int 
                       sc = R::comb(sc, CH(2), tbl); sc = R::comb(sc, CH(0), tbl); break;
               default: sc = R::comb(CH(5), INIT(d - sd), tbl); sc = R::comb(sc, CH(4), tbl); sc = R::comb(sc, CH(3), tbl);
                        sc = R::comb(sc, CH(2), tbl); sc = R::comb(sc, CH(1), tbl); sc = R::comb(sc, CH(0), tbl); break;
-#undef CH
               }
+#undef CH
               if (emit == 3)      sc = R::add(sc, esc[res[W + r - d] * Kp + res[W + r - 1]]);
               else if (emit == 1) sc = R::add(sc, esc[res[W + r - d]]);
               else if (emit == 2) sc = R::add(sc, esc[res[W + r - 1]]);
@@ -666,8 +666,11 @@ CMGB_DEV void qdb_scan_body(const KParams &p0, float *smf, int tid, int nt, int 
 }
 
 #ifndef CMGB_HOST_EMULATION
+// CYK fits 64 registers without spilling, so two 512-thread CTAs (or four of
+// 256) share an SM and hide each other's barrier and dependency stalls; the
+// Inside kernels keep 128 registers (they spill below that).
 template <int ALG, bool GL, bool MULTI>
-__global__ void __launch_bounds__(512) qdb_scan_kernel(KParams p)
+__global__ void __launch_bounds__(512, (ALG == 0 && !MULTI) ? 2 : 1) qdb_scan_kernel(KParams p)
 {
   extern __shared__ __align__(128) float smem_dyn[];
   qdb_scan_body<ALG, GL, MULTI>(p, smem_dyn, threadIdx.x, blockDim.x, blockIdx.x);
