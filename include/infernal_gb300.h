@@ -319,6 +319,31 @@ int cmgb_ScanMulti(cmgb_ctx *ctx, cmgb_model *const *models, int nmodels, const 
                    cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
                    int64_t *ret_nhits, int64_t *ret_envi, int64_t *ret_envj, float *ret_sc);
 
+/* ---- E-value calibration ----
+ * cmcalibrate's exponential tail fit for one search mode of a configured
+ * model (src/cmcalibrate.c: process_search_workunit :2328 scans random
+ * sequence with FastCYKScan / FastIInsideScan at the QDB2 bands, NULL3 on;
+ * fit_histogram :1930 fits the top hits with esl_exp_FitComplete).  Scans
+ * total_len residues of seeded random sequence (pieces of seq_len residues
+ * of a background whose GC content changes between segments) in one batched
+ * launch with algo (CMGB_ALGO_CYK or CMGB_ALGO_IINSIDE), keeps the best
+ * tail_per_mb hits per Mb (the reference's --ltailn 750 for local modes,
+ * --gtailn 250 for glocal) and fits them by maximum likelihood: mu = the
+ * lowest tail score, lambda = 1 / mean excess over mu.  The result fills the
+ * fields of the CM file's ECM lines (cm_file.c: "ECMLC lambda mu_extrap
+ * mu_orig dbsize nrandhits tailp").  Only the tail is collected, so
+ * nrandhits = tail size and tailp = 1; E-values, which depend on
+ * nrandhits * tailp only (E = Z / dbsize * nrandhits * tailp *
+ * exp(-lambda (S - mu_orig))), are those of the reference's fit.  ret_ms:
+ * scan kernel time. */
+typedef struct {
+  double  lambda, mu_extrap, mu_orig, dbsize;
+  int64_t nrandhits;
+  double  tailp;
+} cmgb_expinfo;
+int cmgb_Calibrate(cmgb_ctx *ctx, cmgb_model *model, char *errbuf, int algo, int64_t total_len, int64_t seq_len,
+                   uint64_t seed, int tail_per_mb, cmgb_expinfo *ret, float *ret_ms);
+
 /* ---- learned window pre-filter ----
  * No reference counterpart: a learned screen placed before the CYK stage.
  * Windows of 2W residues at stride W over [i0, j0] (window k starts at

@@ -928,6 +928,8 @@ def save_npz(m: CMModel, path: str) -> None:
     for s in _F32:
         d[s] = np.float32(getattr(m, s))
     d["name"] = np.array(m.name)
+    for tag, vals in (m.ecm or {}).items():     # E-value calibration lines (ECMLC, ECMGC, ECMLI, ECMGI)
+        d["ecm_" + tag] = np.array(vals, np.float64)
     np.savez_compressed(path, **d)
 
 
@@ -943,6 +945,7 @@ def load_npz(path: str) -> CMModel:
     for s in _F32:
         setattr(m, s, f32(z[s]))
     m.configured = True
+    m.ecm = {k[4:]: tuple(float(x) for x in z[k]) for k in z.files if k.startswith("ecm_")}
     if m.t_global is not None and m.plast is not None:
         truncation_tables(m)
     return m

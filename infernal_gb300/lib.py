@@ -36,7 +36,7 @@ EXPORTS = [
     "cmgb_FastIInsideScan_dev", "cmgb_count_cells", "cmgb_autotune", "cmgb_FastCYKScan_noalloc",
     "cmgb_FastFInsideScan", "cmgb_FastFInsideScan_dev",
     "cmgb_RefTrCYKScan", "cmgb_RefITrInsideScan", "cmgb_RefTrCYKScan_dev", "cmgb_RefITrInsideScan_dev",
-    "cmgb_ScanBatch", "cmgb_ScanMulti", "cmgb_filter_create", "cmgb_filter_destroy", "cmgb_filter_windows",
+    "cmgb_ScanBatch", "cmgb_ScanMulti", "cmgb_Calibrate", "cmgb_filter_create", "cmgb_filter_destroy", "cmgb_filter_windows",
 ]
 BATCH_ALGOS = {"cyk": 0, "inside": 1, "finside": 2, "trcyk": 3, "trinside": 4}
 
@@ -100,6 +100,8 @@ def bind(path: str) -> ctypes.CDLL:
     lib.cmgb_ScanBatch.restype = I
     lib.cmgb_ScanMulti.argtypes = [P, P, I, P, ctypes.c_char_p, I, I, P, I64, P, P, I, P, P, I, P, I, F, P, P, P, P]
     lib.cmgb_ScanMulti.restype = I
+    lib.cmgb_Calibrate.argtypes = [P, P, ctypes.c_char_p, I, I64, I64, ctypes.c_uint64, I, P, P]
+    lib.cmgb_Calibrate.restype = I
     lib.cmgb_filter_create.argtypes = [P, I, P, P, P, P, ctypes.POINTER(P), ctypes.c_char_p]
     lib.cmgb_filter_create.restype = I
     lib.cmgb_filter_destroy.argtypes = [P]
@@ -123,6 +125,26 @@ def load(path: Optional[str] = None) -> ctypes.CDLL:
     if not os.path.exists(path):
         raise RuntimeError(f"{path} is missing: build it with __graft_entry__.build()")
     return bind(path)
+
+
+class ExpInfo(ctypes.Structure):
+    """cmgb_expinfo: the fields of a CM file ECM line."""
+    _fields_ = [("lambda_", ctypes.c_double), ("mu_extrap", ctypes.c_double), ("mu_orig", ctypes.c_double),
+                ("dbsize", ctypes.c_double), ("nrandhits", ctypes.c_int64), ("tailp", ctypes.c_double)]
+
+
+def evalue(ecm, score: float, Z: float) -> float:
+    """E-value of a bit score in a search of Z residues from an ECM line
+    (lambda, mu_extrap, mu_orig, dbsize, nrandhits, tailp): Z / dbsize *
+    nrandhits * exp(-lambda (S - mu_extrap))."""
+    lam, mu_x, _mu, db, nrand, _tailp = ecm
+    return Z / db * nrand * float(np.exp(-lam * (score - mu_x)))
+
+
+def bits_at_evalue(ecm, E: float, Z: float) -> float:
+    """The bit score whose E-value is E in a search of Z residues."""
+    lam, mu_x, _mu, db, nrand, _tailp = ecm
+    return mu_x - float(np.log(E / (Z / db * nrand))) / lam
 
 
 @dataclass
@@ -345,6 +367,19 @@ class Scanner:
             out.append(ScanResult(allhits[k: k + int(nh[q])], int(ei[q]), int(ej[q]), float(sc[q]), None, ms, 0))
             k += int(nh[q])
         return out
+
+    def calibrate(self, m: cmfile.CMModel, algo: str = "cyk", total_len: int = 1_600_000, seq_len: int = 100_000,
+                  seed: int = 181, tail_per_mb: int = 750):
+        """Runs cmgb_Calibrate; returns (ExpInfo as the CM file's ECM fields, kernel ms)."""
+        mh = self.model(m, 0)
+        e = ExpInfo()
+        ms = ctypes.c_float()
+        err = ctypes.create_string_buffer(256)
+        st = self.lib.cmgb_Calibrate(self._ctx, mh, err, BATCH_ALGOS[{"cyk": "cyk", "inside": "inside"}[algo]],
+                                     total_len, seq_len, seed, tail_per_mb, ctypes.byref(e), ctypes.byref(ms))
+        if st != 0:
+            raise ScanError(st, err.value.decode())
+        return (e.lambda_, e.mu_extrap, e.mu_orig, e.dbsize, float(e.nrandhits), e.tailp), ms.value
 
     def autotune(self, m: cmfile.CMModel, qdbidx: int, algo: str = "cyk", sample_len: int = 0):
         """Runs cmgb_autotune for (model, band set, algorithm); returns (tile_rows, arena)."""

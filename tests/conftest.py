@@ -44,13 +44,13 @@ def emu():
     so = os.path.join(ROOT, "tests", "emu", "_build", "libinfernal_gb300_emu.so")
     os.makedirs(os.path.dirname(so), exist_ok=True)
     csrc = os.path.join(ROOT, "infernal_gb300", "csrc")
-    srcs = [os.path.join(csrc, f) for f in ("capi.cu", "filter.cu", "scan_plan.cpp", "hits.cpp")]
+    srcs = [os.path.join(csrc, f) for f in ("capi.cu", "filter.cu", "scan_plan.cpp", "hits.cpp", "calibrate.cpp")]
     deps = [os.path.join(csrc, f) for f in os.listdir(csrc)] + [os.path.join(ROOT, "include", "infernal_gb300.h"),
                                                              os.path.join(ROOT, "tests", "emu", "cmgb_emu.h")]
     if not os.path.exists(so) or os.path.getmtime(so) < max(os.path.getmtime(s) for s in deps):
         tmp = so + f".tmp{os.getpid()}"
         subprocess.check_call(["g++", "-std=c++20", "-O2", "-fPIC", "-shared", "-ffp-contract=off",
                                "-DCMGB_HOST_EMULATION", "-I", os.path.join(ROOT, "tests", "emu"),
-                               "-x", "c++", srcs[0], srcs[1], "-x", "none", srcs[2], srcs[3], "-o", tmp, "-lpthread"])
+                               "-x", "c++", srcs[0], srcs[1], "-x", "none", srcs[2], srcs[3], srcs[4], "-o", tmp, "-lpthread"])
         os.replace(tmp, so)
     return L.Scanner(lib=L.bind(so))

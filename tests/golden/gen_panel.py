@@ -9,7 +9,8 @@ CMs that ship with the reference (testsuite/*.c.cm, tutorial/*.c.cm) with the
 project's reader (infernal_gb300/cmfile.py) and stores their score tables as
 ``panel/<name>.model.npz``.  The panel spans consensus lengths 71-307
 (227-960 states, 0-7 bifurcations); tRNA, Vault and Plant_SRP are the golden
-models one directory up.
+models one directory up, re-written here too so that every stored model
+carries its CM file's E-value calibration lines (ECMLC/ECMGC/ECMLI/ECMGI).
 """
 from __future__ import annotations
 
@@ -33,6 +34,9 @@ def main(ref_root="/root/reference"):
         m = cmfile.load(os.path.join(ref_root, sub, f"{name}.c.cm"))
         cmfile.save_npz(m, os.path.join(HERE, "panel", f"{name}.model.npz"))
         print(name, m.M, m.clen, m.W)
+    for name in ("tRNA", "Vault", "Plant_SRP"):
+        m = cmfile.load(os.path.join(ref_root, "testsuite", f"{name}.c.cm"))
+        cmfile.save_npz(m, os.path.join(HERE, f"{name}.model.npz"))
 
 
 if __name__ == "__main__":
