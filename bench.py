@@ -624,17 +624,17 @@ def roofline_block(cells, kms, Lres, args):
     alg_bytes = 2 * (Lres + 2) * args.steps
     ach = alg_bytes / (kms / 1e3) / 1e9 if kms > 0 else 0.0
     traffic = None
-    prof = os.path.join(ROOT, "profiles", "qdb_scan_cyk_traffic.json")
-    if os.path.exists(prof):
-        try:
-            traffic = json.load(open(prof)).get("dram_bytes_per_residue")
-            if traffic is not None:
-                traffic = traffic * 2 * (Lres + 2)
-        except Exception:
-            traffic = None
+    prof = os.path.join(ROOT, "profiles", "qdb_scan_cyk_plant_srp_1mb_global.md")
+    if os.path.exists(prof):      # DRAM bytes per residue of one ncu capture of the CYK kernel, scaled
+        import re
+        mt = re.search(r"^dram_bytes_per_residue:\s*([0-9.]+)", open(prof).read(), re.M)
+        if mt:
+            traffic = float(mt.group(1)) * (Lres + 2)     # per CYK launch (one strand)
     return {"bound": "hbm", "achieved": round(ach, 4), "peak": peak, "unit": "GB/s",
             "frac": round(ach / peak, 8), "traffic": traffic,
-            "note": "algorithmic bytes = residues only; the DP is bound by shared-memory/ALU issue, see cell rate"}
+            "note": "algorithmic bytes = residues only; traffic = the CYK kernel's measured DRAM bytes per residue "
+                    "(ncu, 1 Mb capture: tile-arena re-reads past L2) times the residues of one CYK launch; "
+                    "the DP is bound by ALU issue and latency, see alu_roofline and the cell rate"}
 
 
 def cpu_baseline(m, dsq, threads=1, seconds=10.0):
