@@ -494,7 +494,7 @@ CMGB_DEV void tr_scan_body(const TrKParams &p, float *smf, int tid, int nt, int 
 
 #ifndef CMGB_HOST_EMULATION
 template <int ALG, bool GL>
-__global__ void __launch_bounds__(512, 1) tr_scan_kernel(TrKParams p)
+__global__ void __launch_bounds__(512, 2) tr_scan_kernel(TrKParams p)
 {
   extern __shared__ __align__(128) float smem_dyn[];
   tr_scan_body<ALG, GL>(p, smem_dyn, threadIdx.x, blockDim.x, blockIdx.x);
