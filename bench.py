@@ -64,13 +64,16 @@ def _env_int(k, d):
         return d
 
 
-def make_step_input(model_glob, step, mb, seed=20261203, hits_per_mb=2.0):
+def make_step_input(model_glob, step, mb, seed=20261203, hits_per_mb=2.0, gc=0.40):
+    """One step's target and its reverse complement: iid background at GC gc
+    (or per-50-kb segments of GC drawn from a (low, high) range) with
+    hits_per_mb emitted sequences embedded on random strands."""
     from infernal_gb300 import emit
     rng = np.random.default_rng([seed, step])
     L = int(mb * 1_000_000)
     nhits = max(1, int(round(hits_per_mb * mb)))     # default: 200 hits per 100 Mb
     ins = [emit.sample(model_glob, rng) for _ in range(nhits)]
-    dsq, spans = emit.make_target(rng, L, 0.40, ins)
+    dsq, spans = emit.make_target(rng, L, gc, ins)
     return dsq, emit.revcomp_dsq(dsq)
 
 
@@ -211,12 +214,15 @@ def run_learned(args, rank, world):
     import torch
     from infernal_gb300 import cmfile, lib as L, prefilter
     m = cmfile.load_npz(os.path.join(ROOT, "tests", "golden", "Plant_SRP.model.npz"))
-    wts = prefilter.load(os.path.join(ROOT, "infernal_gb300", "filters", "Plant_SRP.filter.npz"))
+    wts = prefilter.load(args.filter or os.path.join(ROOT, "infernal_gb300", "filters", "Plant_SRP.filter.npz"))
     torch.cuda.set_device(0)
     sc = L.Scanner(0)
     filt = prefilter.Prefilter(sc, wts, m.W)
+    if args.filter_recall is not None:
+        filt.use_recall(args.filter_recall)
     nsteps = args.warmup + args.steps
-    inputs = [make_step_input(m, 500000 + s, args.mb, hits_per_mb=args.hits_per_mb) for s in range(nsteps)]
+    inputs = [make_step_input(m, 500000 + s, args.mb, hits_per_mb=args.hits_per_mb, gc=(0.35, 0.60))
+              for s in range(nsteps)]
     Lres = len(inputs[0][0]) - 2
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     sc.autotune(m, 1, "cyk"); sc.autotune(m, 2, "inside")
@@ -309,9 +315,11 @@ def run_learned(args, rank, world):
         "value": round(value, 3), "unit": "Mres/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1000 * tot / args.steps, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "bf16 (filter) + f32 (CYK) + int32 (Inside)", "data": "synthetic",
-        "config": {"workload": f"Plant_SRP CM stand-in, {args.mb} Mb x 2 strands per step, GC 0.40, "
+        "config": {"workload": f"Plant_SRP CM stand-in, {args.mb} Mb x 2 strands per step, GC varying 0.35-0.60 "
+                               f"per 50 kb segment, "
                                f"{args.hits_per_mb} emitted hits per Mb; filter threshold "
-                               f"{filt.thr:.3f}; kept regions scanned by CYK QDB1 ({CYK_CUT} bits) -> Inside QDB2 ({INS_CUT} bits)",
+                               f"{filt.thr:.3f} (validation recall {args.filter_recall or 0.995} of windows with an "
+                               f"E <= 0.01 hit); kept regions scanned by CYK QDB1 ({CYK_CUT} bits) -> Inside QDB2 ({INS_CUT} bits)",
                    "l2": "flushed between timed steps (256 MB write)", "parallelism": "1 GPU"},
         "plain_mres_s": round(res / t_plain / 1e6, 3),
         "speedup_vs_plain": round(t_plain / tot, 2),
@@ -768,6 +776,10 @@ def main():
     ap.add_argument("--cm-slots", type=int, default=0, help="CM slots of the multi workload (default: the panel)")
     ap.add_argument("--reads", type=int, default=5000, help="reads per step of the trunc workload")
     ap.add_argument("--hits-per-mb", type=float, default=2.0, help="embedded hits per Mb (learned workload)")
+    ap.add_argument("--filter", default=None, help="learned workload: filter weights (default: the shipped Plant_SRP filter)")
+    ap.add_argument("--filter-recall", type=float, default=None,
+                    help="learned workload: the filter's stored validation operating point to use "
+                         "(recall of windows holding an E <= 0.01 hit; default: the file's threshold, 0.995)")
     args = ap.parse_args()
     world = _env_int("WORLD_SIZE", 1)
     rank = _env_int("RANK", 0)

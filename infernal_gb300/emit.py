@@ -67,11 +67,22 @@ def background(rng: np.random.Generator, L: int, gc: float) -> np.ndarray:
     return rng.choice(4, size=L, p=p).astype(np.uint8)
 
 
-def make_target(rng: np.random.Generator, L: int, gc: float, inserts: List[str]) -> Tuple[np.ndarray, List[tuple]]:
+def make_target(rng: np.random.Generator, L: int, gc, inserts: List[str],
+                seg_len: int = 50_000) -> Tuple[np.ndarray, List[tuple]]:
     """Digital target (Easel dsq with sentinels) of length L: iid background
     with each insert written over it at a random non-overlapping position on a
-    random strand.  Returns (dsq, [(start, stop, strand)])."""
-    seq = background(rng, L, gc)
+    random strand.  gc is one GC fraction, or a (low, high) range: then every
+    segment of seg_len residues draws its own GC fraction uniformly from it.
+    Returns (dsq, [(start, stop, strand)])."""
+    if isinstance(gc, tuple):
+        parts, left = [], L
+        while left > 0:
+            n = min(seg_len, left)
+            parts.append(background(rng, n, float(rng.uniform(gc[0], gc[1]))))
+            left -= n
+        seq = np.concatenate(parts)
+    else:
+        seq = background(rng, L, gc)
     spans = []
     if inserts:
         slots = np.sort(rng.choice(max(1, L // 2000), size=min(len(inserts), max(1, L // 2000)), replace=False))

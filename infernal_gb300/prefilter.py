@@ -274,6 +274,7 @@ class Prefilter:
         self.sc, self.lib = scanner, scanner.lib
         self.W = W
         self.thr = float(weights.get("threshold", 0.0))
+        self.points = weights.get("recall_points")
         self._keep = [np.ascontiguousarray(weights["w0"], np.float32), np.ascontiguousarray(weights["w"], np.uint16),
                       np.ascontiguousarray(weights["bias"], np.float32), np.ascontiguousarray(weights["wout"], np.float32)]
         self._f = ctypes.c_void_p()
@@ -298,6 +299,17 @@ class Prefilter:
         if st != 0:
             raise lib.ScanError(st, err.value.decode())
         return out[: nw.value], float(ms.value)
+
+    def use_recall(self, recall: float) -> float:
+        """Selects the stored validation operating point with this recall of
+        windows holding an E <= 0.01 hit; returns its threshold."""
+        if self.points is None:
+            raise ValueError("the filter file stores no operating points")
+        k = int(np.argmin(np.abs(self.points[:, 0] - recall)))
+        if abs(self.points[k, 0] - recall) > 1e-9:
+            raise ValueError(f"no stored operating point at recall {recall}")
+        self.thr = float(self.points[k, 1])
+        return self.thr
 
     def regions(self, logits: np.ndarray, i0: int, j0: int, thr: Optional[float] = None) -> List[Tuple[int, int]]:
         """Kept windows (logit > thr) merged into scan regions [a, b]."""
@@ -359,10 +371,13 @@ def main(argv):
           f"negatives kept {kept_neg:.4f}", flush=True)
     bg = np.array([k % 3 == 1 for k in range(ntr, nwin)])      # pure background windows
     print(f"  background windows kept {float((val[bg] > thr).mean()):.4f}", flush=True)
-    for q in (0.9, 0.95, 0.98, 0.99, 0.999):
+    points = []                 # operating points: (recall of E <= 0.01 windows, threshold, negatives kept)
+    for q in (0.9, 0.95, 0.98, 0.99, 0.995, 0.999):
         t = float(pos[int((1 - q) * len(pos))] - 1e-3) if len(pos) else 0.0
-        print(f"  recall {q}: threshold {t:.3f}, negatives kept {float((val[y[ntr:] == 0] > t).mean()):.4f}", flush=True)
-    save(wts, out, threshold=thr, W=m.W, trained_windows=ntr)
+        nk = float((val[y[ntr:] == 0] > t).mean())
+        points.append((q, t, nk))
+        print(f"  recall {q}: threshold {t:.3f}, negatives kept {nk:.4f}", flush=True)
+    save(wts, out, threshold=thr, W=m.W, trained_windows=ntr, recall_points=np.array(points))
     sc.close()
     return 0
 
