@@ -64,6 +64,23 @@ def _env_int(k, d):
         return d
 
 
+def rank_step_seed(rank, step):
+    """Seed of one rank's step: every replica scans its own targets (weak
+    scaling; no data is exchanged between ranks)."""
+    return rank * 100000 + step
+
+
+def max_over_ranks(values, world, device="cuda"):
+    """Each entry's maximum over all ranks (the slowest replica's time); the
+    only collective of a multi-GPU run, outside the timed region."""
+    if world == 1:
+        return [float(v) for v in values]
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
 def make_step_input(model_glob, step, mb, seed=20261203, hits_per_mb=2.0, gc=0.40):
     """One step's target and its reverse complement: iid background at GC gc
     (or per-50-kb segments of GC drawn from a (low, high) range) with
@@ -124,7 +141,7 @@ def run_trunc(args, rank, world):
     keep = []
     desc = cmfile.make_desc(m, keep=keep)
     nsteps = args.warmup + args.steps
-    inputs = [make_reads(m, rank * 100000 + s, args.reads) for s in range(nsteps)]
+    inputs = [make_reads(m, rank_step_seed(rank, s), args.reads) for s in range(nsteps)]
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     lib = sc.lib
 
@@ -469,7 +486,7 @@ def run_ours(args, rank, world):
     import ctypes
 
     nsteps = args.warmup + args.steps
-    inputs = [make_step_input(m, rank * 100000 + s, args.mb) for s in range(nsteps)]
+    inputs = [make_step_input(m, rank_step_seed(rank, s), args.mb) for s in range(nsteps)]
     Lres = len(inputs[0][0]) - 2
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
@@ -537,10 +554,7 @@ def run_ours(args, rank, world):
     clocks = stop_clock_sampler(clk)
     t_e2e, _, _, _, _ = timed(False)
     h2d_step, d2h_step = xfer[0], xfer[1]     # transfers of the last host-buffer step
-    if world > 1:
-        tt = torch.tensor([t_dev, t_e2e], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_dev, t_e2e = float(tt[0]), float(tt[1])
+    t_dev, t_e2e = max_over_ranks([t_dev, t_e2e], world)
     res_per_rank = 2 * Lres * args.steps
     total_res = res_per_rank * world
     value = total_res / t_dev / 1e6
