@@ -364,6 +364,27 @@ void cmgb_filter_destroy(cmgb_filter *filter);
 int  cmgb_filter_windows(cmgb_ctx *ctx, cmgb_filter *filter, const uint8_t *d_dsq, int64_t i0, int64_t j0,
                          float *ret_logits, int64_t max_windows, int64_t *ret_nwin, float *ret_ms, char *errbuf);
 
+/* Training of the same network without batch normalisation (convolution,
+ * bias, ReLU; the result loads into cmgb_filter_create as is), all on the
+ * device: forward on the tensor cores keeping every activation; backward with
+ * the input gradients on the tensor cores (BF16) and the weight gradients in
+ * fp32; AdamW on fp32 master weights.  A trainer holds one batch size.
+ * cmgb_filter_trainer_step takes host windows ([batch][2W] residue codes;
+ * codes above 3 read as missing) and labels ([batch] 0/1); the loss is the
+ * mean over the batch of -w y log s(z) - (1 - y) log(1 - s(z)), s the
+ * logistic function, w = pos_weight; lr = 0 computes gradients without an
+ * update.  _set / _get move the fp32 weights (w as [5][9][128][128] floats)
+ * and, in _get, the last step's gradients (NULL pointers are skipped). */
+typedef struct cmgb_filter_trainer_s cmgb_filter_trainer;
+int  cmgb_filter_trainer_create(cmgb_ctx *ctx, int W, int batch, uint64_t seed, cmgb_filter_trainer **ret, char *errbuf);
+void cmgb_filter_trainer_destroy(cmgb_filter_trainer *trainer);
+int  cmgb_filter_trainer_set(cmgb_filter_trainer *trainer, const float *w0, const float *w, const float *bias,
+                             const float *wout, char *errbuf);
+int  cmgb_filter_trainer_step(cmgb_filter_trainer *trainer, const uint8_t *windows, const float *labels, float pos_weight,
+                              float lr, float weight_decay, float *ret_loss, float *ret_ms, char *errbuf);
+int  cmgb_filter_trainer_get(cmgb_filter_trainer *trainer, float *w0, float *w, float *bias, float *wout,
+                             float *gw0, float *gw, float *gb, float *gwout, char *errbuf);
+
 /* ---- allocation-free CYK scan ----
  * This entry point has no counterpart in the reference.  It exists for
  * callers that must not allocate device memory while they scan: code that

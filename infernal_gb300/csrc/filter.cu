@@ -65,12 +65,14 @@ __device__ __forceinline__ unsigned short f2bf(float x)
 __device__ __forceinline__ float bf2f(unsigned short h) { return __uint_as_float(((unsigned) h) << 16); }
 
 // Layer 0: one-hot input -> 128 channels (a gather of nine weight rows).
-__global__ void filter_layer0(const unsigned char *dsq, long long i0, long long j0, long long W, int nwin, int LP,
-                              const float *w0, const float *b, unsigned short *out)
+// Window win starts at residue i0 + win * wstride (W when scanning, 2W for
+// training batches stored back to back).
+__global__ void filter_layer0(const unsigned char *dsq, long long i0, long long j0, long long W, long long wstride, int nwin,
+                              int LP, const float *w0, const float *b, unsigned short *out)
 {
   const int win = blockIdx.y;
   const int co = threadIdx.x;                  // 128 threads
-  const long long ws = i0 + (long long) win * W;   // first residue of the window
+  const long long ws = i0 + (long long) win * wstride;   // first residue of the window
   for (int i = blockIdx.x; i < LP; i += gridDim.x) {
     float acc = b[co];
     if (i < 2 * W) {
@@ -116,8 +118,12 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *mb, unsign
   return false;
 }
 
+// mask == NULL: out = bf16(relu(acc + bias)) (a forward layer).  mask != NULL:
+// out = bf16(acc) where mask > 0, else 0, no bias (the input gradient of a
+// layer, with the previous layer's ReLU derivative folded in).
 __global__ void __launch_bounds__(128, 1) filter_conv_tc(const unsigned short *in, unsigned short *out, int LP, int W2, int dil,
-                                                         const unsigned short *wt, const float *bias, int *err)
+                                                         const unsigned short *wt, const float *bias, int *err,
+                                                         const unsigned short *mask)
 {
   extern __shared__ __align__(1024) unsigned char tsm[];
   const int rows = TILE + 8 * dil;
@@ -189,8 +195,15 @@ __global__ void __launch_bounds__(128, 1) filter_conv_tc(const unsigned short *i
 #pragma unroll
     for (int j = 0; j < 8; j++) {
       const int co = cb * 16 + 2 * j;
-      float v0 = __uint_as_float(r[2 * j]) + bias[co], v1 = __uint_as_float(r[2 * j + 1]) + bias[co + 1];
-      v0 = v0 > 0.f ? v0 : 0.f; v1 = v1 > 0.f ? v1 : 0.f;
+      float v0, v1;
+      if (mask) {
+        const unsigned mk = *reinterpret_cast<const unsigned *>(mask + (size_t) win * LP * CH + (size_t) row * CH + co);
+        v0 = (mk & 0xFFFFu) != 0 ? __uint_as_float(r[2 * j]) : 0.f;      // activations are >= 0: nonzero bits <=> > 0
+        v1 = (mk >> 16) != 0 ? __uint_as_float(r[2 * j + 1]) : 0.f;
+      } else {
+        v0 = __uint_as_float(r[2 * j]) + bias[co]; v1 = __uint_as_float(r[2 * j + 1]) + bias[co + 1];
+        v0 = v0 > 0.f ? v0 : 0.f; v1 = v1 > 0.f ? v1 : 0.f;
+      }
       if (row >= W2 || !ok) v0 = v1 = 0.f;
       pk[j] = (unsigned) f2bf(v0) | ((unsigned) f2bf(v1) << 16);
     }
@@ -288,14 +301,15 @@ extern "C" int cmgb_filter_windows(cmgb_ctx *ctx, cmgb_filter *f, const uint8_t 
   cudaEvent_t e0, e1;
   FCUDA(cudaEventCreate(&e0)); FCUDA(cudaEventCreate(&e1));
   FCUDA(cudaEventRecord(e0));
-  filter_layer0<<<dim3(64, nwin), CH>>>(d_dsq, i0, j0, W, nwin, f->LP, f->d_w0, f->d_b, f->d_act[0]);
+  filter_layer0<<<dim3(64, nwin), CH>>>(d_dsq, i0, j0, W, W, nwin, f->LP, f->d_w0, f->d_b, f->d_act[0]);
   FCUDA(cudaGetLastError());
   int cur = 0;
   for (int l = 1; l < NL; l++) {
     const int d = DIL[l];
     const size_t sm = (size_t) 16 * (TILE + 8 * d) * 16 + (size_t) 16 * CH * 16 + 64;
     filter_conv_tc<<<dim3(f->LP / TILE, nwin), 128, sm>>>(f->d_act[cur], f->d_act[cur ^ 1], f->LP, (int) (2 * W), d,
-                                                          f->d_w + (size_t) (l - 1) * KT * CH * CH, f->d_b + l * CH, f->d_err);
+                                                          f->d_w + (size_t) (l - 1) * KT * CH * CH, f->d_b + l * CH, f->d_err,
+                                                          nullptr);
     FCUDA(cudaGetLastError());
     cur ^= 1;
   }
@@ -311,6 +325,356 @@ extern "C" int cmgb_filter_windows(cmgb_ctx *ctx, cmgb_filter *f, const uint8_t 
   cudaEventDestroy(e0); cudaEventDestroy(e1);
   if (ret_nwin) *ret_nwin = nwin;
   if (ret_ms) *ret_ms = ms;
+  return CMGB_OK;
+#endif
+}
+
+// ---------------------------------------------------------------------------
+// Training.  The network above without batch normalisation (convolution,
+// bias, ReLU), trained on batches of B windows of 2W residues with a
+// pos-weighted logistic loss and AdamW, all on the device:
+//   forward   layer 0 gather, layers 1-5 on tcgen05 (every activation kept),
+//             max over positions (arg-max kept), linear read-out, loss;
+//   backward  read-out -> the arg-max cells of layer 5; per layer l = 5..1:
+//             bias gradient (column sums), weight gradient (CUDA-core
+//             reduction over every position, fp32), input gradient on
+//             tcgen05 as a forward convolution with the taps reversed and
+//             each tap's weights transposed, the ReLU derivative of layer
+//             l-1 folded into its epilogue; layer 0's weight gradient is a
+//             scatter over the one-hot residues;
+//   update    AdamW on fp32 master weights, then BF16 copies for the
+//             forward and (transposed, taps reversed) for the backward.
+// Gradients of a layer's input are rounded to BF16 (the tensor-core
+// operand type); weight and bias gradients accumulate in fp32.
+namespace {
+constexpr size_t OFF_W0 = 0;                                   // [9][4][128]
+constexpr size_t OFF_W = OFF_W0 + (size_t) KT * 4 * CH;        // [5][9][128 co][128 ci]
+constexpr size_t OFF_B = OFF_W + (size_t) 5 * KT * CH * CH;    // [6][128]
+constexpr size_t OFF_WOUT = OFF_B + (size_t) NL * CH;          // [128] + bias
+constexpr size_t NPARAM = OFF_WOUT + CH + 1;
+}
+
+struct cmgb_filter_trainer_s {
+  int W = 0, LP = 0, B = 0;
+  long long t = 0;                                  // AdamW steps taken
+  float *p = nullptr, *g = nullptr, *m1 = nullptr, *m2 = nullptr;   // [NPARAM] each
+  unsigned short *wbf = nullptr, *wtbf = nullptr;   // [5][9][128][128]
+  unsigned char *win = nullptr;                     // [B][2W]
+  float *y = nullptr, *pooled = nullptr, *logit = nullptr, *dlogit = nullptr, *loss = nullptr;
+  int *argm = nullptr;
+  unsigned short *act[NL] = {nullptr};              // [B][LP][128]
+  unsigned short *dz[2] = {nullptr, nullptr};
+  int *err = nullptr;
+};
+
+#ifndef CMGB_HOST_EMULATION
+// max over positions (first arg-max) per channel, then the read-out
+__global__ void train_readout_fwd(const unsigned short *act, int LP, int W2, const float *wout, float *pooled, int *argm,
+                                  float *logit)
+{
+  __shared__ float red[CH];
+  const int b = blockIdx.x, c = threadIdx.x;
+  const unsigned short *a = act + (size_t) b * LP * CH + c;
+  float m = 0.f; int am = 0;
+  for (int i = 0; i < W2; i++) { const float v = bf2f(a[(size_t) i * CH]); if (v > m) { m = v; am = i; } }
+  pooled[b * CH + c] = m; argm[b * CH + c] = am;
+  red[c] = m * wout[c];
+  __syncthreads();
+  for (int s = CH / 2; s > 0; s >>= 1) { if (c < s) red[c] += red[c + s]; __syncthreads(); }
+  if (c == 0) logit[b] = red[0] + wout[CH];
+}
+
+// loss = mean_b [ -w y log s(z) - (1 - y) log(1 - s(z)) ],  dz = d loss / d z
+__global__ void train_loss(const float *logit, const float *y, float posw, int B, float *dlogit, float *loss)
+{
+  __shared__ float red[256];
+  float acc = 0.f;
+  for (int b = threadIdx.x; b < B; b += blockDim.x) {
+    const float z = logit[b], t = y[b];
+    const float ls = z >= 0.f ? -log1pf(expf(-z)) : z - log1pf(expf(z));        // log s(z)
+    const float l1s = z >= 0.f ? -z - log1pf(expf(-z)) : -log1pf(expf(z));      // log (1 - s(z))
+    const float s = 1.f / (1.f + expf(-z));
+    acc += -posw * t * ls - (1.f - t) * l1s;
+    dlogit[b] = (posw * t * (s - 1.f) + (1.f - t) * s) / (float) B;
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) { if ((int) threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s]; __syncthreads(); }
+  if (threadIdx.x == 0) *loss = red[0] / (float) B;
+}
+
+// read-out backward: weight gradients and the layer-5 gradient at the arg-max cells
+__global__ void train_readout_bwd(const float *dlogit, const float *pooled, const int *argm, const float *wout, int LP,
+                                  float *g_wout, unsigned short *dz5)
+{
+  const int b = blockIdx.x, c = threadIdx.x;
+  const float d = dlogit[b], pv = pooled[b * CH + c];
+  atomicAdd(g_wout + c, d * pv);
+  if (c == 0) atomicAdd(g_wout + CH, d);
+  if (pv > 0.f) dz5[((size_t) b * LP + argm[b * CH + c]) * CH + c] = f2bf(d * wout[c]);
+}
+
+// bias gradient: column sums of dz over rows [0, nrows)
+__global__ void train_bias_grad(const unsigned short *dz, long long nrows, float *gb)
+{
+  const int c = threadIdx.x;
+  float acc = 0.f;
+  for (long long r = blockIdx.x; r < nrows; r += gridDim.x) acc += bf2f(dz[(size_t) r * CH + c]);
+  atomicAdd(gb + c, acc);
+}
+
+// weight gradient of a dilated layer: gw[t][co][ci] += sum over (b, p) of
+// dz[b][p][co] * a[b][p + (t - 4) dil][ci]; block: one tap, a 32 x 32 (co, ci)
+// tile, a slice of the positions; 256 threads x 2 x 2 outputs
+__global__ void __launch_bounds__(256) train_wgrad(const unsigned short *dz, const unsigned short *a, int B, int LP, int W2,
+                                                   int dil, float *gw)
+{
+  __shared__ float sd[32][33], sa[32][33];
+  const int t = blockIdx.x, co0 = (blockIdx.y >> 2) * 32, ci0 = (blockIdx.y & 3) * 32;
+  const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+  const long long npos = (long long) B * LP;
+  const long long per = (npos + gridDim.z - 1) / gridDim.z;
+  const long long P0 = per * blockIdx.z, P1 = P0 + per < npos ? P0 + per : npos;
+  const int sh = (t - 4) * dil;
+  float acc[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+  for (long long P = P0; P < P1; P += 32) {
+    for (int x = tid; x < 32 * 32; x += 256) {
+      const int r = x >> 5, c = x & 31;
+      const long long Q = P + r;
+      float vd = 0.f, va = 0.f;
+      if (Q < P1) {
+        const int b = (int) (Q / LP), p = (int) (Q - (long long) b * LP);
+        if (p < W2) {
+          vd = bf2f(dz[(size_t) Q * CH + co0 + c]);
+          const int q = p + sh;
+          if (q >= 0 && q < W2) va = bf2f(a[((size_t) b * LP + q) * CH + ci0 + c]);
+        }
+      }
+      sd[r][c] = vd; sa[r][c] = va;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int r = 0; r < 32; r++) {
+      const float d0 = sd[r][2 * ty], d1 = sd[r][2 * ty + 1], a0 = sa[r][2 * tx], a1 = sa[r][2 * tx + 1];
+      acc[0][0] += d0 * a0; acc[0][1] += d0 * a1; acc[1][0] += d1 * a0; acc[1][1] += d1 * a1;
+    }
+    __syncthreads();
+  }
+  float *o = gw + (size_t) t * CH * CH;
+  for (int i = 0; i < 2; i++)
+    for (int j = 0; j < 2; j++) atomicAdd(o + (size_t) (co0 + 2 * ty + i) * CH + ci0 + 2 * tx + j, acc[i][j]);
+}
+
+// layer 0 weight gradient: gw0[t][x][co] += dz0[b][p][co] where residue
+// p + t - 4 of window b is x (one block per window slice, 128 threads = co)
+__global__ void train_wgrad0(const unsigned short *dz, const unsigned char *win, int LP, int W, float *gw0)
+{
+  __shared__ float acc[KT * 4][CH];
+  const int b = blockIdx.y, c = threadIdx.x, W2 = 2 * W;
+  for (int k = 0; k < KT * 4; k++) acc[k][c] = 0.f;
+  const int per = (W2 + gridDim.x - 1) / gridDim.x;
+  const int p0 = per * blockIdx.x, p1 = p0 + per < W2 ? p0 + per : W2;
+  for (int p = p0; p < p1; p++) {
+    const float gv = bf2f(dz[((size_t) b * LP + p) * CH + c]);
+    if (gv == 0.f) continue;
+    for (int t = 0; t < KT; t++) {
+      const int q = p + t - 4;
+      if (q < 0 || q >= W2) continue;
+      const int x = win[(size_t) b * W2 + q];
+      if (x < 4) acc[t * 4 + x][c] += gv;
+    }
+  }
+  for (int k = 0; k < KT * 4; k++) if (acc[k][c] != 0.f) atomicAdd(gw0 + (size_t) k * CH + c, acc[k][c]);
+}
+
+__global__ void train_adamw(float *p, const float *g, float *m1, float *m2, long long n, float lr, float b1, float b2,
+                            float eps, float wd, float bc1, float bc2)
+{
+  for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float a = b1 * m1[i] + (1.f - b1) * gi, v = b2 * m2[i] + (1.f - b2) * gi * gi;
+    m1[i] = a; m2[i] = v;
+    p[i] = p[i] * (1.f - lr * wd) - lr * (a / bc1) / (sqrtf(v / bc2) + eps);
+  }
+}
+
+// BF16 copies of the dilated layers: forward [l][t][co][ci] and backward
+// [l][t'][ci][co] = w[l][8 - t'][co][ci]
+__global__ void train_pack(const float *w, unsigned short *wbf, unsigned short *wtbf)
+{
+  const long long n = (long long) 5 * KT * CH * CH;
+  for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+    const int ci = (int) (i % CH), co = (int) ((i / CH) % CH), t = (int) ((i / (CH * CH)) % KT), l = (int) (i / ((long long) KT * CH * CH));
+    const unsigned short h = f2bf(w[i]);
+    wbf[i] = h;
+    wtbf[(((size_t) l * KT + (KT - 1 - t)) * CH + ci) * CH + co] = h;
+  }
+}
+#endif
+
+extern "C" int cmgb_filter_trainer_create(cmgb_ctx *ctx, int W, int batch, uint64_t seed, cmgb_filter_trainer **ret, char *errbuf)
+{
+  (void) ctx;
+  *ret = nullptr;
+#ifdef CMGB_HOST_EMULATION
+  (void) W; (void) batch; (void) seed;
+  FERR(CMGB_ENODEV, "filter trainer: not available in the host emulation");
+#else
+  if (W < 16 || batch < 1 || batch > 65535) FERR(CMGB_EINVAL, "filter trainer: invalid W or batch");
+  std::unique_ptr<cmgb_filter_trainer> f(new cmgb_filter_trainer);
+  f->W = W; f->B = batch; f->LP = ((2 * W + TILE - 1) / TILE) * TILE;
+  const size_t act = (size_t) batch * f->LP * CH * sizeof(unsigned short);
+  FCUDA(cudaMalloc(&f->p, NPARAM * sizeof(float))); FCUDA(cudaMalloc(&f->g, NPARAM * sizeof(float)));
+  FCUDA(cudaMalloc(&f->m1, NPARAM * sizeof(float))); FCUDA(cudaMalloc(&f->m2, NPARAM * sizeof(float)));
+  FCUDA(cudaMemset(f->m1, 0, NPARAM * sizeof(float))); FCUDA(cudaMemset(f->m2, 0, NPARAM * sizeof(float)));
+  FCUDA(cudaMalloc(&f->wbf, (size_t) 5 * KT * CH * CH * 2)); FCUDA(cudaMalloc(&f->wtbf, (size_t) 5 * KT * CH * CH * 2));
+  FCUDA(cudaMalloc(&f->win, (size_t) batch * 2 * W));
+  FCUDA(cudaMalloc(&f->y, sizeof(float) * batch)); FCUDA(cudaMalloc(&f->pooled, sizeof(float) * batch * CH));
+  FCUDA(cudaMalloc(&f->logit, sizeof(float) * batch)); FCUDA(cudaMalloc(&f->dlogit, sizeof(float) * batch));
+  FCUDA(cudaMalloc(&f->loss, sizeof(float))); FCUDA(cudaMalloc(&f->argm, sizeof(int) * batch * CH));
+  for (int l = 0; l < NL; l++) FCUDA(cudaMalloc(&f->act[l], act));
+  FCUDA(cudaMalloc(&f->dz[0], act)); FCUDA(cudaMalloc(&f->dz[1], act));
+  FCUDA(cudaMalloc(&f->err, sizeof(int))); FCUDA(cudaMemset(f->err, 0, sizeof(int)));
+  // He-uniform initial weights from a splitmix64 stream, zero biases
+  std::vector<float> h(NPARAM, 0.f);
+  uint64_t s = seed ^ 0x9E3779B97F4A7C15ULL;
+  auto uni = [&s]() {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL; z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL; z ^= z >> 31;
+    return (double) (z >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+  };
+  const double a0 = std::sqrt(6.0 / (4 * KT)), a1 = std::sqrt(6.0 / (CH * KT)), a2 = std::sqrt(6.0 / CH);
+  for (size_t i = OFF_W0; i < OFF_W; i++) h[i] = (float) (a0 * uni());
+  for (size_t i = OFF_W; i < OFF_B; i++) h[i] = (float) (a1 * uni());
+  for (size_t i = OFF_WOUT; i < OFF_WOUT + CH; i++) h[i] = (float) (a2 * uni());
+  FCUDA(cudaMemcpy(f->p, h.data(), NPARAM * sizeof(float), cudaMemcpyHostToDevice));
+  train_pack<<<512, 256>>>(f->p + OFF_W, f->wbf, f->wtbf);
+  FCUDA(cudaGetLastError());
+  const int maxsm = 16 * (TILE + 8 * DIL[NL - 1]) * 16 + 16 * CH * 16 + 64;
+  FCUDA(cudaFuncSetAttribute(filter_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm));
+  FCUDA(cudaDeviceSynchronize());
+  *ret = f.release();
+  return CMGB_OK;
+#endif
+}
+
+extern "C" void cmgb_filter_trainer_destroy(cmgb_filter_trainer *f)
+{
+  if (!f) return;
+#ifndef CMGB_HOST_EMULATION
+  cudaFree(f->p); cudaFree(f->g); cudaFree(f->m1); cudaFree(f->m2); cudaFree(f->wbf); cudaFree(f->wtbf);
+  cudaFree(f->win); cudaFree(f->y); cudaFree(f->pooled); cudaFree(f->logit); cudaFree(f->dlogit); cudaFree(f->loss);
+  cudaFree(f->argm); for (int l = 0; l < NL; l++) cudaFree(f->act[l]);
+  cudaFree(f->dz[0]); cudaFree(f->dz[1]); cudaFree(f->err);
+#endif
+  delete f;
+}
+
+// Sets the fp32 master weights (layout of cmgb_filter_create, but the dilated
+// layers in fp32) and resets the optimiser state.
+extern "C" int cmgb_filter_trainer_set(cmgb_filter_trainer *f, const float *w0, const float *w, const float *bias,
+                                       const float *wout, char *errbuf)
+{
+#ifdef CMGB_HOST_EMULATION
+  (void) f; (void) w0; (void) w; (void) bias; (void) wout;
+  FERR(CMGB_ENODEV, "filter trainer: not available in the host emulation");
+#else
+  if (!f || !w0 || !w || !bias || !wout) FERR(CMGB_EINVAL, "filter trainer: invalid arguments");
+  FCUDA(cudaMemcpy(f->p + OFF_W0, w0, sizeof(float) * (OFF_W - OFF_W0), cudaMemcpyHostToDevice));
+  FCUDA(cudaMemcpy(f->p + OFF_W, w, sizeof(float) * (OFF_B - OFF_W), cudaMemcpyHostToDevice));
+  FCUDA(cudaMemcpy(f->p + OFF_B, bias, sizeof(float) * (OFF_WOUT - OFF_B), cudaMemcpyHostToDevice));
+  FCUDA(cudaMemcpy(f->p + OFF_WOUT, wout, sizeof(float) * (CH + 1), cudaMemcpyHostToDevice));
+  FCUDA(cudaMemset(f->m1, 0, NPARAM * sizeof(float))); FCUDA(cudaMemset(f->m2, 0, NPARAM * sizeof(float)));
+  f->t = 0;
+  train_pack<<<512, 256>>>(f->p + OFF_W, f->wbf, f->wtbf);
+  FCUDA(cudaGetLastError());
+  return CMGB_OK;
+#endif
+}
+
+// One step on a batch: windows (host, [batch][2W] residue codes 0-3, others
+// read as missing), labels (host, [batch] 0/1), the positive-class weight and
+// the learning rate (0: gradients only, no update).
+extern "C" int cmgb_filter_trainer_step(cmgb_filter_trainer *f, const uint8_t *windows, const float *labels, float pos_weight,
+                                        float lr, float weight_decay, float *ret_loss, float *ret_ms, char *errbuf)
+{
+#ifdef CMGB_HOST_EMULATION
+  (void) f; (void) windows; (void) labels; (void) pos_weight; (void) lr; (void) weight_decay; (void) ret_loss; (void) ret_ms;
+  FERR(CMGB_ENODEV, "filter trainer: not available in the host emulation");
+#else
+  if (!f || !windows || !labels) FERR(CMGB_EINVAL, "filter trainer: invalid arguments");
+  const int B = f->B, W = f->W, LP = f->LP, W2 = 2 * W;
+  const size_t actb = (size_t) B * LP * CH * sizeof(unsigned short);
+  cudaEvent_t e0, e1;
+  FCUDA(cudaEventCreate(&e0)); FCUDA(cudaEventCreate(&e1));
+  FCUDA(cudaMemcpy(f->win, windows, (size_t) B * W2, cudaMemcpyHostToDevice));
+  FCUDA(cudaMemcpy(f->y, labels, sizeof(float) * B, cudaMemcpyHostToDevice));
+  FCUDA(cudaEventRecord(e0));
+  // forward
+  filter_layer0<<<dim3(64, B), CH>>>(f->win, 0, (long long) B * W2 - 1, W, W2, B, LP, f->p + OFF_W0, f->p + OFF_B, f->act[0]);
+  for (int l = 1; l < NL; l++) {
+    const int d = DIL[l];
+    const size_t sm = (size_t) 16 * (TILE + 8 * d) * 16 + (size_t) 16 * CH * 16 + 64;
+    filter_conv_tc<<<dim3(LP / TILE, B), 128, sm>>>(f->act[l - 1], f->act[l], LP, W2, d, f->wbf + (size_t) (l - 1) * KT * CH * CH,
+                                                    f->p + OFF_B + l * CH, f->err, nullptr);
+  }
+  train_readout_fwd<<<B, CH>>>(f->act[NL - 1], LP, W2, f->p + OFF_WOUT, f->pooled, f->argm, f->logit);
+  train_loss<<<1, 256>>>(f->logit, f->y, pos_weight, B, f->dlogit, f->loss);
+  // backward
+  FCUDA(cudaMemset(f->g, 0, NPARAM * sizeof(float)));
+  FCUDA(cudaMemset(f->dz[0], 0, actb));
+  train_readout_bwd<<<B, CH>>>(f->dlogit, f->pooled, f->argm, f->p + OFF_WOUT, LP, f->g + OFF_WOUT, f->dz[0]);
+  int cur = 0;
+  const int zsplit = std::max(1, std::min(64, (int) (((long long) B * LP) / 2048)));
+  for (int l = NL - 1; l >= 1; l--) {
+    const int d = DIL[l];
+    train_bias_grad<<<256, CH>>>(f->dz[cur], (long long) B * LP, f->g + OFF_B + l * CH);
+    train_wgrad<<<dim3(KT, 16, zsplit), 256>>>(f->dz[cur], f->act[l - 1], B, LP, W2, d, f->g + OFF_W + (size_t) (l - 1) * KT * CH * CH);
+    const size_t sm = (size_t) 16 * (TILE + 8 * d) * 16 + (size_t) 16 * CH * 16 + 64;
+    filter_conv_tc<<<dim3(LP / TILE, B), 128, sm>>>(f->dz[cur], f->dz[cur ^ 1], LP, W2, d, f->wtbf + (size_t) (l - 1) * KT * CH * CH,
+                                                    nullptr, f->err, f->act[l - 1]);
+    cur ^= 1;
+  }
+  train_bias_grad<<<256, CH>>>(f->dz[cur], (long long) B * LP, f->g + OFF_B);
+  train_wgrad0<<<dim3(8, B), CH>>>(f->dz[cur], f->win, LP, W, f->g + OFF_W0);
+  if (lr > 0.f) {
+    f->t++;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float bc1 = (float) (1.0 - std::pow((double) b1, (double) f->t)), bc2 = (float) (1.0 - std::pow((double) b2, (double) f->t));
+    train_adamw<<<512, 256>>>(f->p, f->g, f->m1, f->m2, (long long) NPARAM, lr, b1, b2, 1e-8f, weight_decay, bc1, bc2);
+    train_pack<<<512, 256>>>(f->p + OFF_W, f->wbf, f->wtbf);
+  }
+  FCUDA(cudaGetLastError());
+  FCUDA(cudaEventRecord(e1));
+  float hl = 0.f; int herr = 0;
+  FCUDA(cudaMemcpy(&hl, f->loss, sizeof(float), cudaMemcpyDeviceToHost));
+  FCUDA(cudaMemcpy(&herr, f->err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (herr) FERR(CMGB_ENODEV, "filter trainer: a bounded tensor-core wait ran out");
+  float ms = 0.f;
+  FCUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0); cudaEventDestroy(e1);
+  if (ret_loss) *ret_loss = hl;
+  if (ret_ms) *ret_ms = ms;
+  return CMGB_OK;
+#endif
+}
+
+// Copies out the fp32 master weights (set's layout) and, when gw0 != NULL, the
+// last step's gradients in the same layout (gw0, gw, gb, gwout).
+extern "C" int cmgb_filter_trainer_get(cmgb_filter_trainer *f, float *w0, float *w, float *bias, float *wout,
+                                       float *gw0, float *gw, float *gb, float *gwout, char *errbuf)
+{
+#ifdef CMGB_HOST_EMULATION
+  (void) f; (void) w0; (void) w; (void) bias; (void) wout; (void) gw0; (void) gw; (void) gb; (void) gwout;
+  FERR(CMGB_ENODEV, "filter trainer: not available in the host emulation");
+#else
+  if (!f) FERR(CMGB_EINVAL, "filter trainer: invalid arguments");
+  const float *src[2] = {f->p, f->g};
+  float *dst[2][4] = {{w0, w, bias, wout}, {gw0, gw, gb, gwout}};
+  const size_t off[5] = {OFF_W0, OFF_W, OFF_B, OFF_WOUT, NPARAM};
+  for (int k = 0; k < 2; k++)
+    for (int j = 0; j < 4; j++)
+      if (dst[k][j]) FCUDA(cudaMemcpy(dst[k][j], src[k] + off[j], sizeof(float) * (off[j + 1] - off[j]), cudaMemcpyDeviceToHost));
   return CMGB_OK;
 #endif
 }

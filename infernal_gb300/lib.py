@@ -36,7 +36,8 @@ EXPORTS = [
     "cmgb_FastIInsideScan_dev", "cmgb_count_cells", "cmgb_autotune", "cmgb_FastCYKScan_noalloc",
     "cmgb_FastFInsideScan", "cmgb_FastFInsideScan_dev",
     "cmgb_RefTrCYKScan", "cmgb_RefITrInsideScan", "cmgb_RefTrCYKScan_dev", "cmgb_RefITrInsideScan_dev",
-    "cmgb_ScanBatch", "cmgb_ScanMulti", "cmgb_Calibrate", "cmgb_filter_create", "cmgb_filter_destroy", "cmgb_filter_windows",
+    "cmgb_ScanBatch", "cmgb_ScanMulti", "cmgb_Calibrate", "cmgb_filter_trainer_create", "cmgb_filter_trainer_destroy",
+    "cmgb_filter_trainer_set", "cmgb_filter_trainer_step", "cmgb_filter_trainer_get", "cmgb_filter_create", "cmgb_filter_destroy", "cmgb_filter_windows",
 ]
 BATCH_ALGOS = {"cyk": 0, "inside": 1, "finside": 2, "trcyk": 3, "trinside": 4}
 
@@ -102,6 +103,16 @@ def bind(path: str) -> ctypes.CDLL:
     lib.cmgb_ScanMulti.restype = I
     lib.cmgb_Calibrate.argtypes = [P, P, ctypes.c_char_p, I, I64, I64, ctypes.c_uint64, I, P, P]
     lib.cmgb_Calibrate.restype = I
+    lib.cmgb_filter_trainer_create.argtypes = [P, I, I, ctypes.c_uint64, ctypes.POINTER(P), ctypes.c_char_p]
+    lib.cmgb_filter_trainer_create.restype = I
+    lib.cmgb_filter_trainer_destroy.argtypes = [P]
+    lib.cmgb_filter_trainer_destroy.restype = None
+    lib.cmgb_filter_trainer_set.argtypes = [P, P, P, P, P, ctypes.c_char_p]
+    lib.cmgb_filter_trainer_set.restype = I
+    lib.cmgb_filter_trainer_step.argtypes = [P, P, P, F, F, F, P, P, ctypes.c_char_p]
+    lib.cmgb_filter_trainer_step.restype = I
+    lib.cmgb_filter_trainer_get.argtypes = [P, P, P, P, P, P, P, P, P, ctypes.c_char_p]
+    lib.cmgb_filter_trainer_get.restype = I
     lib.cmgb_filter_create.argtypes = [P, I, P, P, P, P, ctypes.POINTER(P), ctypes.c_char_p]
     lib.cmgb_filter_create.restype = I
     lib.cmgb_filter_destroy.argtypes = [P]

@@ -265,6 +265,68 @@ def load(path: str) -> dict:
     return {k: z[k] for k in z.files}
 
 
+class NativeTrainer:
+    """The hand-written device trainer (cmgb_filter_trainer_*): the network
+    without batch normalisation, trained with AdamW on the GPU; the weights it
+    returns load into Prefilter directly."""
+
+    def __init__(self, scanner: "lib.Scanner", W: int, batch: int, seed: int = 0):
+        import ctypes
+        self.lib, self.W, self.B = scanner.lib, W, batch
+        self._h = ctypes.c_void_p()
+        err = ctypes.create_string_buffer(256)
+        st = self.lib.cmgb_filter_trainer_create(scanner._ctx, W, batch, seed, ctypes.byref(self._h), err)
+        if st != 0:
+            raise lib.ScanError(st, err.value.decode())
+
+    def close(self):
+        if self._h:
+            self.lib.cmgb_filter_trainer_destroy(self._h)
+            self._h = None
+
+    def set(self, w0, w, bias, wout):
+        import ctypes
+        arrs = [np.ascontiguousarray(a, np.float32) for a in (w0, w, bias, wout)]
+        err = ctypes.create_string_buffer(256)
+        st = self.lib.cmgb_filter_trainer_set(self._h, *[a.ctypes.data for a in arrs], err)
+        if st != 0:
+            raise lib.ScanError(st, err.value.decode())
+
+    def step(self, windows: np.ndarray, labels: np.ndarray, pos_weight: float, lr: float, weight_decay: float = 1e-4):
+        """One batch: windows uint8 [B][2W] residue codes, labels [B]; returns (loss, ms)."""
+        import ctypes
+        x = np.ascontiguousarray(windows, np.uint8)
+        y = np.ascontiguousarray(labels, np.float32)
+        assert x.shape == (self.B, 2 * self.W) and y.shape == (self.B,)
+        loss, ms = ctypes.c_float(), ctypes.c_float()
+        err = ctypes.create_string_buffer(256)
+        st = self.lib.cmgb_filter_trainer_step(self._h, x.ctypes.data, y.ctypes.data, pos_weight, lr, weight_decay,
+                                               ctypes.byref(loss), ctypes.byref(ms), err)
+        if st != 0:
+            raise lib.ScanError(st, err.value.decode())
+        return loss.value, ms.value
+
+    def get(self, grads: bool = False):
+        """fp32 weights (w0 [9,4,128], w [5,9,128,128], bias [6,128], wout [129]), and the last step's gradients."""
+        import ctypes
+        shapes = [(9, 4, 128), (5, 9, 128, 128), (6, 128), (129,)]
+        ws = [np.zeros(sh, np.float32) for sh in shapes]
+        gs = [np.zeros(sh, np.float32) for sh in shapes] if grads else [None] * 4
+        err = ctypes.create_string_buffer(256)
+        ptr = [a.ctypes.data if a is not None else None for a in ws + gs]
+        st = self.lib.cmgb_filter_trainer_get(self._h, *ptr, err)
+        if st != 0:
+            raise lib.ScanError(st, err.value.decode())
+        return (ws, gs) if grads else ws
+
+    def weights(self) -> dict:
+        """The trained network in the layout of export() (BF16 dilated layers)."""
+        w0, w, bias, wout = self.get()
+        import torch
+        wb = torch.from_numpy(w).bfloat16().view(torch.int16).numpy().view(np.uint16)
+        return {"w0": w0, "w": wb, "bias": bias, "wout": wout}
+
+
 # ---------------------------------------------------------------------------
 # scan-time use
 class Prefilter:

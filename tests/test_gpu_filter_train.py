@@ -1,0 +1,107 @@
+"""Hand-written training of the pre-filter network (cmgb_filter_trainer_*).
+
+1. One step's gradients against PyTorch autograd on the same weights and
+   windows (FP32 on the CPU, with the kernels' BF16 rounding points in the
+   forward pass: the dilated layers' weights and every layer's output).  The
+   device backward also rounds each layer's input gradient to BF16 (the
+   tensor-core operand type), so the comparison is a relative norm error per
+   gradient tensor, bounded in the test.
+2. A short training run on a motif task converges, and the trained weights
+   load into the inference kernels (Prefilter) and classify held-out windows.
+"""
+import numpy as np
+import pytest
+
+from infernal_gb300 import cmfile, lib as L, prefilter
+
+pytestmark = pytest.mark.gpu
+DIL = (1, 2, 4, 8, 16, 32)
+
+
+def _torch_grads(ws, wins, y, posw):
+    import torch
+    import torch.nn.functional as F
+    bf = lambda t: t.to(torch.bfloat16).to(torch.float32)
+    w0, w, bias, wout = [torch.tensor(a, dtype=torch.float32, requires_grad=True) for a in ws]
+    B, n = wins.shape
+    x = torch.zeros(B, 4, n)
+    x[np.repeat(np.arange(B), n), wins.ravel().astype(np.int64), np.tile(np.arange(n), B)] = 1.0   # one-hot [B, 4, 2W]
+    a = bf(F.relu(F.conv1d(x, w0.permute(2, 1, 0), bias[0], padding=4)))
+    for l in range(1, 6):
+        d = DIL[l]
+        a = bf(F.relu(F.conv1d(a, bf(w[l - 1]).permute(1, 2, 0), bias[l], padding=4 * d, dilation=d)))
+    z = a.max(dim=2).values @ wout[:128] + wout[128]
+    loss = F.binary_cross_entropy_with_logits(z, torch.tensor(y), pos_weight=torch.tensor(posw))
+    loss.backward()
+    return float(loss), [t.grad.numpy() for t in (w0, w, bias, wout)]
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    s = L.Scanner(0)
+    yield s
+    s.close()
+
+
+def test_gradients_match_autograd(gpu):
+    W, B = 336, 8
+    rng = np.random.default_rng(5)
+    tr = prefilter.NativeTrainer(gpu, W, B, seed=3)
+    try:
+        wins = rng.integers(0, 4, (B, 2 * W)).astype(np.uint8)
+        y = np.array([1, 0] * (B // 2), np.float32)
+        ws = tr.get()
+        loss, _ = tr.step(wins, y, 3.0, 0.0)
+        _, gs = tr.get(grads=True)
+    finally:
+        tr.close()
+    ref_loss, ref = _torch_grads(ws, wins, y, 3.0)
+    assert abs(loss - ref_loss) < 1e-3 * max(1.0, abs(ref_loss))
+    names = ("w0", "w", "bias", "wout")
+    for name, g, r in zip(names, gs, ref):
+        rel = np.linalg.norm(g - r) / max(np.linalg.norm(r), 1e-12)
+        print(f"{name}: |g| {np.linalg.norm(r):.4g}, relative error {rel:.4f}")
+        assert rel < (0.01 if name == "wout" else 0.05), name
+    for l in range(5):                     # per dilated layer too
+        rel = np.linalg.norm(gs[1][l] - ref[1][l]) / max(np.linalg.norm(ref[1][l]), 1e-12)
+        assert rel < 0.05, l
+
+
+def _motif_batch(rng, B, W, motif):
+    wins = rng.integers(0, 4, (B, 2 * W)).astype(np.uint8)
+    y = (rng.random(B) < 0.5).astype(np.float32)
+    for b in np.nonzero(y)[0]:
+        p = int(rng.integers(0, 2 * W - len(motif)))
+        wins[b, p:p + len(motif)] = motif
+    return wins, y
+
+
+def test_training_converges_and_loads_into_inference(gpu):
+    import torch
+    W, B = 64, 64
+    rng = np.random.default_rng(11)
+    motif = np.array([2, 2, 2, 0, 1, 1, 1, 3, 0, 2], np.uint8)     # GGGACCCUAG
+    tr = prefilter.NativeTrainer(gpu, W, B, seed=1)
+    try:
+        first = None
+        for it in range(300):
+            x, y = _motif_batch(rng, B, W, motif)
+            loss, ms = tr.step(x, y, 1.0, 2e-3)
+            first = loss if first is None else first
+        print(f"loss {first:.3f} -> {loss:.3f}; last step {ms:.2f} ms")
+        assert loss < 0.5 * first
+        wts = tr.weights()
+    finally:
+        tr.close()
+    # held-out windows through the inference kernels: window k of a scan starts at 1 + kW
+    x, y = _motif_batch(rng, 200, W, motif)
+    seq = np.concatenate([[cmfile.DSQ_SENTINEL], x.ravel(), [cmfile.DSQ_SENTINEL]]).astype(np.uint8)
+    f = prefilter.Prefilter(gpu, wts, W)
+    try:
+        d = torch.from_numpy(seq).cuda()
+        logit, _ = f.logits(d.data_ptr(), 1, len(seq) - 2)
+    finally:
+        f.close()
+    acc = float(((logit[0::2][:200] > 0) == (y > 0.5)).mean())
+    print(f"held-out accuracy {acc:.3f}")
+    assert acc > 0.9
