@@ -335,7 +335,7 @@ def run_learned(args, rank, world):
         "config": {"workload": f"Plant_SRP CM stand-in, {args.mb} Mb x 2 strands per step, GC varying 0.35-0.60 "
                                f"per 50 kb segment, "
                                f"{args.hits_per_mb} emitted hits per Mb; filter threshold "
-                               f"{filt.thr:.3f} (validation recall {args.filter_recall or 0.995} of windows with an "
+                               f"{filt.thr:.3f} (validation recall {args.filter_recall or 0.99} of windows with an "
                                f"E <= 0.01 hit); kept regions scanned by CYK QDB1 ({CYK_CUT} bits) -> Inside QDB2 ({INS_CUT} bits)",
                    "l2": "flushed between timed steps (256 MB write)", "parallelism": "1 GPU"},
         "plain_mres_s": round(res / t_plain / 1e6, 3),
@@ -793,7 +793,7 @@ def main():
     ap.add_argument("--filter", default=None, help="learned workload: filter weights (default: the shipped Plant_SRP filter)")
     ap.add_argument("--filter-recall", type=float, default=None,
                     help="learned workload: the filter's stored validation operating point to use "
-                         "(recall of windows holding an E <= 0.01 hit; default: the file's threshold, 0.995)")
+                         "(recall of windows holding an E <= 0.01 hit; default: the file's threshold, 0.99)")
     args = ap.parse_args()
     world = _env_int("WORLD_SIZE", 1)
     rank = _env_int("RANK", 0)

@@ -11,8 +11,10 @@ positive when the plain QDB-CYK scan (cutoff ``CYK_CUT``) followed by the
 QDB2 Inside scan (cutoff ``INS_CUT``) reports a hit in them.  Positives are windows holding sequences emitted by the CM (whole or
 cut at random points) in background of varying GC; negatives are iid
 background and dinucleotide-shuffled positives (the Altschul-Erickson
-doublet-preserving shuffle, restated here).  PyTorch fits the weights
-(``train``); only the exported arrays are used at scan time.
+doublet-preserving shuffle, restated here).  Either PyTorch fits the
+weights (``train``, with batch normalisation folded at export) or the
+hand-written device trainer does (``train_native``, cmgb_filter_trainer_*,
+no batch normalisation); only the exported arrays are used at scan time.
 
 ``filtered_scan`` is the pipeline: filter all windows of both strands, keep
 those above the threshold, merge them into regions and run the plain
@@ -20,6 +22,7 @@ CYK -> Inside scan on the regions only.  The plain scan on everything stays
 the judge of what the filter misses.
 
     python -m infernal_gb300.prefilter train <model> <out.npz> [n_windows] [steps]
+    python -m infernal_gb300.prefilter train-native <model> <out.npz> [n_windows] [steps]
 """
 from __future__ import annotations
 
@@ -403,11 +406,35 @@ def make_windows_parallel(name: str, n: int, seed: int, procs: int = 0) -> List[
     return [w for p in parts for w in p]
 
 
+def train_native(sc, W: int, wins: List[np.ndarray], y: np.ndarray, steps: int, batch: int = 256,
+                 lr: float = 1e-3, seed: int = 0) -> dict:
+    """Trains the network (no batch normalisation) with the device trainer:
+    batches drawn uniformly from wins (Easel dsq windows of 2W residues),
+    positive class weighted by the class ratio, learning rate warmed up over
+    the first 10% of steps and annealed by a cosine; returns the weights."""
+    rng = np.random.default_rng(seed)
+    X = np.stack([w[1:-1] for w in wins]).astype(np.uint8)
+    posw = max(1.0, float((y == 0).sum()) / max(1.0, float((y == 1).sum())))
+    tr = NativeTrainer(sc, W, batch, seed=seed + 1)
+    try:
+        for it in range(steps):
+            idx = rng.integers(0, len(X), batch)
+            warm = max(1, steps // 10)
+            f = (it + 1) / warm if it < warm else 0.5 * (1 + np.cos(np.pi * (it - warm) / max(1, steps - warm)))
+            loss, ms = tr.step(X[idx], y[idx].astype(np.float32), posw, lr * f)
+            if it % 500 == 0:
+                print(f"step {it} loss {loss:.4f} ({ms:.1f} ms)", flush=True)
+        return tr.weights()
+    finally:
+        tr.close()
+
+
 def main(argv):
-    if len(argv) < 4 or argv[1] != "train":
+    if len(argv) < 4 or argv[1] not in ("train", "train-native"):
         print(__doc__)
         return 2
     import torch
+    native = argv[1] == "train-native"
     name, out = argv[2], argv[3]
     nwin = int(argv[4]) if len(argv) > 4 else 60000
     steps = int(argv[5]) if len(argv) > 5 else 4000
@@ -418,16 +445,20 @@ def main(argv):
     y = label_windows(sc, m, wins)
     print(f"{nwin} windows, {int(y.sum())} positive, made+labelled in {time.time() - t0:.0f}s", flush=True)
     ntr = int(0.85 * nwin)
-    X = onehot(wins)
-    net = train(make_net(), X[:ntr], y[:ntr], steps=steps)
-    wts = export(net.float())
-    # threshold: keep >= 99.5% of the validation windows holding a hit with
-    # E <= 0.01 at 4 Mb per search (E_BITS, from the CM's ECMLI calibration)
+    if native:
+        wts = train_native(sc, m.W, wins[:ntr], y[:ntr], steps)
+    else:
+        X = onehot(wins)
+        net = train(make_net(), X[:ntr], y[:ntr], steps=steps)
+        wts = export(net.float())
+    # threshold: keep >= 99% of the validation windows holding a hit with
+    # E <= 0.01 at 4 Mb per search (E_BITS, from the CM's ECMLI calibration):
+    # the loss budget of at most 1% of those hits
     val = reference_logits(wts, wins[ntr:])
     best = label_windows.best[ntr:]
     print(f"validation: {int((y[ntr:] == 1).sum())} positives, {int((best >= E_BITS).sum())} with E <= 0.01", flush=True)
     pos = np.sort(val[best >= E_BITS])
-    thr = float(pos[int(0.005 * len(pos))] - 1e-3) if len(pos) else 0.0
+    thr = float(pos[int(0.01 * len(pos))] - 1e-3) if len(pos) else 0.0
     kept_neg = float((val[y[ntr:] == 0] > thr).mean())
     print(f"threshold {thr:.3f}: validation positives kept {(val[y[ntr:] == 1] > thr).mean():.4f}, "
           f"negatives kept {kept_neg:.4f}", flush=True)
@@ -439,7 +470,8 @@ def main(argv):
         nk = float((val[y[ntr:] == 0] > t).mean())
         points.append((q, t, nk))
         print(f"  recall {q}: threshold {t:.3f}, negatives kept {nk:.4f}", flush=True)
-    save(wts, out, threshold=thr, W=m.W, trained_windows=ntr, recall_points=np.array(points))
+    save(wts, out, threshold=thr, W=m.W, trained_windows=ntr, recall_points=np.array(points),
+         trainer=np.array("cmgb_filter_trainer (device, no batch normalisation)" if native else "PyTorch (batch normalisation folded)"))
     sc.close()
     return 0
 
