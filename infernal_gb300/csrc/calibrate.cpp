@@ -72,13 +72,13 @@ extern "C" int cmgb_Calibrate(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo
   buf.push_back(255);
 
   // scan at a cutoff below the tail; lower it until the tail is collected
-  // (hits above a cutoff do not depend on it: greedy resolution takes the
-  // best scores first)
+  // in 15-bit steps (hits above a cutoff do not depend on it: greedy
+  // resolution takes the best scores first)
   cmgb_hitlist *hl = cmgb_hitlist_create();
   std::vector<float> sc;
   float ms_tot = 0.f;
   int st = CMGB_OK;
-  for (float cut = 0.0f; cut >= -40.0f; cut -= 10.0f) {
+  for (float cut = 0.0f; cut >= -120.0f; cut -= 15.0f) {   // glocal tails can start near -45 bits
     cmgb_hitlist_clear(hl);
     st = cmgb_ScanBatch(c, m, errbuf, algo, CMGB_QDB2_LOOSE, 0, buf.data(), (int64_t) buf.size(), offsets.data(),
                         lengths.data(), nseq, cut, hl, 1, cut, nullptr, nullptr, nullptr, nullptr, nullptr);
@@ -92,7 +92,7 @@ extern "C" int cmgb_Calibrate(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo
   cmgb_hitlist_destroy(hl);
   if (st != CMGB_OK) return st;
   if ((int64_t) sc.size() < ntail)
-    CERR(CMGB_ERANGE, "Calibrate, only %zu hits down to -40 bits; the tail needs %lld", sc.size(), (long long) ntail);
+    CERR(CMGB_ERANGE, "Calibrate, only %zu hits down to -120 bits; the tail needs %lld", sc.size(), (long long) ntail);
 
   // maximum-likelihood exponential with known origin over the best ntail scores
   std::sort(sc.begin(), sc.end(), [](float a, float b) { return a > b; });

@@ -52,3 +52,27 @@ def test_gpu_calibration_matches_cm_file(models, name, algo, tag):
     assert abs(ours[2] - ref[2]) < 0.5
     assert abs(ours[0] - ref[0]) < 0.1
     assert abs(b_ours - b_ref) < 2.0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,algo,tag", [("Vault", "cyk", "ECMGC"), ("Vault", "inside", "ECMGI"),
+                                           ("tRNA", "cyk", "ECMGC")])
+def test_gpu_glocal_calibration(name, algo, tag):
+    """Glocal modes: the model configured without local begins or ends, the
+    tail of 250 hits per Mb (the reference's --gtailn)."""
+    import os
+    from infernal_gb300 import cmfile
+    m = cmfile.load_npz(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", f"{name}.glocal.model.npz"))
+    s = L.Scanner(0)
+    try:
+        ours, ms = s.calibrate(m, algo=algo, total_len=1_600_000, seq_len=100_000, seed=181, tail_per_mb=250)
+    finally:
+        s.close()
+    ref = m.ecm[tag]
+    b_ours, b_ref = L.bits_at_evalue(ours, 0.01, 1e6), L.bits_at_evalue(ref, 0.01, 1e6)
+    print(f"{name} {tag}: lambda {ours[0]:.4f} (file {ref[0]:.4f}), mu {ours[2]:.3f} (file {ref[2]:.3f}), "
+          f"E=0.01 @ 1 Mb: {b_ours:.2f} bits (file {b_ref:.2f}); {ms:.0f} ms of scanning")
+    assert ours[4] == 400 and ours[5] == 1.0
+    assert abs(ours[2] - ref[2]) < 3.0
+    assert abs(ours[0] - ref[0]) < 0.25 * ref[0]
+    assert abs(b_ours - b_ref) < 4.0
