@@ -47,7 +47,7 @@ def _check(sc, ms, seqs, jobs, algo, qdb, cutoffs):
 def test_multi_equals_batch_emulated(emu, models):
     ms = [models["tRNA"], models["Vault"]]
     rng = np.random.default_rng(31)
-    seqs = _seqs(ms, rng, 2, 80, 160)
+    seqs = _seqs(ms, rng, 2, 50, 110)
     jobs = [(a, q) for a in range(2) for q in range(2)]
     _check(emu, ms, seqs, jobs, "cyk", 1, [0.0, 2.0])
 
