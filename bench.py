@@ -227,7 +227,7 @@ def _overlap(a, b):
 
 def run_learned(args, rank, world):
     """Learned pre-filter + batched CYK -> Inside on the kept regions, against
-    the plain scan of everything on the same targets (the hit-loss judge)."""
+    the plain scan of everything on the same targets (which measures the hit loss)."""
     import torch
     from infernal_gb300 import cmfile, lib as L, prefilter
     m = cmfile.load_npz(os.path.join(ROOT, "tests", "golden", "Plant_SRP.model.npz"))
@@ -308,7 +308,7 @@ def run_learned(args, rank, world):
         tot += time.perf_counter() - t0
         kms += k; kept += kp; fhits.append(h)
     clocks = stop_clock_sampler(clk)
-    # the judge: the plain scan of everything on the same steps (timed too)
+    # the hit-loss reference: the plain scan of everything on the same steps (timed too)
     t0 = time.perf_counter()
     phits = [plain_step(inputs[s], [t.data_ptr() for t in dev[s]]) for s in range(args.warmup, nsteps)]
     t_plain = time.perf_counter() - t0
@@ -735,8 +735,9 @@ _clk = {}
 def start_clock_sampler(rank):
     if rank != 0:
         return None
-    os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
-    path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+    import tempfile
+    fd, path = tempfile.mkstemp(prefix="clocks_", suffix=".csv")
+    os.close(fd)
     try:
         fh = open(path, "w")
         p = subprocess.Popen(["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,"
@@ -756,9 +757,12 @@ def stop_clock_sampler(h):
     p.wait()
     fh.close()
     sm, mx, reasons = [], 0, set()
-    for ln in open(path):
+    with open(path) as fh:
+        lines = fh.readlines()
+    os.unlink(path)
+    for ln in lines:
         f = [x.strip() for x in ln.split(",")]
-        if len(f) < 8 or f[0] != str(os.environ.get("CUDA_VISIBLE_DEVICES", "0")).split(",")[0] and len(f) < 8:
+        if len(f) < 8:
             continue
         try:
             sm.append(float(f[1])); mx = max(mx, float(f[2]))

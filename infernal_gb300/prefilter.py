@@ -19,7 +19,7 @@ no batch normalisation); only the exported arrays are used at scan time.
 ``filtered_scan`` is the pipeline: filter all windows of both strands, keep
 those above the threshold, merge them into regions and run the plain
 CYK -> Inside scan on the regions only.  The plain scan on everything stays
-the judge of what the filter misses.
+the measure of what the filter misses.
 
     python -m infernal_gb300.prefilter train <model> <out.npz> [n_windows] [steps]
     python -m infernal_gb300.prefilter train-native <model> <out.npz> [n_windows] [steps]
