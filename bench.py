@@ -746,6 +746,7 @@ def start_clock_sampler(rank):
                               "--format=csv,noheader,nounits", "-lms", "200"], stdout=fh, stderr=subprocess.DEVNULL)
         return (p, fh, path)
     except Exception:
+        os.unlink(path)
         return None
 
 
