@@ -101,3 +101,43 @@ def test_multi_autotuned_shapes_gpu(gpu, models):
     seqs = _seqs(ms, rng, 30, 200, 4000)
     jobs = [(a, q) for a in range(3) for q in range(30)]
     _check(gpu, ms, seqs, jobs, "cyk", 1, [0.0, 0.0, 0.0])
+
+
+def test_multi_and_calibrate_argument_checks(emu, models):
+    """Contract violations return an error status before any device work."""
+    import ctypes
+    m = models["tRNA"]
+    seqs = [cmfile.digitize("ACGU" * 30)]
+    with pytest.raises(L.ScanError):                       # model index out of range
+        emu.scan_multi([m], seqs, jobs=[(1, 0)], algo="cyk", qdbidx=1)
+    with pytest.raises(L.ScanError):                       # sequence index out of range
+        emu.scan_multi([m], seqs, jobs=[(0, 3)], algo="cyk", qdbidx=1)
+    with pytest.raises(L.ScanError):                       # band set out of range
+        emu.scan_multi([m], seqs, algo="cyk", qdbidx=3)
+    # a sequence that does not fit its buffer (sentinel, residues, sentinel)
+    lib = emu.lib
+    mh = emu.model(m)
+    buf = np.ascontiguousarray(seqs[0])
+    offs, lens = np.array([0], np.int64), np.array([len(buf)], np.int64)
+    jm, js = np.zeros(1, np.int32), np.zeros(1, np.int32)
+    cut = np.zeros(1, np.float32)
+    harr = (ctypes.c_void_p * 1)(mh.value)
+    err = ctypes.create_string_buffer(256)
+    st = lib.cmgb_ScanMulti(emu._ctx, harr, 1, cut.ctypes.data, err, 0, 1, buf.ctypes.data, len(buf), offs.ctypes.data,
+                            lens.ctypes.data, 1, jm.ctypes.data, js.ctypes.data, 1, None, 1, 0.0, None, None, None, None)
+    assert st == 10 and b"outside the buffer" in err.value
+    # calibration: sizes and algorithm (float Inside is not a calibrated mode)
+    e2 = L.ExpInfo()
+    for algo, total, seqlen, tail in ((0, 500, 100, 750), (0, 10_000, 50, 750), (2, 10_000, 1000, 750), (0, 10_000, 1000, 0)):
+        st = lib.cmgb_Calibrate(emu._ctx, mh, err, algo, total, seqlen, 1, tail, ctypes.byref(e2), None)
+        assert st == 11, (algo, total, seqlen, tail)
+
+
+def test_trainer_fails_loudly_without_a_gpu(emu):
+    """The emulation build has no tensor cores: the trainer refuses instead of
+    falling back to anything."""
+    import ctypes
+    h = ctypes.c_void_p()
+    err = ctypes.create_string_buffer(256)
+    st = emu.lib.cmgb_filter_trainer_create(emu._ctx, 64, 8, 1, ctypes.byref(h), err)
+    assert st == 30 and not h.value and b"not available" in err.value
