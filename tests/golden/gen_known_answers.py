@@ -1,0 +1,50 @@
+"""Stores the targets of the reference's known-answer sensitivity test.
+
+Run in a container where the reference tree exists (default /root/reference):
+
+    python tests/golden/gen_known_answers.py [reference_root]
+
+testsuite/itest6-sensitivity.pl runs cmsearch with three calibrated CMs on
+five test-suite sequences and checks the coordinates of the top hit.  This
+script digitizes those sequences into ``known_answers.npz`` and writes the
+cases (model, target, search options, expected top hit) to
+``known_answers.json``; the models are in panel/ (gen_panel.py).
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from infernal_gb300 import cmfile  # noqa: E402
+
+# (model, target file, fbeta, beta, expected (sfrom, sto), line of the check in testsuite/itest6-sensitivity.pl)
+CASES = [
+    ("tRNA1415G", "mito-ascaris.fa", None, None, (4169, 4230), 112),
+    ("srp-euk", "ffs-frag.fa", 1e-2, 1e-4, (15714, 15739), 150),
+    ("srp-euk", "ffs-ecoli.fa", 1e-2, 1e-4, (43, 68), 158),
+    ("rnaseP-eubact", "rnaseP-frag.fa", None, None, (10920, 10580), 196),
+    ("rnaseP-eubact", "rnaseP-bsu.fa", None, None, (43, 383), 205),
+]
+
+
+def main(ref_root="/root/reference"):
+    arrays, meta = {}, []
+    for model, fa, fbeta, beta, (a, b), line in CASES:
+        seq = cmfile.read_fasta(os.path.join(ref_root, "testsuite", fa))[0][1].upper().replace("T", "U")
+        arrays["dsq." + fa] = cmfile.digitize(seq)
+        meta.append(dict(model=model, target=fa, fbeta=fbeta, beta=beta, sfrom=a, sto=b,
+                         source=f"testsuite/itest6-sensitivity.pl:{line}"))
+    np.savez_compressed(os.path.join(HERE, "known_answers.npz"), **arrays)
+    with open(os.path.join(HERE, "known_answers.json"), "w") as fh:
+        json.dump(meta, fh, indent=1)
+
+
+if __name__ == "__main__":
+    main(*sys.argv[1:])
