@@ -48,7 +48,7 @@ def test_multi_equals_batch_emulated(emu, models):
     ms = [models["tRNA"], models["Vault"]]
     rng = np.random.default_rng(31)
     seqs = _seqs(ms, rng, 2, 50, 110)
-    jobs = [(a, q) for a in range(2) for q in range(2)]
+    jobs = [(0, 0), (1, 1), (1, 0)]
     _check(emu, ms, seqs, jobs, "cyk", 1, [0.0, 2.0])
 
 

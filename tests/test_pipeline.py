@@ -1,0 +1,70 @@
+"""The --nohmm search pipeline (infernal_gb300/pipeline.py): survivor-window
+rules of pli_cyk_seq_filter, E-value arithmetic, and the reference's
+known answers through the whole pipeline (CYK filter at F6, windows, final
+Inside, E-values): the short SRP case on the CPU through the emulated
+kernels, every case on the GPU."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from infernal_gb300 import cmfile, lib as L, pipeline
+
+HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def test_cyk_windows_rules():
+    W, L_ = 100, 10_000
+    # hit (start, stop): window [stop - 99, start + 99]
+    assert pipeline.cyk_windows([(500, 560)], W, L_) == [(461, 599)]
+    # the second window (from its stop: 650 - 99 = 551) starts inside the first: merged, end from the second hit
+    assert pipeline.cyk_windows([(600, 650), (500, 560)], W, L_) == [(461, 699)]
+    # the second window starts after the first ends: apart
+    assert pipeline.cyk_windows([(700, 760), (500, 560)], W, L_) == [(461, 599), (661, 799)]
+    # adjacent but not overlapping windows stay apart
+    assert pipeline.cyk_windows([(500, 560), (739, 800)], W, L_) == [(461, 599), (701, 838)]
+    # clipped at the sequence ends
+    assert pipeline.cyk_windows([(5, 40), (9960, 9990)], W, L_) == [(1, 104), (9891, 10_000)]
+
+
+def _known():
+    with open(os.path.join(HERE, "known_answers.json")) as fh:
+        meta = json.load(fh)
+    arrays = dict(np.load(os.path.join(HERE, "known_answers.npz")))
+    return meta, arrays
+
+
+def _model(c):
+    m = cmfile.load_npz(os.path.join(HERE, "panel", f"{c['model']}.model.npz"))
+    if c["fbeta"] is not None:
+        d1, x1, d2, x2, _ = cmfile.qdb_bands(m, beta1=c["fbeta"], beta2=c["beta"], beta_W=1e-7)
+        m.dmin1, m.dmax1, m.dmin2, m.dmax2 = d1, x1, d2, x2
+    return m
+
+
+# itest6-sensitivity.pl's E-value thresholds per model
+E_OF = {"tRNA1415G": 1e-3, "srp-euk": 0.01, "rnaseP-eubact": 0.1}
+
+
+def test_pipeline_known_answer_emulated(emu):
+    meta, arrays = _known()
+    c = [x for x in meta if x["target"] == "ffs-ecoli.fa"][0]
+    m = _model(c)
+    hits = pipeline.search(emu, m, [(c["target"], arrays["dsq." + c["target"]])], E=E_OF[c["model"]], toponly=True)
+    assert hits and (hits[0].sfrom, hits[0].sto) == (c["sfrom"], c["sto"])
+    assert hits[0].evalue <= E_OF[c["model"]] and hits[0].strand == "+"
+
+
+@pytest.mark.gpu
+def test_pipeline_known_answers_gpu():
+    meta, arrays = _known()
+    s = L.Scanner(0)
+    try:
+        for c in meta:
+            m = _model(c)
+            hits = pipeline.search(s, m, [(c["target"], arrays["dsq." + c["target"]])], E=E_OF[c["model"]])
+            assert hits, c["source"]
+            assert (hits[0].sfrom, hits[0].sto) == (c["sfrom"], c["sto"]), (c["source"], hits[:2])
+    finally:
+        s.close()
