@@ -95,15 +95,10 @@ def make_step_input(model_glob, step, mb, seed=20261203, hits_per_mb=2.0, gc=0.4
 
 
 def windows_from_hits(hits, W, L):
-    """Pads survivors by W-1 and merges overlaps (src/cm_pipeline.c:3566-3601)."""
-    ws = []
-    for h in sorted(hits, key=lambda h: h[0]):
-        a, b = max(1, h[1] - (W - 1)), min(L, h[0] + (W - 1))
-        if ws and a <= ws[-1][1] + 1:
-            ws[-1][1] = max(ws[-1][1], b)
-        else:
-            ws.append([a, b])
-    return ws
+    """Survivor windows of the CYK filter: hits padded by W-1 and merged as
+    pli_cyk_seq_filter does (src/cm_pipeline.c:3566-3601)."""
+    from infernal_gb300 import pipeline
+    return [list(w) for w in pipeline.cyk_windows(hits, W, L)]
 
 
 def make_reads(model_glob, step, nreads, seed=20261204):
