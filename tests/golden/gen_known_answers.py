@@ -8,7 +8,9 @@ testsuite/itest6-sensitivity.pl runs cmsearch with three calibrated CMs on
 five test-suite sequences and checks the coordinates of the top hit.  This
 script digitizes those sequences into ``known_answers.npz`` and writes the
 cases (model, target, search options, expected top hit) to
-``known_answers.json``; the models are in panel/ (gen_panel.py).
+``known_answers.json``; the models are in panel/ (gen_panel.py).  It also
+stores the truncated-mode known answer of testsuite/itest7-trunc.pl (Vault on
+tremitted-Vault.fa) in ``known_answers_trunc.json``.
 """
 from __future__ import annotations
 
@@ -34,6 +36,13 @@ CASES = [
 ]
 
 
+# truncated mode (testsuite/itest7-trunc.pl:56-67): Vault on three truncated
+# emitted sequences, default cmsearch -E 0.01: exactly two hits,
+# (sequence, sfrom, sto, printed score)
+TR_FILE = "tremitted-Vault.fa"
+TR_HITS = [("Vault-1", 1, 63, 33.2), ("Vault-2", 1, 59, 25.5)]
+
+
 def main(ref_root="/root/reference"):
     arrays, meta = {}, []
     for model, fa, fbeta, beta, (a, b), line in CASES:
@@ -41,9 +50,16 @@ def main(ref_root="/root/reference"):
         arrays["dsq." + fa] = cmfile.digitize(seq)
         meta.append(dict(model=model, target=fa, fbeta=fbeta, beta=beta, sfrom=a, sto=b,
                          source=f"testsuite/itest6-sensitivity.pl:{line}"))
+    tr = cmfile.read_fasta(os.path.join(ref_root, "testsuite", TR_FILE))
+    for name, seq in tr:
+        arrays[f"trdsq.{name}"] = cmfile.digitize(seq.upper().replace("T", "U"))
+    trunc = dict(model="Vault", target=TR_FILE, names=[n for n, _ in tr], E=0.01,
+                 hits=[list(h) for h in TR_HITS], source="testsuite/itest7-trunc.pl:56-67")
     np.savez_compressed(os.path.join(HERE, "known_answers.npz"), **arrays)
     with open(os.path.join(HERE, "known_answers.json"), "w") as fh:
         json.dump(meta, fh, indent=1)
+    with open(os.path.join(HERE, "known_answers_trunc.json"), "w") as fh:
+        json.dump(trunc, fh, indent=1)
 
 
 if __name__ == "__main__":

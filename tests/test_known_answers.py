@@ -10,7 +10,13 @@ W stays the file's).  The reference's default pipeline (tRNA1415G,
 rnaseP-eubact) filters with HMMs first and its final stage uses HMM bands;
 its top hits are the QDB scan's top hits too.  CPU: the oracle over a 3 kb
 window around each expected hit on its strand (whole targets take minutes on
-one core); GPU: whole targets, both strands, every case."""
+one core); GPU: whole targets, both strands, every case.
+
+Truncated mode (testsuite/itest7-trunc.pl): Vault on three truncated
+emitted reads must give exactly two hits with E <= 0.01, at the reference's
+coordinates; the oracle and the GPU run the truncated Inside scanner over
+passes 2-4 and both strands, and the emulated kernel matches the oracle on
+the reads and passes that report the hits."""
 import json
 import os
 
@@ -81,3 +87,69 @@ def test_known_answer_top_hits_gpu():
             assert top[1:] == (c["sfrom"], c["sto"]), (c["source"], top)
     finally:
         s.close()
+
+
+def _trunc_hits(scan):
+    """Per read: the best hit with E <= 0.01 over both strands and the
+    truncated passes 2, 3 and 4 (5' only, 3' only, 5' and 3'), as the
+    default pipeline runs them on reads that are terminal at both ends."""
+    with open(os.path.join(HERE, "known_answers_trunc.json")) as fh:
+        c = json.load(fh)
+    _, arrays = _cases()
+    m = cmfile.load_npz(os.path.join(HERE, f"{c['model']}.model.npz"))
+    reads = [arrays["trdsq." + n] for n in c["names"]]
+    Z = 2 * sum(len(d) - 2 for d in reads)
+    li = m.ecm["ECMLI"]
+    found = []
+    for name, dsq in zip(c["names"], reads):
+        n = len(dsq) - 2
+        best = None
+        for strand, d in (("+", dsq), ("-", emit.revcomp_dsq(dsq))):
+            for p in (2, 3, 4):
+                for h in scan(m, d, n, p):
+                    if L.evalue(li, h[4], Z) <= c["E"] and (best is None or h[4] > best[3]):
+                        best = (name,) + _strand_coords(h, n, strand) + (h[4],)
+        if best:
+            found.append(best)
+    return c, found
+
+
+def _check_trunc(c, found):
+    # exactly the reference's hits; scores within 0.15 bits of the printed
+    # one-decimal scores (the reference's default pipeline scores truncated
+    # hits with HMM-banded Inside, these are QDB-banded: 33.10 vs 33.2,
+    # 25.46 vs 25.5)
+    assert [f[:3] for f in found] == [tuple(h[:3]) for h in c["hits"]], found
+    for f, h in zip(found, c["hits"]):
+        assert abs(f[3] - h[3]) < 0.15, (f, h)
+
+
+def test_known_answer_truncated_oracle():
+    c, found = _trunc_hits(lambda m, d, n, p: oracle.tr_scan(m, d, 1, n, algo="trinside", qdbidx=2, pass_idx=p,
+                                                             cutoff=0.0, env_cutoff=0.0)[0])
+    _check_trunc(c, found)
+
+
+def test_known_answer_truncated_emulated(emu):
+    """The emulated truncated kernel gives the oracle's hit list, bit for bit,
+    on the two reads that hold the known hits, at the passes that report
+    them (5'-truncated for Vault-1, 3'-truncated for Vault-2)."""
+    _, arrays = _cases()
+    m = cmfile.load_npz(os.path.join(HERE, "Vault.model.npz"))
+    for name, p in (("Vault-1", 2), ("Vault-2", 3)):
+        d = arrays["trdsq." + name]
+        n = len(d) - 2
+        r = emu.tr_scan(m, d, 1, n, algo="trinside", qdbidx=2, pass_idx=p, cutoff=0.0, env_cutoff=0.0)
+        o = oracle.tr_scan(m, d, 1, n, algo="trinside", qdbidx=2, pass_idx=p, cutoff=0.0, env_cutoff=0.0)
+        assert r.hits == o[0] and r.hits, name
+
+
+@pytest.mark.gpu
+def test_known_answer_truncated_gpu():
+    s = L.Scanner(0)
+    try:
+        c, found = _trunc_hits(lambda m, d, n, p: s.tr_scan(m, d, 1, n, algo="trinside", qdbidx=2, pass_idx=p,
+                                                            cutoff=0.0, env_cutoff=0.0).hits)
+    finally:
+        s.close()
+    _check_trunc(c, found)
