@@ -28,6 +28,16 @@ def test_header_and_binding_agree():
     assert _declared_functions() == set(L.EXPORTS)
 
 
+def test_header_compiles_as_c_and_cpp(tmp_path):
+    """The C ABI header stands alone: pedantic C99 (Infernal's C) and C++."""
+    import subprocess
+    for ext, cmd in (("c", ["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror"]),
+                     ("cpp", ["g++", "-std=c++11", "-Wall", "-Wextra", "-Werror"])):
+        src = tmp_path / f"h.{ext}"
+        src.write_text('#include "infernal_gb300.h"\nint main(void) { return 0; }\n')
+        subprocess.check_call(cmd + ["-fsyntax-only", "-I", os.path.join(ROOT, "include"), str(src)])
+
+
 @pytest.fixture(scope="module")
 def built_lib():
     import __graft_entry__ as g
