@@ -47,7 +47,7 @@ def _check(sc, ms, seqs, jobs, algo, qdb, cutoffs):
 def test_multi_equals_batch_emulated(emu, models):
     ms = [models["tRNA"], models["Vault"]]
     rng = np.random.default_rng(31)
-    seqs = _seqs(ms, rng, 2, 50, 110)
+    seqs = _seqs(ms, rng, 2, 40, 80)
     jobs = [(0, 0), (1, 1), (1, 0)]
     _check(emu, ms, seqs, jobs, "cyk", 1, [0.0, 2.0])
 
@@ -55,7 +55,7 @@ def test_multi_equals_batch_emulated(emu, models):
 def test_multi_sparse_jobs_inside_emulated(emu, models):
     ms = [models["tRNA"], models["Vault"]]
     rng = np.random.default_rng(32)
-    seqs = _seqs(ms, rng, 3, 60, 120)
+    seqs = _seqs(ms, rng, 3, 40, 80)
     _check(emu, ms, seqs, [(1, 2), (0, 0)], "inside", 2, [0.0, 0.0])
 
 
