@@ -109,7 +109,8 @@ typedef struct {
   const int8_t *stid;      /* cm->stid[v]   */
   const int   *cfirst;     /* cm->cfirst[v] */
   const int   *cnum;       /* cm->cnum[v]   */
-  const int   *dmin1, *dmax1, *dmin2, *dmax2;  /* cm->qdbinfo bands */
+  const int   *dmin1, *dmax1, *dmin2, *dmax2;  /* cm->qdbinfo bands; a band set may be NULL (both arrays):
+                                                  scans then accept qdbidx 0 and the other set only */
   const float *tsc;        /* [M*6]     cm->tsc      */
   const float *oesc;       /* [M*Kp*Kp] cm->oesc     */
   const float *endsc;      /* [M]       cm->endsc    */

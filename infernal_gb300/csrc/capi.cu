@@ -326,6 +326,12 @@ extern "C" int cmgb_model_create(cmgb_ctx *c, const cmgb_model_desc *d, cmgb_mod
   *ret = nullptr;
   if (!c || !d) ERRF(CMGB_EINVAL, "cmgb_model_create: NULL argument");
   if (d->M < 2 || d->W < 1 || d->K != 4 || d->Kp != 18) ERRF(CMGB_EINCOMPAT, "cmgb_model_create: unsupported model shape (M=%d W=%d K=%d Kp=%d)", d->M, d->W, d->K, d->Kp);
+  if (!d->sttype || !d->stid || !d->cfirst || !d->cnum || !d->tsc || !d->itsc || !d->oesc || !d->ioesc || !d->endsc ||
+      !d->beginsc || !d->iendsc || !d->ibeginsc || !d->null)
+    ERRF(CMGB_EINVAL, "cmgb_model_create: a required table of the model description is NULL");
+  // band sets are optional (a model without query-dependent bands scans with qdbidx 0 only)
+  if (!d->dmin1 != !d->dmax1 || !d->dmin2 != !d->dmax2)
+    ERRF(CMGB_EINVAL, "cmgb_model_create: a band set needs both its dmin and its dmax array");
   const int M = d->M, KK = d->Kp * d->Kp;
   std::unique_ptr<cmgb_model> m(new cmgb_model);
   m->ctx = c; m->M = M; m->W = d->W; m->K = d->K; m->Kp = d->Kp; m->flags = d->flags;
@@ -333,8 +339,8 @@ extern "C" int cmgb_model_create(cmgb_ctx *c, const cmgb_model_desc *d, cmgb_mod
   m->null3_omega = d->null3_omega;
   m->sttype.assign(d->sttype, d->sttype + M); m->stid.assign(d->stid, d->stid + M);
   m->cfirst.assign(d->cfirst, d->cfirst + M); m->cnum.assign(d->cnum, d->cnum + M);
-  m->dmin1.assign(d->dmin1, d->dmin1 + M); m->dmax1.assign(d->dmax1, d->dmax1 + M);
-  m->dmin2.assign(d->dmin2, d->dmin2 + M); m->dmax2.assign(d->dmax2, d->dmax2 + M);
+  if (d->dmin1) { m->dmin1.assign(d->dmin1, d->dmin1 + M); m->dmax1.assign(d->dmax1, d->dmax1 + M); }
+  if (d->dmin2) { m->dmin2.assign(d->dmin2, d->dmin2 + M); m->dmax2.assign(d->dmax2, d->dmax2 + M); }
   m->tsc.assign(d->tsc, d->tsc + 6 * M); m->itsc.assign(d->itsc, d->itsc + 6 * M);
   m->endsc.assign(d->endsc, d->endsc + M); m->beginsc.assign(d->beginsc, d->beginsc + M);
   m->iendsc.assign(d->iendsc, d->iendsc + M); m->ibeginsc.assign(d->ibeginsc, d->ibeginsc + M);
@@ -345,7 +351,8 @@ extern "C" int cmgb_model_create(cmgb_ctx *c, const cmgb_model_desc *d, cmgb_mod
   cmgb_model_desc &D = m->desc;
   D.M = M; D.W = d->W; D.K = d->K; D.Kp = d->Kp; D.flags = d->flags;
   D.sttype = m->sttype.data(); D.stid = m->stid.data(); D.cfirst = m->cfirst.data(); D.cnum = m->cnum.data();
-  D.dmin1 = m->dmin1.data(); D.dmax1 = m->dmax1.data(); D.dmin2 = m->dmin2.data(); D.dmax2 = m->dmax2.data();
+  D.dmin1 = m->dmin1.empty() ? nullptr : m->dmin1.data(); D.dmax1 = m->dmax1.empty() ? nullptr : m->dmax1.data();
+  D.dmin2 = m->dmin2.empty() ? nullptr : m->dmin2.data(); D.dmax2 = m->dmax2.empty() ? nullptr : m->dmax2.data();
   D.tsc = m->tsc.data(); D.itsc = m->itsc.data(); D.endsc = m->endsc.data(); D.beginsc = m->beginsc.data();
   D.iendsc = m->iendsc.data(); D.ibeginsc = m->ibeginsc.data();
   D.el_selfsc = d->el_selfsc; D.iel_selfsc = d->iel_selfsc;
@@ -413,6 +420,8 @@ extern "C" void cmgb_hitlist_clear(cmgb_hitlist *hl) { if (hl) hl->h.clear(); }
 static int get_plan(cmgb_model *m, int qdbidx, int alg, DevPlan **ret, char *errbuf)
 {
   cmgb_ctx *c = m->ctx;
+  if ((qdbidx == 1 && m->dmin1.empty()) || (qdbidx == 2 && m->dmin2.empty()))
+    ERRF(CMGB_EINCOMPAT, "the model was created without band set %d (qdbidx %d)", qdbidx, qdbidx);
   DevPlan &dp = m->plans[qdbidx][alg];
   // shape: the context's explicit choice, else the autotuner's, else 16 rows in shared memory
   const int wantT = c->tile_rows ? c->tile_rows : (m->tuned_T[qdbidx][alg] ? m->tuned_T[qdbidx][alg] : 16);
@@ -648,6 +657,8 @@ static int tr_cand_reserve(cmgb_ctx *c, int64_t need, int *cap, char *errbuf)
 
 static int get_tr_plan(cmgb_model *m, int qdbidx, int alg, DevTrPlan **ret, char *errbuf)
 {
+  if ((qdbidx == 1 && m->dmin1.empty()) || (qdbidx == 2 && m->dmin2.empty()))
+    ERRF(CMGB_EINCOMPAT, "the model was created without band set %d (qdbidx %d)", qdbidx, qdbidx);
   cmgb_ctx *c = m->ctx;
   DevTrPlan &dp = m->trplans[qdbidx][alg];
   const int wantT = c->tile_rows ? c->tile_rows : 16;
