@@ -1,6 +1,7 @@
 """Exhaustive check on hand-specified tiny CMs, after the reference's
 "brute" integration test (src/itest_brute.c): a four-node model (ROOT, MATL,
-MATL, END; ten states) with random parameters, configured in global mode.
+MATL, END; ten states) with random parameters, configured in global mode and in local mode (local
+begins into the MATL nodes, a local end through EL).
 Every parse of every subsequence of short random targets is scored by a
 top-down recursion written from the model's definition -- the maximum over
 parses (CYK) in float32 with the scanners' two-term additions, the sum over
@@ -28,7 +29,7 @@ CFIRST = [1, 1, 2, 5, 5, 5, 8, 8, 8, -1]
 CNUM = [4, 4, 3, 3, 3, 3, 2, 2, 2, 0]
 
 
-def tiny_cm(rng, W=10):
+def tiny_cm(rng, W=10, local=False):
     m = cmfile.CMModel(name="brute", M=10, nodes=4, clen=2, W=W)
     m.sttype = np.array(STTYPE, np.int8)
     m.stid = np.array(STID, np.int8)
@@ -47,14 +48,20 @@ def tiny_cm(rng, W=10):
     m.null = np.full(4, 0.25, np.float32)
     m.null3_omega = np.float32(2.0 ** -16)
     m.dmin1 = m.dmax1 = m.dmin2 = m.dmax2 = None
-    return cmfile.configure(m, local=False)
+    m.el_selfsc = np.float32(math.log2(0.94))       # EL self-loop (local ends emit through EL)
+    return cmfile.configure(m, local=local)
 
 
 def brute(m, x):
     """Best root score over all subsequences x[i..j] (1-based, j >= i):
-    (CYK max over parses in float32, Inside log2-sum over parses in double)."""
+    (CYK max over parses in float32, Inside log2-sum over parses in double).
+    Local mode: a state with a local end may leave for EL, which emits the
+    rest of its subsequence at el_selfsc per residue (after the state's own
+    emission); a parse may start at any state with a local begin (the best
+    begin is taken by max, also for Inside, as the scanners do)."""
     f32 = np.float32
     tsc, esc = m.tsc, m.oesc
+    el, endsc, beginsc = f32(m.el_selfsc), m.endsc, m.beginsc
 
     @functools.lru_cache(maxsize=None)
     def cyk(v, i, j):          # parse of x[i..j] (empty when i > j) rooted at state v
@@ -77,6 +84,9 @@ def brute(m, x):
             if c > IMP / 2:
                 s = f32(c + tsc[v, o])
                 best = s if s > best else best
+        if endsc[v] > IMP / 2:                       # local end: EL emits the remaining residues
+            s = f32(f32(el * f32(max(0, cj - ci + 1))) + endsc[v])
+            best = s if s > best else best
         if best <= IMP / 2:
             return f32(IMP)
         return f32(best + e) if e is not None else best
@@ -97,22 +107,38 @@ def brute(m, x):
         else:
             ci, cj, e = i, j, 0.0
         terms = [ins(CFIRST[v] + o, ci, cj) + float(tsc[v, o]) for o in range(CNUM[v])]
-        terms = [a for a in terms if a > -math.inf]
+        if endsc[v] > IMP / 2:
+            terms.append(float(el) * max(0, cj - ci + 1) + float(endsc[v]))
+        terms = [a for a in terms if a > IMP / 2]
         if not terms:
             return -math.inf
         mx = max(terms)
         return mx + math.log2(sum(2.0 ** (a - mx) for a in terms)) + e
 
+    begins = [v for v in range(1, len(STTYPE)) if beginsc[v] > IMP / 2]
+
+    def root_c(i, j):
+        b = cyk(0, i, j)
+        for v in begins:
+            c = cyk(v, i, j)
+            if c > IMP / 2:
+                s = f32(c + beginsc[v])
+                b = s if s > b else b
+        return b
+
+    def root_i(i, j):
+        return max([ins(0, i, j)] + [ins(v, i, j) + float(beginsc[v]) for v in begins])
+
     n = len(x)
-    best_c = max(cyk(0, i, j) for j in range(1, n + 1) for i in range(1, j + 1))
-    best_i = max(ins(0, i, j) for j in range(1, n + 1) for i in range(1, j + 1))
+    best_c = max(root_c(i, j) for j in range(1, n + 1) for i in range(1, j + 1))
+    best_i = max(root_i(i, j) for j in range(1, n + 1) for i in range(1, j + 1))
     return float(best_c), best_i
 
 
-def _cases(n_models=12):
-    rng = np.random.default_rng(181)
+def _cases(n_models=12, local=False):
+    rng = np.random.default_rng(181 + int(local))
     for k in range(n_models):
-        m = tiny_cm(rng)
+        m = tiny_cm(rng, local=local)
         x = [int(a) for a in rng.integers(0, 4, int(rng.integers(3, 9)))]
         yield k, m, x
 
@@ -121,8 +147,9 @@ def _dsq(x):
     return np.array([cmfile.DSQ_SENTINEL] + x + [cmfile.DSQ_SENTINEL], np.uint8)
 
 
-def test_brute_oracle():
-    for k, m, x in _cases():
+@pytest.mark.parametrize("local", [False, True])
+def test_brute_oracle(local):
+    for k, m, x in _cases(local=local):
         bc, bi = brute(m, x)
         d = _dsq(x)
         c = oracle.scan(m, d, 1, len(x), algo="cyk", qdbidx=0, cutoff=1e30, env_cutoff=1e30)[3]
@@ -132,8 +159,9 @@ def test_brute_oracle():
         assert abs(i - bi) < 0.02 and abs(f - bi) < 0.01, (k, i, f, bi)
 
 
-def test_brute_emulated_kernel(emu):
-    for k, m, x in list(_cases())[:4]:
+@pytest.mark.parametrize("local", [False, True])
+def test_brute_emulated_kernel(emu, local):
+    for k, m, x in list(_cases(local=local))[:4]:
         bc, bi = brute(m, x)
         d = _dsq(x)
         c = emu.scan(m, d, 1, len(x), algo="cyk", qdbidx=0, cutoff=1e30, env_cutoff=1e30).sc
@@ -143,10 +171,11 @@ def test_brute_emulated_kernel(emu):
 
 
 @pytest.mark.gpu
-def test_brute_gpu():
+@pytest.mark.parametrize("local", [False, True])
+def test_brute_gpu(local):
     s = L.Scanner(0)
     try:
-        for k, m, x in _cases():
+        for k, m, x in _cases(local=local):
             bc, bi = brute(m, x)
             d = _dsq(x)
             c = s.scan(m, d, 1, len(x), algo="cyk", qdbidx=0, cutoff=1e30, env_cutoff=1e30).sc
