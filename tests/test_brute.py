@@ -1,12 +1,16 @@
 """Exhaustive check on hand-specified tiny CMs, after the reference's
-"brute" integration test (src/itest_brute.c): a four-node model (ROOT, MATL,
-MATL, END; ten states) with random parameters, configured in global mode and in local mode (local
-begins into the MATL nodes, a local end through EL).
+"brute" integration test (src/itest_brute.c): hand-specified models with
+random parameters -- four nodes (ROOT, MATL, MATL, END; ten states), and
+eight nodes with a bifurcation and a base pair (ROOT, BIF, BEGL, MATP, END,
+BEGR, MATL, END; eighteen states) -- configured in global mode and in local
+mode (local begins into the internal nodes, local ends through EL).
 Every parse of every subsequence of short random targets is scored by a
 top-down recursion written from the model's definition -- the maximum over
 parses (CYK) in float32 with the scanners' two-term additions, the sum over
-parses (Inside) in exact double log-space -- and the best root score over
-all subsequences is compared with the scanners' best score: CYK exactly,
+parses (Inside) in exact double log-space, except that an empty subsequence
+at an S or D state takes the maximum of its alternatives, which is how the
+reference's matrix initialisation defines those cells -- and the best root
+score over all subsequences is compared with the scanners' best score: CYK exactly,
 integer and float Inside within the log-sum tables' error.  The oracle and
 the emulated kernel run on the CPU, the kernels on the GPU."""
 import functools
@@ -18,32 +22,57 @@ import pytest
 import oracle
 from infernal_gb300 import cmfile, lib as L
 
-D, ML, IL, IR, S, E = cmfile.D_st, cmfile.ML_st, cmfile.IL_st, cmfile.IR_st, cmfile.S_st, cmfile.E_st
+D, MP, ML, MR, IL, IR, S, E, B = (cmfile.D_st, cmfile.MP_st, cmfile.ML_st, cmfile.MR_st, cmfile.IL_st, cmfile.IR_st,
+                                  cmfile.S_st, cmfile.E_st, cmfile.B_st)
 IMP = float(np.float32(cmfile.IMPOSSIBLE))
+ND = cmfile
 
-# states: ROOT (S IL IR), MATL (ML D IL), MATL (ML D IL), END (E); children of
-# a state are cfirst .. cfirst + cnum - 1 (inserts list themselves first)
-STTYPE = [S, IL, IR, ML, D, IL, ML, D, IL, E]
-STID = [0, 1, 2, 12, 13, 14, 12, 13, 14, 18]      # ROOT_S ROOT_IL ROOT_IR MATL_ML MATL_D MATL_IL ... END_E
-CFIRST = [1, 1, 2, 5, 5, 5, 8, 8, 8, -1]
-CNUM = [4, 4, 3, 3, 3, 3, 2, 2, 2, 0]
+# Topologies: per state (type, unique id, node index, cfirst, cnum); children
+# of a state are cfirst .. cfirst + cnum - 1 (inserts list themselves first);
+# a B state's cfirst is its BEGL_S and its cnum its BEGR_S.
+TOPOLOGIES = {
+    # ROOT (S IL IR), MATL (ML D IL), MATL (ML D IL), END (E)
+    "matl": dict(
+        states=[(S, 0, 0, 1, 4), (IL, 1, 0, 1, 4), (IR, 2, 0, 2, 3),
+                (ML, 12, 1, 5, 3), (D, 13, 1, 5, 3), (IL, 14, 1, 5, 3),
+                (ML, 12, 2, 8, 2), (D, 13, 2, 8, 2), (IL, 14, 2, 8, 2),
+                (E, 18, 3, -1, 0)],
+        nodes=[ND.ROOT_nd, ND.MATL_nd, ND.MATL_nd, ND.END_nd], clen=2),
+    # ROOT (S IL IR), BIF (B), BEGL (S), MATP (MP ML MR D IL IR), END (E),
+    # BEGR (S IL), MATL (ML D IL), END (E)
+    "bif": dict(
+        states=[(S, 0, 0, 1, 3), (IL, 1, 0, 1, 3), (IR, 2, 0, 2, 2),
+                (B, 19, 1, 4, 12),
+                (S, 3, 2, 5, 4),
+                (MP, 6, 3, 9, 3), (ML, 7, 3, 9, 3), (MR, 8, 3, 9, 3), (D, 9, 3, 9, 3), (IL, 10, 3, 9, 3), (IR, 11, 3, 10, 2),
+                (E, 18, 4, -1, 0),
+                (S, 4, 5, 13, 3), (IL, 5, 5, 13, 3),
+                (ML, 12, 6, 16, 2), (D, 13, 6, 16, 2), (IL, 14, 6, 16, 2),
+                (E, 18, 7, -1, 0)],
+        nodes=[ND.ROOT_nd, ND.BIF_nd, ND.BEGL_nd, ND.MATP_nd, ND.END_nd, ND.BEGR_nd, ND.MATL_nd, ND.END_nd], clen=3),
+}
 
 
-def tiny_cm(rng, W=10, local=False):
-    m = cmfile.CMModel(name="brute", M=10, nodes=4, clen=2, W=W)
-    m.sttype = np.array(STTYPE, np.int8)
-    m.stid = np.array(STID, np.int8)
-    m.cfirst = np.array(CFIRST, np.int32)
-    m.cnum = np.array(CNUM, np.int32)
-    m.ndidx = np.array([0, 0, 0, 1, 1, 1, 2, 2, 2, 3], np.int32)
-    m.ndtype = np.array([cmfile.ROOT_nd, cmfile.MATL_nd, cmfile.MATL_nd, cmfile.END_nd], np.int8)
-    m.nodemap = np.array([0, 3, 6, 9], np.int32)
-    m.t = np.zeros((10, 6), np.float32)
-    m.e = np.zeros((10, 16), np.float32)
-    for v in range(10):
-        if CNUM[v]:
-            m.t[v, :CNUM[v]] = rng.dirichlet(np.ones(CNUM[v]))
-        if STTYPE[v] in (ML, IL, IR):
+def tiny_cm(rng, W=10, local=False, topology="matl"):
+    T = TOPOLOGIES[topology]
+    st = T["states"]
+    M, nodes = len(st), len(T["nodes"])
+    m = cmfile.CMModel(name="brute", M=M, nodes=nodes, clen=T["clen"], W=W)
+    m.sttype = np.array([x[0] for x in st], np.int8)
+    m.stid = np.array([x[1] for x in st], np.int8)
+    m.ndidx = np.array([x[2] for x in st], np.int32)
+    m.cfirst = np.array([x[3] for x in st], np.int32)
+    m.cnum = np.array([x[4] for x in st], np.int32)
+    m.ndtype = np.array(T["nodes"], np.int8)
+    m.nodemap = np.array([min(v for v in range(M) if st[v][2] == nd) for nd in range(nodes)], np.int32)
+    m.t = np.zeros((M, 6), np.float32)
+    m.e = np.zeros((M, 16), np.float32)
+    for v, (t, _, _, _, cn) in enumerate(st):
+        if t not in (B, E) and cn:
+            m.t[v, :cn] = rng.dirichlet(np.ones(cn))
+        if t == MP:
+            m.e[v, :16] = rng.dirichlet(np.ones(16))
+        elif t in (ML, MR, IL, IR):
             m.e[v, :4] = rng.dirichlet(np.ones(4))
     m.null = np.full(4, 0.25, np.float32)
     m.null3_omega = np.float32(2.0 ** -16)
@@ -62,22 +91,36 @@ def brute(m, x):
     f32 = np.float32
     tsc, esc = m.tsc, m.oesc
     el, endsc, beginsc = f32(m.el_selfsc), m.endsc, m.beginsc
+    STTYPE, CFIRST, CNUM, Kp = [int(t) for t in m.sttype], [int(c) for c in m.cfirst], [int(c) for c in m.cnum], m.Kp
+
+    def shape(v, i, j):
+        """(child i, child j, emission score or None); None when v cannot emit here."""
+        t = STTYPE[v]
+        if t in (ML, IL):
+            return (i + 1, j, esc[v, x[i - 1]]) if i <= j else None
+        if t in (MR, IR):
+            return (i, j - 1, esc[v, x[j - 1]]) if i <= j else None
+        if t == MP:
+            return (i + 1, j - 1, esc[v, x[i - 1] * Kp + x[j - 1]]) if i < j else None
+        return (i, j, None)
 
     @functools.lru_cache(maxsize=None)
     def cyk(v, i, j):          # parse of x[i..j] (empty when i > j) rooted at state v
         t = STTYPE[v]
         if t == E:
             return f32(0.0) if i > j else f32(IMP)
-        if t in (ML, IL):
-            if i > j:
-                return f32(IMP)
-            ci, cj, e = i + 1, j, esc[v, x[i - 1]]
-        elif t == IR:
-            if i > j:
-                return f32(IMP)
-            ci, cj, e = i, j - 1, esc[v, x[j - 1]]
-        else:
-            ci, cj, e = i, j, None
+        if t == B:             # split into BEGL x[i..k] and BEGR x[k+1..j], either part may be empty
+            best = f32(IMP)
+            for k in range(i - 1, j + 1):
+                a, b = cyk(CFIRST[v], i, k), cyk(CNUM[v], k + 1, j)
+                if a > IMP / 2 and b > IMP / 2:
+                    s = f32(a + b)
+                    best = s if s > best else best
+            return best
+        sh = shape(v, i, j)
+        if sh is None:
+            return f32(IMP)
+        ci, cj, e = sh
         best = f32(IMP)
         for o in range(CNUM[v]):
             c = cyk(CFIRST[v] + o, ci, cj)
@@ -91,21 +134,25 @@ def brute(m, x):
             return f32(IMP)
         return f32(best + e) if e is not None else best
 
+    def lsum(terms):
+        terms = [a for a in terms if a > IMP / 2]
+        if not terms:
+            return -math.inf
+        mx = max(terms)
+        return mx + math.log2(sum(2.0 ** (a - mx) for a in terms))
+
     @functools.lru_cache(maxsize=None)
     def ins(v, i, j):          # log2 of the summed probability-odds of all parses
         t = STTYPE[v]
         if t == E:
             return 0.0 if i > j else -math.inf
-        if t in (ML, IL):
-            if i > j:
-                return -math.inf
-            ci, cj, e = i + 1, j, float(esc[v, x[i - 1]])
-        elif t == IR:
-            if i > j:
-                return -math.inf
-            ci, cj, e = i, j - 1, float(esc[v, x[j - 1]])
-        else:
-            ci, cj, e = i, j, 0.0
+        if t == B:
+            return lsum([ins(CFIRST[v], i, k) + ins(CNUM[v], k + 1, j) for k in range(i - 1, j + 1)])
+        sh = shape(v, i, j)
+        if sh is None:
+            return -math.inf
+        ci, cj, e = sh
+        e = 0.0 if e is None else float(e)
         terms = [ins(CFIRST[v] + o, ci, cj) + float(tsc[v, o]) for o in range(CNUM[v])]
         if endsc[v] > IMP / 2:
             terms.append(float(el) * max(0, cj - ci + 1) + float(endsc[v]))
@@ -113,6 +160,11 @@ def brute(m, x):
         if not terms:
             return -math.inf
         mx = max(terms)
+        if i > j and t in (S, D):
+            # empty subsequence: the reference initialises these cells with the
+            # MAX over the local end and the children, for Inside too
+            # (cm_scan_mx_InitializeIntegers / InitializeFloats, src/cm_mx.c:6039-6138)
+            return mx + e
         return mx + math.log2(sum(2.0 ** (a - mx) for a in terms)) + e
 
     begins = [v for v in range(1, len(STTYPE)) if beginsc[v] > IMP / 2]
@@ -135,10 +187,10 @@ def brute(m, x):
     return float(best_c), best_i
 
 
-def _cases(n_models=12, local=False):
-    rng = np.random.default_rng(181 + int(local))
+def _cases(n_models=12, local=False, topology="matl"):
+    rng = np.random.default_rng([181, int(local), len(topology)])
     for k in range(n_models):
-        m = tiny_cm(rng, local=local)
+        m = tiny_cm(rng, local=local, topology=topology)
         x = [int(a) for a in rng.integers(0, 4, int(rng.integers(3, 9)))]
         yield k, m, x
 
@@ -147,9 +199,9 @@ def _dsq(x):
     return np.array([cmfile.DSQ_SENTINEL] + x + [cmfile.DSQ_SENTINEL], np.uint8)
 
 
-@pytest.mark.parametrize("local", [False, True])
-def test_brute_oracle(local):
-    for k, m, x in _cases(local=local):
+@pytest.mark.parametrize("topology,local", [("matl", False), ("matl", True), ("bif", False), ("bif", True)])
+def test_brute_oracle(topology, local):
+    for k, m, x in _cases(local=local, topology=topology):
         bc, bi = brute(m, x)
         d = _dsq(x)
         c = oracle.scan(m, d, 1, len(x), algo="cyk", qdbidx=0, cutoff=1e30, env_cutoff=1e30)[3]
@@ -159,9 +211,9 @@ def test_brute_oracle(local):
         assert abs(i - bi) < 0.02 and abs(f - bi) < 0.01, (k, i, f, bi)
 
 
-@pytest.mark.parametrize("local", [False, True])
-def test_brute_emulated_kernel(emu, local):
-    for k, m, x in list(_cases(local=local))[:4]:
+@pytest.mark.parametrize("topology,local", [("matl", False), ("matl", True), ("bif", False), ("bif", True)])
+def test_brute_emulated_kernel(emu, topology, local):
+    for k, m, x in list(_cases(local=local, topology=topology))[:4]:
         bc, bi = brute(m, x)
         d = _dsq(x)
         c = emu.scan(m, d, 1, len(x), algo="cyk", qdbidx=0, cutoff=1e30, env_cutoff=1e30).sc
@@ -171,11 +223,11 @@ def test_brute_emulated_kernel(emu, local):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("local", [False, True])
-def test_brute_gpu(local):
+@pytest.mark.parametrize("topology,local", [("matl", False), ("matl", True), ("bif", False), ("bif", True)])
+def test_brute_gpu(topology, local):
     s = L.Scanner(0)
     try:
-        for k, m, x in _cases(local=local):
+        for k, m, x in _cases(local=local, topology=topology):
             bc, bi = brute(m, x)
             d = _dsq(x)
             c = s.scan(m, d, 1, len(x), algo="cyk", qdbidx=0, cutoff=1e30, env_cutoff=1e30).sc
