@@ -102,3 +102,52 @@ def search(scanner: "lib.Scanner", m, targets: Sequence[Tuple[str, np.ndarray]],
                         out.append(SearchHit(name, strand, sfrom, sto, float(h[4]), min(1.0, p), ev, h[2]))
     out.sort(key=lambda x: (x.evalue, -x.score))
     return out
+
+
+def scan_models(scanner: "lib.Scanner", models: Sequence, targets: Sequence[Tuple[str, np.ndarray]], E: float = 10.0,
+                F6: float = 1e-4, toponly: bool = False, null3: bool = True) -> List[Tuple[int, SearchHit]]:
+    """cmscan's --nohmm search: every model against every target, each target
+    searched as its own database (Z = its residues on both strands, as cmscan
+    computes E-values per query sequence).  The CYK filter of every (model,
+    strand) pair runs in one multi-model launch (cmgb_ScanMulti); each
+    model's final Inside runs on all of its windows in one batched launch.
+    Returns (model index, hit) pairs, per target best E-value first; each
+    (model, target) pair gives exactly search(scanner, model, [target]).
+    """
+    seqs, where = [], []                     # strands in launch order: (target index, strand, length)
+    for t, (name, dsq) in enumerate(targets):
+        L = len(dsq) - 2
+        seqs.append(dsq); where.append((t, "+", L))
+        if not toponly:
+            seqs.append(emit.revcomp_dsq(dsq)); where.append((t, "-", L))
+    cuts = []
+    for m in models:
+        lc = _ecm(m, "cyk")
+        cuts.append(float(lc[1] + math.log(F6) / (-lc[0])))
+    rs = scanner.scan_multi(list(models), seqs, algo="cyk", qdbidx=1, cutoffs=cuts, do_null3=null3,
+                            env_cutoff=0.0)
+    nseq = len(seqs)
+    per_target: List[List[Tuple[int, SearchHit]]] = [[] for _ in targets]
+    for a, m in enumerate(models):
+        li = _ecm(m, "inside")
+        wins = []                            # (strand index, a, b)
+        for q in range(nseq):
+            wins += [(q, a0, b0) for a0, b0 in cyk_windows(rs[a * nseq + q].hits, m.W, where[q][2])]
+        if not wins:
+            continue
+        pieces = [np.concatenate([[255], seqs[q][a0:b0 + 1], [255]]).astype(np.uint8) for q, a0, b0 in wins]
+        ri = scanner.scan_batch(m, pieces, algo="inside", qdbidx=2, cutoff=0.0, do_null3=null3, env_cutoff=0.0)
+        for (q, a0, b0), rw in zip(wins, ri):
+            t, strand, L = where[q]
+            z = float(L * (1 if toponly else 2))
+            for h in rw.hits:
+                i, j = h[0] + a0 - 1, h[1] + a0 - 1
+                sfrom, sto = (i, j) if strand == "+" else (L - i + 1, L - j + 1)
+                ev = lib.evalue(li, h[4], z)
+                if ev <= E:
+                    p = math.exp(-li[0] * (h[4] - li[1]))
+                    per_target[t].append((a, SearchHit(targets[t][0], strand, sfrom, sto, float(h[4]), min(1.0, p), ev, h[2])))
+    out: List[Tuple[int, SearchHit]] = []
+    for lst in per_target:
+        out += sorted(lst, key=lambda x: (x[1].evalue, -x[1].score))
+    return out

@@ -68,3 +68,51 @@ def test_pipeline_known_answers_gpu():
             assert (hits[0].sfrom, hits[0].sto) == (c["sfrom"], c["sto"]), (c["source"], hits[:2])
     finally:
         s.close()
+
+
+def _scan_models_case():
+    from infernal_gb300 import emit
+    ms = [cmfile.load_npz(os.path.join(HERE, f"{n}.model.npz")) for n in ("tRNA", "Vault")]
+    rng = np.random.default_rng(44)
+    s = emit.sample(ms[0], rng)
+    seq = "".join(rng.choice(list("ACGU"), 20)) + s + "".join(rng.choice(list("ACGU"), 20))
+    return ms, [("t1", cmfile.digitize(seq))]
+
+
+def _per_model(scanner, ms, targets, E, toponly=False):
+    out = []
+    for t in targets:
+        for a, m in enumerate(ms):
+            out += [(a, h) for h in pipeline.search(scanner, m, [t], E=E, toponly=toponly)]
+    return sorted(out, key=lambda x: (x[1].evalue, -x[1].score))
+
+
+def test_scan_models_equals_per_model_search_emulated(emu):
+    ms, targets = _scan_models_case()
+    got = pipeline.scan_models(emu, ms, targets, E=10.0, toponly=True)
+    want = _per_model(emu, ms, targets, 10.0, toponly=True)
+    assert got == want and got
+
+
+@pytest.mark.gpu
+def test_scan_models_equals_per_model_search_gpu():
+    from infernal_gb300 import emit
+    ms = [cmfile.load_npz(os.path.join(HERE, f"{n}.model.npz")) for n in ("tRNA", "Vault", "Plant_SRP")]
+    rng = np.random.default_rng(45)
+    targets = []
+    for k in range(4):
+        ins = [emit.sample(ms[k % 3], rng)]
+        d, _ = emit.make_target(rng, 4000, 0.45, ins)
+        targets.append((f"t{k}", d))
+    s = L.Scanner(0)
+    try:
+        got = pipeline.scan_models(s, ms, targets, E=1.0)
+        want = []
+        for t in targets:
+            lst = []
+            for a, m in enumerate(ms):
+                lst += [(a, h) for h in pipeline.search(s, m, [t], E=1.0)]
+            want += sorted(lst, key=lambda x: (x[1].evalue, -x[1].score))
+        assert got == want and len(got) >= 4
+    finally:
+        s.close()
