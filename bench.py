@@ -582,14 +582,19 @@ def run_ours(args, rank, world):
     return out
 
 
-def dp_ops_per_residue(m, qdbidx):
-    """Algorithmic DP operations per residue once j >= W: per non-B cell,
-    cnum adds + (cnum + 1) max/log-sum combines + 1 emission add if the state
-    emits; per B cell, one add and one combine per k term (k limits of
-    src/cm_dpsearch.c:258-269)."""
+def work_per_d(m, qdbidx):
+    """(cells[d], ops[d]) for d = 0..W: the DP cells of length d summed over
+    the non-E states whose band holds d (QDB bands capped at W, MP from
+    d = 2; src/cm_mx.c:5725-5738), and their algorithmic operations -- per
+    non-B cell cnum adds + (cnum + 1) max/log-sum combines + 1 emission add
+    if the state emits; per B cell one add and one combine per k term
+    (k limits of src/cm_dpsearch.c:258-269, which depend on d only)."""
     from infernal_gb300 import cmfile
+    W = m.W
     dmin, dmax = m.bands(qdbidx)
-    ops = 0
+    cells = np.zeros(W + 1, np.int64)
+    ops = np.zeros(W + 1, np.int64)
+    d = np.arange(W + 1)
     for v in range(m.M):
         t = int(m.sttype[v])
         if t == cmfile.E_st:
@@ -597,23 +602,51 @@ def dp_ops_per_residue(m, qdbidx):
         lo = 2 if t == cmfile.MP_st else 1
         if dmin is not None:
             lo = max(int(dmin[v]), lo)
-        dn, dx = min(lo, m.W), (min(int(dmax[v]), m.W) if dmax is not None else m.W)
+        dn, dx = min(lo, W), (min(int(dmax[v]), W) if dmax is not None else W)
         if dx < dn:
             continue
+        band = (d >= dn) & (d <= dx)
+        cells += band
         if t == cmfile.B_st:
             w, y = int(m.cfirst[v]), int(m.cnum[v])
-            for d in range(dn, dx + 1):
-                if dmin is not None:
-                    kmin = max(0, max(min(int(dmin[y]), m.W), d - min(int(dmax[w]), m.W)))
-                    kmax = min(min(int(dmax[y]), m.W), d - min(int(dmin[w]), m.W))
-                else:
-                    kmin, kmax = 0, d
-                ops += 2 * max(0, kmax - kmin + 1)
+            if dmin is not None:
+                kmin = np.maximum(0, np.maximum(min(int(dmin[y]), W), d - min(int(dmax[w]), W)))
+                kmax = np.minimum(min(int(dmax[y]), W), d - min(int(dmin[w]), W))
+            else:
+                kmin, kmax = np.zeros_like(d), d
+            ops += np.where(band, 2 * np.maximum(0, kmax - kmin + 1), 0)
         else:
             c = int(m.cnum[v])
             emits = t in (cmfile.MP_st, cmfile.ML_st, cmfile.MR_st, cmfile.IL_st, cmfile.IR_st)
-            ops += (dx - dn + 1) * (c + (c + 1) + (1 if emits else 0))
-    return ops
+            ops += band * (c + (c + 1) + (1 if emits else 0))
+    return cells, ops
+
+
+class Work:
+    """Exact cells and operations of a scan of L residues with one band set:
+    a cell (v, d) exists at every end position j >= d of the scanned range,
+    so a scan of L residues holds sum_d max(0, L - d + 1) x per-d counts."""
+
+    def __init__(self, m, qdbidx):
+        self.c, self.o = work_per_d(m, qdbidx)
+        d = np.arange(len(self.c), dtype=np.int64)
+        # sum_{d<=n} (L + 1 - d) x[d] = (L + 1) S0(n) - S1(n)
+        self.c0, self.c1 = np.cumsum(self.c), np.cumsum(self.c * d)
+        self.o0, self.o1 = np.cumsum(self.o), np.cumsum(self.o * d)
+        self.W = len(self.c) - 1
+
+    def cells(self, L):
+        n = min(int(L), self.W)
+        return int((L + 1) * self.c0[n] - self.c1[n])
+
+    def ops(self, L):
+        n = min(int(L), self.W)
+        return int((L + 1) * self.o0[n] - self.o1[n])
+
+
+def dp_ops_per_residue(m, qdbidx):
+    """Algorithmic DP operations per residue once j >= W."""
+    return int(work_per_d(m, qdbidx)[1].sum())
 
 
 def alu_roofline(ops, kms, clocks):

@@ -296,6 +296,13 @@ int cmgb_ScanBatch(cmgb_ctx *ctx, cmgb_model *model, char *errbuf, int algo, int
                    const uint8_t *seqs, int64_t seqs_len, const int64_t *offsets, const int64_t *lengths,
                    int nseq, float cutoff, cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
                    int64_t *ret_nhits, int64_t *ret_envi, int64_t *ret_envj, float *ret_sc, int *ret_mode);
+/* The same with the residue buffer already in device memory (d_seqs, a
+ * device address; no host->device copy of residues).  Sequences whose
+ * candidate hits need NULL3 compositions are read back individually. */
+int cmgb_ScanBatch_dev(cmgb_ctx *ctx, cmgb_model *model, char *errbuf, int algo, int qdbidx, int pass_idx,
+                       const uint8_t *d_seqs, int64_t seqs_len, const int64_t *offsets, const int64_t *lengths,
+                       int nseq, float cutoff, cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
+                       int64_t *ret_nhits, int64_t *ret_envi, int64_t *ret_envj, float *ret_sc, int *ret_mode);
 
 /* ---- multi-model batched scans ----
  * Runs njobs (model, sequence) scans of several models in one persistent
@@ -387,30 +394,43 @@ int  cmgb_filter_trainer_get(cmgb_filter_trainer *trainer, float *w0, float *w, 
                              float *gw0, float *gw, float *gb, float *gwout, char *errbuf);
 
 /* ---- allocation-free CYK scan ----
- * This entry point has no counterpart in the reference.  It exists for
- * callers that must not allocate device memory while they scan: code that
- * records work into a CUDA stream capture, hosts where a framework's own
- * allocator owns all device memory, and long-running services that allocate
- * everything at start-up.  It runs the same CYK kernel as cmgb_FastCYKScan_dev
- * but keeps the kernel's scratch (per-CTA carry rows, bifurcation history
- * rings, tile arena and work counter) in one static device array of
- * CMGB_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds until
- * the process exits; nothing is allocated per call.  When a model needs more
- * scratch per CTA than fits, fewer CTAs run; if not even one fits, the call
- * fails with CMGB_ERANGE.  The first call on a device looks up the array's
- * device address on that device; make that first call before any stream
- * capture.  All calls share the array, so calls that overlap on the GPU (other
- * host threads, other streams) race: serialise them.
+ * This entry point has no counterpart in the reference.  It is for callers
+ * that cannot call cudaMalloc while they scan:
+ *   - a host program whose own allocator (a deep-learning framework's caching
+ *     allocator, a memory pool sized at start-up) owns the device memory, so
+ *     that memory taken behind its back fragments or overruns its budget;
+ *   - a long-running search service that allocates everything at start-up,
+ *     because cudaMalloc can fail under memory pressure at run time and
+ *     cudaMalloc/cudaFree synchronise the whole device, stalling the
+ *     service's other streams in the middle of a query.
+ * It runs the same CYK kernel as cmgb_FastCYKScan_dev, but the kernel's
+ * scratch (per-CTA carry rows, bifurcation history rings, tile arena, work
+ * counter and control block) lives in one static device array of
+ * CMGB_NOALLOC_SCRATCH_BYTES (64 MiB) that every GPU loading this library
+ * holds until the process exits; the call allocates nothing.  When a model
+ * needs more scratch per CTA than fits, fewer CTAs run; if not even one CTA
+ * fits, the call fails with CMGB_ERANGE.  The context's ctas_per_sm and
+ * window_len settings are honoured within that limit.
+ *
+ * Set-up: the first call on a device, with that device current, looks up
+ * the array's device address there (cudaGetSymbolAddress) and keeps it; make
+ * that first call before any stream capture.  All calls share the array and
+ * it keeps the last call's contents (each call clears what must start at
+ * zero), so calls that overlap on the GPU (other host threads, other
+ * streams, other contexts) race: serialise them.  The caller's current
+ * device is restored before the call returns.
  *
  * The model's plan for qdbidx must already exist on this context (built by an
  * earlier cmgb_FastCYKScan / cmgb_FastCYKScan_dev / cmgb_autotune call);
- * otherwise the call returns CMGB_EINCOMPAT without allocating one.
+ * otherwise the call returns CMGB_EINCOMPAT without building one.
  * Inputs: d_dsq as for cmgb_FastCYKScan_dev.  Outputs: the candidate cells
- * (every root cell of [i0,j0] whose CYK score is >= cutoff; the hit list of
- * the greedy scanner is resolved from these) are written to the caller's
- * device array d_cells[cell_cap] in no particular order, their number to
- * *ret_ncells; envelope and best score as in cmgb_FastCYKScan.  NULL3 and
- * per-state scores are not computed here.  The call waits for its kernel. */
+ * are written to the caller's device array d_cells[cell_cap] in no
+ * particular order, their number to *ret_ncells: every root cell of [i0,j0]
+ * whose CYK score is >= cutoff, or, for a model flagged CMGB_NOTGREEDY,
+ * every cell whose score is > 0 (the candidates of optimal resolution) --
+ * the same cells cmgb_FastCYKScan resolves its hit list from.  Envelope and
+ * best score as in cmgb_FastCYKScan.  NULL3 and per-state scores are not
+ * computed here.  The call waits for its kernel before it returns. */
 #define CMGB_NOALLOC_SCRATCH_BYTES (64u << 20)
 typedef struct {
   int64_t j;      /* end position of the cell */
@@ -423,6 +443,16 @@ int cmgb_FastCYKScan_noalloc(cmgb_ctx *ctx, cmgb_model *model, char *errbuf, int
                              const uint8_t *d_dsq, int64_t i0, int64_t j0, float cutoff, float env_cutoff,
                              cmgb_cell *d_cells, int cell_cap, int *ret_ncells,
                              int64_t *ret_envi, int64_t *ret_envj, float *ret_sc);
+
+/* ---- measured issue peak (roofline denominator) ----
+ * No reference counterpart: a diagnostic for the scan kernels' roofline.
+ * Times 8 independent chains per thread of x = max(x + y, z) on every SM of
+ * the context's device (2048 threads per SM; best of three timed launches,
+ * CUDA events) and returns the arithmetic rate in operations per second,
+ * counting the add and the max as one operation each: kind 0 fp32
+ * (round-to-nearest add, the CYK fold), kind 1 int32 (the integer Inside's
+ * add and combine, without its table lookup). */
+int cmgb_measure_issue_peak(cmgb_ctx *ctx, int kind, double *ret_ops_per_s, char *errbuf);
 
 /* DP cell count of one scan of [i0,j0] with band set qdbidx: the
  * algorithmic work unit, sum over j and non-E states of the band width

@@ -945,15 +945,44 @@ extern "C" int cmgb_RefITrInsideScan_dev(cmgb_ctx *c, cmgb_model *m, char *errbu
 // ---------------------------------------------------------------------------
 // Batched scans: n independent sequences of one model in one persistent
 // launch, one work item per sequence, longest first.
+// seqs: host residues (copied to the device per call) or, when d_seqs is
+// given, residues already in device memory (host copies of single sequences
+// are fetched only for the NULL3 composition of sequences with candidates).
+static int scan_batch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo, int qdbidx, int pass_idx,
+                      const uint8_t *seqs, const uint8_t *d_seqs, int64_t seqs_len, const int64_t *offsets,
+                      const int64_t *lengths, int nseq, float cutoff, cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
+                      int64_t *ret_nhits, int64_t *ret_envi, int64_t *ret_envj, float *ret_sc, int *ret_mode);
+
 extern "C" int cmgb_ScanBatch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo, int qdbidx, int pass_idx,
                               const uint8_t *seqs, int64_t seqs_len, const int64_t *offsets, const int64_t *lengths,
                               int nseq, float cutoff, cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
                               int64_t *ret_nhits, int64_t *ret_envi, int64_t *ret_envj, float *ret_sc, int *ret_mode)
 {
+  if (seqs == nullptr) ERRF(CMGB_EINCOMPAT, "ScanBatch, no sequences");
+  return scan_batch(c, m, errbuf, algo, qdbidx, pass_idx, seqs, nullptr, seqs_len, offsets, lengths, nseq, cutoff, hitlist,
+                    do_null3, env_cutoff, ret_nhits, ret_envi, ret_envj, ret_sc, ret_mode);
+}
+
+extern "C" int cmgb_ScanBatch_dev(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo, int qdbidx, int pass_idx,
+                                  const uint8_t *d_seqs, int64_t seqs_len, const int64_t *offsets, const int64_t *lengths,
+                                  int nseq, float cutoff, cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
+                                  int64_t *ret_nhits, int64_t *ret_envi, int64_t *ret_envj, float *ret_sc, int *ret_mode)
+{
+  if (d_seqs == nullptr) ERRF(CMGB_EINCOMPAT, "ScanBatch, no sequences");
+  return scan_batch(c, m, errbuf, algo, qdbidx, pass_idx, nullptr, d_seqs, seqs_len, offsets, lengths, nseq, cutoff, hitlist,
+                    do_null3, env_cutoff, ret_nhits, ret_envi, ret_envj, ret_sc, ret_mode);
+}
+
+static int scan_batch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo, int qdbidx, int pass_idx,
+                      const uint8_t *seqs, const uint8_t *d_seqs, int64_t seqs_len, const int64_t *offsets,
+                      const int64_t *lengths, int nseq, float cutoff, cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
+                      int64_t *ret_nhits, int64_t *ret_envi, int64_t *ret_envj, float *ret_sc, int *ret_mode)
+{
   static const char *fn = "ScanBatch";
   if (!c || !m) ERRF(CMGB_EINVAL, "%s, NULL context or model", fn);
   if (algo < CMGB_ALGO_CYK || algo > CMGB_ALGO_ITRINSIDE) ERRF(CMGB_EINVAL, "%s, unknown algorithm %d", fn, algo);
-  if (seqs == nullptr || offsets == nullptr || lengths == nullptr || nseq < 1) ERRF(CMGB_EINCOMPAT, "%s, no sequences", fn);
+  if ((seqs == nullptr && d_seqs == nullptr) || offsets == nullptr || lengths == nullptr || nseq < 1)
+    ERRF(CMGB_EINCOMPAT, "%s, no sequences", fn);
   if (qdbidx < 0 || qdbidx > 2) ERRF(CMGB_EINCOMPAT, "%s, qdbidx is invalid", fn);
   const bool tr = algo >= CMGB_ALGO_TRCYK;
   const int alg = tr ? algo - CMGB_ALGO_TRCYK : algo;
@@ -1004,7 +1033,7 @@ extern "C" int cmgb_ScanBatch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo
   }
   // one device block: residues, window ranges, per-window outputs
   auto al = [](size_t x) { return (x + 255) & ~(size_t) 255; };
-  const size_t o_ws = al((size_t) seqs_len), o_we = o_ws + al(sizeof(long long) * nw), o_ws0 = o_we + al(sizeof(long long) * nw);
+  const size_t o_ws = d_seqs ? 0 : al((size_t) seqs_len), o_we = o_ws + al(sizeof(long long) * nw), o_ws0 = o_we + al(sizeof(long long) * nw);
   const size_t o_out = o_ws0 + al(sizeof(long long) * nw);
   const size_t out_bytes = tr ? sizeof(unsigned long long) * nw : sizeof(long long) * 2 * nw + sizeof(unsigned) * nw;
   if ((st = grow((void **) &c->d_dsq, &c->dsq_bytes, o_out + al(out_bytes), errbuf)) != CMGB_OK) return st;
@@ -1014,12 +1043,13 @@ extern "C" int cmgb_ScanBatch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo
     long long *env = reinterpret_cast<long long *>(out_init.data());
     for (int w = 0; w < nw; w++) { env[2 * w] = LLONG_MAX; env[2 * w + 1] = -1; }
   }
-  CUDA_TRY(cudaMemcpyAsync(blk, seqs, (size_t) seqs_len, cudaMemcpyHostToDevice, c->stream));
+  if (!d_seqs) CUDA_TRY(cudaMemcpyAsync(blk, seqs, (size_t) seqs_len, cudaMemcpyHostToDevice, c->stream));
+  const unsigned char *res = d_seqs ? d_seqs : blk;
   CUDA_TRY(cudaMemcpyAsync(blk + o_ws, ws.data(), sizeof(long long) * nw, cudaMemcpyHostToDevice, c->stream));
   CUDA_TRY(cudaMemcpyAsync(blk + o_we, we.data(), sizeof(long long) * nw, cudaMemcpyHostToDevice, c->stream));
   CUDA_TRY(cudaMemcpyAsync(blk + o_ws0, ws0.data(), sizeof(long long) * nw, cudaMemcpyHostToDevice, c->stream));
   CUDA_TRY(cudaMemcpyAsync(blk + o_out, out_init.data(), out_bytes, cudaMemcpyHostToDevice, c->stream));
-  c->last_h2d = seqs_len + (int64_t) (3 * sizeof(long long) * nw + out_bytes + sizeof(Control));
+  c->last_h2d = (d_seqs ? 0 : seqs_len) + (int64_t) (3 * sizeof(long long) * nw + out_bytes + sizeof(Control));
 
   const bool gl = P->arena_global != 0;
   int cps = c->ctas_per_sm;
@@ -1058,7 +1088,7 @@ extern "C" int cmgb_ScanBatch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo
     kp.oesc = m->d_oesc; kp.ioesc = m->d_ioesc;
     kp.lmesc = m->d_lmesc; kp.rmesc = m->d_rmesc; kp.ilmesc = m->d_ilmesc; kp.irmesc = m->d_irmesc;
     kp.ilog = c->d_ilog;
-    kp.dsq = blk; kp.i0 = 1; kp.j0 = seqs_len - 2; kp.win_len = 0; kp.nwin = nw;
+    kp.dsq = res; kp.i0 = 1; kp.j0 = seqs_len - 2; kp.win_len = 0; kp.nwin = nw;
     kp.queue = &c->d_ctl->queue; kp.carry = c->d_carry; kp.ring = c->d_ring;
     kp.cand = c->d_trcand; kp.ncand = &c->d_ctl->ncand; kp.cand_cap = cand_cap;
     kp.cand_cut = ccut; kp.cand_pos = cpos; kp.env_cut = ecut;
@@ -1072,7 +1102,7 @@ extern "C" int cmgb_ScanBatch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo
     std::memset(&kp, 0, sizeof(kp));
     kp.st = (const StateInfo *) d_states; kp.plan = *P; kp.rec = d_rec; kp.arena = c->d_arena;
     kp.oesc = m->d_oesc; kp.ioesc = m->d_ioesc; kp.ilog = c->d_ilog; kp.flog = c->d_flog;
-    kp.dsq = blk; kp.i0 = 1; kp.j0 = seqs_len - 2; kp.win_len = 0; kp.nwin = nw;
+    kp.dsq = res; kp.i0 = 1; kp.j0 = seqs_len - 2; kp.win_len = 0; kp.nwin = nw;
     kp.queue = &c->d_ctl->queue; kp.carry = c->d_carry; kp.ring = c->d_ring;
     kp.cand = c->d_cand; kp.ncand = &c->d_ctl->ncand; kp.cand_cap = cand_cap;
     kp.cand_cut = ccut; kp.cand_pos = cpos; kp.env_cut = ecut;
@@ -1167,6 +1197,17 @@ extern "C" int cmgb_ScanBatch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo
       if (ret_mode) ret_mode[q] = CMGB_TRMODE_J;
     }
   }
+  // device-resident residues: host copies of the sequences whose candidates need NULL3 compositions
+  std::vector<uint8_t> hres;
+  if (d_seqs && hitlist && do_null3) {
+    for (int q = 0; q < nseq; q++) {
+      if (per[q].empty()) continue;
+      if (hres.empty()) hres.assign((size_t) seqs_len, (uint8_t) 255);
+      CUDA_TRY(cudaMemcpy(hres.data() + offsets[q] + 1, d_seqs + offsets[q] + 1, (size_t) lengths[q], cudaMemcpyDeviceToHost));
+      c->last_d2h += lengths[q];
+    }
+  }
+  const uint8_t *hseq = d_seqs ? (hres.empty() ? nullptr : hres.data()) : seqs;
   for (int q = 0; q < nseq; q++) {
     const int64_t off = offsets[q];
     if (ret_envi) ret_envi[q] = envj[q] < off + 1 ? -1 : envi[q] - off;
@@ -1176,7 +1217,7 @@ extern "C" int cmgb_ScanBatch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo
       TruncFilter tf;
       ResolveArgs ra;
       ra.null = m->null.data(); ra.K = m->K; ra.null3_omega = m->null3_omega; ra.do_null3 = do_null3;
-      ra.greedy = greedy ? 1 : 0; ra.cutoff = cutoff; ra.i0 = off + 1; ra.j0 = off + lengths[q]; ra.dsq = seqs;
+      ra.greedy = greedy ? 1 : 0; ra.cutoff = cutoff; ra.i0 = off + 1; ra.j0 = off + lengths[q]; ra.dsq = hseq;
       if (tr) {
         tf.pass_idx = pass_idx; tf.local = (m->flags & CMGB_LOCAL_BEGIN) ? 1 : 0; tf.clen = m->clen;
         tf.ndidx = m->ndidx.data(); tf.ndtype = m->ndtype.data(); tf.lpos = m->emap_lpos.data(); tf.rpos = m->emap_rpos.data();
@@ -1509,6 +1550,11 @@ static __global__ void noalloc_init_kernel(int *queue, Control *ctl)
   ctl->env[0] = LLONG_MAX; ctl->env[1] = -1;
   ctl->best = 0u;
 }
+
+static int noalloc_scan(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx,
+                        const uint8_t *d_dsq, int64_t i0, int64_t j0, float cutoff, float env_cutoff,
+                        cmgb_cell *d_cells, int cell_cap, int *ret_ncells,
+                        int64_t *ret_envi, int64_t *ret_envj, float *ret_sc);
 #endif
 
 extern "C" int cmgb_FastCYKScan_noalloc(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx,
@@ -1517,8 +1563,26 @@ extern "C" int cmgb_FastCYKScan_noalloc(cmgb_ctx *c, cmgb_model *m, char *errbuf
                                         int64_t *ret_envi, int64_t *ret_envj, float *ret_sc)
 {
 #ifdef CMGB_HOST_EMULATION
+  (void) c; (void) m; (void) qdbidx; (void) d_dsq; (void) i0; (void) j0; (void) cutoff; (void) env_cutoff;
+  (void) d_cells; (void) cell_cap; (void) ret_ncells; (void) ret_envi; (void) ret_envj; (void) ret_sc;
   ERRF(CMGB_ENODEV, "FastCYKScan_noalloc, not available in the host emulation");
 #else
+  // the scan runs with the context's device current; the caller's current device is restored on every return
+  int prev = -1;
+  if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+  const int st = noalloc_scan(c, m, errbuf, qdbidx, d_dsq, i0, j0, cutoff, env_cutoff, d_cells, cell_cap, ret_ncells,
+                              ret_envi, ret_envj, ret_sc);
+  if (prev >= 0) cudaSetDevice(prev);
+  return st;
+#endif
+}
+
+#ifndef CMGB_HOST_EMULATION
+static int noalloc_scan(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx,
+                        const uint8_t *d_dsq, int64_t i0, int64_t j0, float cutoff, float env_cutoff,
+                        cmgb_cell *d_cells, int cell_cap, int *ret_ncells,
+                        int64_t *ret_envi, int64_t *ret_envj, float *ret_sc)
+{
   if (!c || !m) ERRF(CMGB_EINVAL, "FastCYKScan_noalloc, NULL context or model");
   if (j0 < i0 || i0 < 1) ERRF(CMGB_EINCOMPAT, "FastCYKScan_noalloc, i0: %lld j0: %lld", (long long) i0, (long long) j0);
   if (d_dsq == nullptr) ERRF(CMGB_EINCOMPAT, "FastCYKScan_noalloc, dsq is NULL");
@@ -1555,11 +1619,15 @@ extern "C" int cmgb_FastCYKScan_noalloc(cmgb_ctx *c, cmgb_model *m, char *errbuf
   int nb = 1;
   if (gl) CUDA_TRY((prepare_qdb<false, true>(c->threads, P.smem_bytes, &nb)));
   else    CUDA_TRY((prepare_qdb<false, false>(c->threads, P.smem_bytes, &nb)));
-  int64_t grid_max = (int64_t) c->nsm * (nb < 1 ? 1 : nb);
+  const int cps = c->ctas_per_sm > 0 ? c->ctas_per_sm : (nb < 1 ? 1 : nb);
+  int64_t grid_max = (int64_t) c->nsm * cps;
   const int64_t fit = (int64_t) (((size_t) CMGB_NOALLOC_SCRATCH_BYTES - head - 1024) / per_cta);   // 1024: room for region alignment
   if (grid_max > fit) grid_max = fit;
-  int64_t win = (L + grid_max - 1) / grid_max;
-  if (win < 8LL * m->W) win = 8LL * m->W;
+  int64_t win = c->window_len;
+  if (win <= 0) {
+    win = (L + grid_max - 1) / grid_max;
+    if (win < 8LL * m->W) win = 8LL * m->W;
+  }
   win = ((win + P.T - 1) / P.T) * P.T;
   const int64_t nwin = (L + win - 1) / win;
   if (nwin > INT_MAX) ERRF(CMGB_ERANGE, "FastCYKScan_noalloc, too many windows");
@@ -1585,7 +1653,8 @@ extern "C" int cmgb_FastCYKScan_noalloc(cmgb_ctx *c, cmgb_model *m, char *errbuf
   kp.dsq = d_dsq; kp.i0 = i0; kp.j0 = j0; kp.win_len = win; kp.nwin = (int) nwin;
   kp.queue = queue; kp.carry = carry; kp.ring = ring;
   kp.cand = reinterpret_cast<Cand *>(d_cells); kp.ncand = &ctl->ncand; kp.cand_cap = cell_cap;
-  kp.cand_cut = cutoff; kp.cand_pos = 0;
+  // the candidate set of cmgb_FastCYKScan: cells >= cutoff (greedy), cells > 0 (optimal resolution)
+  kp.cand_cut = cutoff; kp.cand_pos = (m->flags & CMGB_NOTGREEDY) ? 1 : 0;
   kp.env_cut = env_cutoff; kp.env = ctl->env; kp.vsc = nullptr; kp.best = &ctl->best; kp.err = &ctl->err;
   CUDA_TRY(cudaEventRecord(c->ev0, c->stream));
   if (gl) launch_qdb<false, true>(grid, c->threads, (size_t) P.smem_bytes, c->stream, kp);
@@ -1608,6 +1677,85 @@ extern "C" int cmgb_FastCYKScan_noalloc(cmgb_ctx *c, cmgb_model *m, char *errbuf
     if (u != 0) { unsigned b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u; std::memcpy(&f, &b, 4); }
     *ret_sc = f;
   }
+  return CMGB_OK;
+}
+#endif
+
+// ---------------------------------------------------------------------------
+// Measured issue peaks of the DP's arithmetic: the roofline denominators of
+// the scan kernels.  Every thread runs 8 independent chains of
+// x = max(x + y, z) -- one add and one max, the CYK fold's pair of
+// operations (kind 0: fp32 round-to-nearest add and fmaxf) or the integer
+// Inside's (kind 1: int32 add and max) -- on every SM at 2048 threads per SM.
+#ifndef CMGB_HOST_EMULATION
+template <int KIND>
+static __global__ void __launch_bounds__(256) issue_peak_kernel(const int *in, int *out, int iters)
+{
+  if (KIND == 0) {
+    const float y = __int_as_float(in[0]), z = __int_as_float(in[1]);
+    float x[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) x[k] = (float) (threadIdx.x + k);
+#pragma unroll 4
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+      for (int k = 0; k < 8; k++) x[k] = fmaxf(__fadd_rn(x[k], y), z);
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; k++) s = __fadd_rn(s, x[k]);
+    if (in[2]) out[blockIdx.x * blockDim.x + threadIdx.x] = __float_as_int(s);
+  } else {
+    const int y = in[0], z = in[1];
+    int x[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) x[k] = (int) threadIdx.x + k;
+#pragma unroll 4
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+      for (int k = 0; k < 8; k++) x[k] = max(x[k] + y, z);
+    }
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) s += x[k];
+    if (in[2]) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+  }
+}
+#endif
+
+extern "C" int cmgb_measure_issue_peak(cmgb_ctx *c, int kind, double *ret_ops_per_s, char *errbuf)
+{
+#ifdef CMGB_HOST_EMULATION
+  (void) c; (void) kind; (void) ret_ops_per_s;
+  ERRF(CMGB_ENODEV, "measure_issue_peak, not available in the host emulation");
+#else
+  if (!c || !ret_ops_per_s || kind < 0 || kind > 1) ERRF(CMGB_EINVAL, "measure_issue_peak, invalid arguments");
+  CUDA_TRY(cudaSetDevice(c->device));
+  const int threads = 256, blocks = c->nsm * 8, iters = 1 << 16;
+  int *d = nullptr;
+  CUDA_TRY(cudaMalloc(&d, sizeof(int) * (4 + (size_t) blocks * threads)));
+  // y = -1, z = a large negative floor, no output (in[2] = 0)
+  const float fy = -1.0f, fz = -1.0e30f;
+  int h[4] = {0, 0, 0, 0};
+  if (kind == 0) { std::memcpy(&h[0], &fy, 4); std::memcpy(&h[1], &fz, 4); }
+  else { h[0] = -1; h[1] = -1000000000; }
+  cudaError_t e = cudaMemcpy(d, h, sizeof(h), cudaMemcpyHostToDevice);
+  float best = 1e30f;
+  for (int rep = 0; rep < 4 && e == cudaSuccess; rep++) {
+    cudaEventRecord(c->ev0, c->stream);
+    if (kind == 0) issue_peak_kernel<0><<<blocks, threads, 0, c->stream>>>(d, d + 4, iters);
+    else           issue_peak_kernel<1><<<blocks, threads, 0, c->stream>>>(d, d + 4, iters);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) break;
+    cudaEventRecord(c->ev1, c->stream);
+    e = cudaEventSynchronize(c->ev1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    if (rep > 0 && ms < best) best = ms;      // rep 0 warms up
+  }
+  cudaFree(d);
+  if (e != cudaSuccess) ERRF(CMGB_ENODEV, "measure_issue_peak: %s", cudaGetErrorString(e));
+  *ret_ops_per_s = 2.0 * 8.0 * (double) iters * (double) blocks * threads / (best * 1e-3);
   return CMGB_OK;
 #endif
 }

@@ -346,7 +346,14 @@ extern "C" int cmgb_filter_windows(cmgb_ctx *ctx, cmgb_filter *f, const uint8_t 
 //             forward and (transposed, taps reversed) for the backward.
 // Gradients of a layer's input are rounded to BF16 (the tensor-core
 // operand type); weight and bias gradients accumulate in fp32.
+//
+// Every reduction is deterministic: a block writes its partial sums to its
+// own slot of a partial buffer and a second kernel adds the slots in a fixed
+// order (no floating-point atomics), so two runs from the same seed on the
+// same batches give bit-identical losses and weights.
 namespace {
+constexpr int NB_BIAS = 256;   // partial slots of a bias gradient (row-strided blocks)
+constexpr int NB_W0 = 128;     // partial slots of layer 0's weight gradient (position slices)
 constexpr size_t OFF_W0 = 0;                                   // [9][4][128]
 constexpr size_t OFF_W = OFF_W0 + (size_t) KT * 4 * CH;        // [5][9][128 co][128 ci]
 constexpr size_t OFF_B = OFF_W + (size_t) 5 * KT * CH * CH;    // [6][128]
@@ -364,6 +371,10 @@ struct cmgb_filter_trainer_s {
   int *argm = nullptr;
   unsigned short *act[NL] = {nullptr};              // [B][LP][128]
   unsigned short *dz[2] = {nullptr, nullptr};
+  int zsplit = 1;                                   // position slices of a dilated layer's weight gradient
+  float *part_w = nullptr;                          // [zsplit][9][128][128] partial weight gradients
+  float *part_b = nullptr;                          // [NB_BIAS][128] partial bias gradients
+  float *part_w0 = nullptr;                         // [NB_W0][9][4][128] partial layer-0 weight gradients
   int *err = nullptr;
 };
 
@@ -403,31 +414,50 @@ __global__ void train_loss(const float *logit, const float *y, float posw, int B
   if (threadIdx.x == 0) *loss = red[0] / (float) B;
 }
 
-// read-out backward: weight gradients and the layer-5 gradient at the arg-max cells
+// out[i] = sum over k = 0, 1, .., nparts - 1 (in that order) of part[k n + i]
+__global__ void train_sum_parts(const float *part, int nparts, long long n, float *out)
+{
+  for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int k = 0; k < nparts; k++) s += part[(size_t) k * n + i];
+    out[i] = s;
+  }
+}
+
+// read-out backward: the layer-5 gradient at the arg-max cells (one block per window)
 __global__ void train_readout_bwd(const float *dlogit, const float *pooled, const int *argm, const float *wout, int LP,
-                                  float *g_wout, unsigned short *dz5)
+                                  unsigned short *dz5)
 {
   const int b = blockIdx.x, c = threadIdx.x;
   const float d = dlogit[b], pv = pooled[b * CH + c];
-  atomicAdd(g_wout + c, d * pv);
-  if (c == 0) atomicAdd(g_wout + CH, d);
   if (pv > 0.f) dz5[((size_t) b * LP + argm[b * CH + c]) * CH + c] = f2bf(d * wout[c]);
 }
 
-// bias gradient: column sums of dz over rows [0, nrows)
-__global__ void train_bias_grad(const unsigned short *dz, long long nrows, float *gb)
+// read-out weight gradients: thread c < 128 sums dlogit[b] * pooled[b][c] over
+// the batch in window order, thread 128 the bias term (CH + 1 threads)
+__global__ void train_readout_wgrad(const float *dlogit, const float *pooled, int B, float *g_wout)
+{
+  const int c = threadIdx.x;
+  float s = 0.f;
+  if (c < CH) for (int b = 0; b < B; b++) s += dlogit[b] * pooled[(size_t) b * CH + c];
+  else for (int b = 0; b < B; b++) s += dlogit[b];
+  g_wout[c] = s;
+}
+
+// bias gradient, partial: block k sums rows k, k + gridDim.x, .. of dz into part[k][c]
+__global__ void train_bias_grad(const unsigned short *dz, long long nrows, float *part)
 {
   const int c = threadIdx.x;
   float acc = 0.f;
   for (long long r = blockIdx.x; r < nrows; r += gridDim.x) acc += bf2f(dz[(size_t) r * CH + c]);
-  atomicAdd(gb + c, acc);
+  part[(size_t) blockIdx.x * CH + c] = acc;
 }
 
-// weight gradient of a dilated layer: gw[t][co][ci] += sum over (b, p) of
-// dz[b][p][co] * a[b][p + (t - 4) dil][ci]; block: one tap, a 32 x 32 (co, ci)
-// tile, a slice of the positions; 256 threads x 2 x 2 outputs
+// weight gradient of a dilated layer, partial: part[z][t][co][ci] = sum over
+// the (b, p) of position slice z of dz[b][p][co] * a[b][p + (t - 4) dil][ci];
+// block: one tap, a 32 x 32 (co, ci) tile, one slice; 256 threads x 2 x 2 outputs
 __global__ void __launch_bounds__(256) train_wgrad(const unsigned short *dz, const unsigned short *a, int B, int LP, int W2,
-                                                   int dil, float *gw)
+                                                   int dil, float *part)
 {
   __shared__ float sd[32][33], sa[32][33];
   const int t = blockIdx.x, co0 = (blockIdx.y >> 2) * 32, ci0 = (blockIdx.y & 3) * 32;
@@ -460,21 +490,24 @@ __global__ void __launch_bounds__(256) train_wgrad(const unsigned short *dz, con
     }
     __syncthreads();
   }
-  float *o = gw + (size_t) t * CH * CH;
+  float *o = part + ((size_t) blockIdx.z * KT + t) * CH * CH;
   for (int i = 0; i < 2; i++)
-    for (int j = 0; j < 2; j++) atomicAdd(o + (size_t) (co0 + 2 * ty + i) * CH + ci0 + 2 * tx + j, acc[i][j]);
+    for (int j = 0; j < 2; j++) o[(size_t) (co0 + 2 * ty + i) * CH + ci0 + 2 * tx + j] = acc[i][j];
 }
 
-// layer 0 weight gradient: gw0[t][x][co] += dz0[b][p][co] where residue
-// p + t - 4 of window b is x (one block per window slice, 128 threads = co)
-__global__ void train_wgrad0(const unsigned short *dz, const unsigned char *win, int LP, int W, float *gw0)
+// layer 0 weight gradient, partial: part[k][t][x][co] = sum of dz0[b][p][co]
+// over the positions (b, p) of slice k (of the B x 2W flattened in window
+// order) where residue p + t - 4 of window b is x (128 threads = co)
+__global__ void train_wgrad0(const unsigned short *dz, const unsigned char *win, int B, int LP, int W2, float *part)
 {
   __shared__ float acc[KT * 4][CH];
-  const int b = blockIdx.y, c = threadIdx.x, W2 = 2 * W;
+  const int c = threadIdx.x;
   for (int k = 0; k < KT * 4; k++) acc[k][c] = 0.f;
-  const int per = (W2 + gridDim.x - 1) / gridDim.x;
-  const int p0 = per * blockIdx.x, p1 = p0 + per < W2 ? p0 + per : W2;
-  for (int p = p0; p < p1; p++) {
+  const long long npos = (long long) B * W2;
+  const long long per = (npos + gridDim.x - 1) / gridDim.x;
+  const long long Q0 = per * blockIdx.x, Q1 = Q0 + per < npos ? Q0 + per : npos;
+  for (long long Q = Q0; Q < Q1; Q++) {
+    const int b = (int) (Q / W2), p = (int) (Q - (long long) b * W2);
     const float gv = bf2f(dz[((size_t) b * LP + p) * CH + c]);
     if (gv == 0.f) continue;
     for (int t = 0; t < KT; t++) {
@@ -484,7 +517,8 @@ __global__ void train_wgrad0(const unsigned short *dz, const unsigned char *win,
       if (x < 4) acc[t * 4 + x][c] += gv;
     }
   }
-  for (int k = 0; k < KT * 4; k++) if (acc[k][c] != 0.f) atomicAdd(gw0 + (size_t) k * CH + c, acc[k][c]);
+  float *o = part + (size_t) blockIdx.x * KT * 4 * CH;
+  for (int k = 0; k < KT * 4; k++) o[(size_t) k * CH + c] = acc[k][c];
 }
 
 __global__ void train_adamw(float *p, const float *g, float *m1, float *m2, long long n, float lr, float b1, float b2,
@@ -534,6 +568,10 @@ extern "C" int cmgb_filter_trainer_create(cmgb_ctx *ctx, int W, int batch, uint6
   FCUDA(cudaMalloc(&f->loss, sizeof(float))); FCUDA(cudaMalloc(&f->argm, sizeof(int) * batch * CH));
   for (int l = 0; l < NL; l++) FCUDA(cudaMalloc(&f->act[l], act));
   FCUDA(cudaMalloc(&f->dz[0], act)); FCUDA(cudaMalloc(&f->dz[1], act));
+  f->zsplit = std::max(1, std::min(64, (int) (((long long) batch * f->LP) / 2048)));
+  FCUDA(cudaMalloc(&f->part_w, sizeof(float) * (size_t) f->zsplit * KT * CH * CH));
+  FCUDA(cudaMalloc(&f->part_b, sizeof(float) * (size_t) NB_BIAS * CH));
+  FCUDA(cudaMalloc(&f->part_w0, sizeof(float) * (size_t) NB_W0 * KT * 4 * CH));
   FCUDA(cudaMalloc(&f->err, sizeof(int))); FCUDA(cudaMemset(f->err, 0, sizeof(int)));
   // He-uniform initial weights from a splitmix64 stream, zero biases
   std::vector<float> h(NPARAM, 0.f);
@@ -566,6 +604,7 @@ extern "C" void cmgb_filter_trainer_destroy(cmgb_filter_trainer *f)
   cudaFree(f->win); cudaFree(f->y); cudaFree(f->pooled); cudaFree(f->logit); cudaFree(f->dlogit); cudaFree(f->loss);
   cudaFree(f->argm); for (int l = 0; l < NL; l++) cudaFree(f->act[l]);
   cudaFree(f->dz[0]); cudaFree(f->dz[1]); cudaFree(f->err);
+  cudaFree(f->part_w); cudaFree(f->part_b); cudaFree(f->part_w0);
 #endif
   delete f;
 }
@@ -623,20 +662,25 @@ extern "C" int cmgb_filter_trainer_step(cmgb_filter_trainer *f, const uint8_t *w
   // backward
   FCUDA(cudaMemset(f->g, 0, NPARAM * sizeof(float)));
   FCUDA(cudaMemset(f->dz[0], 0, actb));
-  train_readout_bwd<<<B, CH>>>(f->dlogit, f->pooled, f->argm, f->p + OFF_WOUT, LP, f->g + OFF_WOUT, f->dz[0]);
+  train_readout_bwd<<<B, CH>>>(f->dlogit, f->pooled, f->argm, f->p + OFF_WOUT, LP, f->dz[0]);
+  train_readout_wgrad<<<1, CH + 1>>>(f->dlogit, f->pooled, B, f->g + OFF_WOUT);
   int cur = 0;
-  const int zsplit = std::max(1, std::min(64, (int) (((long long) B * LP) / 2048)));
+  const long long nw = (long long) KT * CH * CH;
   for (int l = NL - 1; l >= 1; l--) {
     const int d = DIL[l];
-    train_bias_grad<<<256, CH>>>(f->dz[cur], (long long) B * LP, f->g + OFF_B + l * CH);
-    train_wgrad<<<dim3(KT, 16, zsplit), 256>>>(f->dz[cur], f->act[l - 1], B, LP, W2, d, f->g + OFF_W + (size_t) (l - 1) * KT * CH * CH);
+    train_bias_grad<<<NB_BIAS, CH>>>(f->dz[cur], (long long) B * LP, f->part_b);
+    train_sum_parts<<<1, CH>>>(f->part_b, NB_BIAS, CH, f->g + OFF_B + l * CH);
+    train_wgrad<<<dim3(KT, 16, f->zsplit), 256>>>(f->dz[cur], f->act[l - 1], B, LP, W2, d, f->part_w);
+    train_sum_parts<<<(unsigned) ((nw + 255) / 256), 256>>>(f->part_w, f->zsplit, nw, f->g + OFF_W + (size_t) (l - 1) * nw);
     const size_t sm = (size_t) 16 * (TILE + 8 * d) * 16 + (size_t) 16 * CH * 16 + 64;
     filter_conv_tc<<<dim3(LP / TILE, B), 128, sm>>>(f->dz[cur], f->dz[cur ^ 1], LP, W2, d, f->wtbf + (size_t) (l - 1) * KT * CH * CH,
                                                     nullptr, f->err, f->act[l - 1]);
     cur ^= 1;
   }
-  train_bias_grad<<<256, CH>>>(f->dz[cur], (long long) B * LP, f->g + OFF_B);
-  train_wgrad0<<<dim3(8, B), CH>>>(f->dz[cur], f->win, LP, W, f->g + OFF_W0);
+  train_bias_grad<<<NB_BIAS, CH>>>(f->dz[cur], (long long) B * LP, f->part_b);
+  train_sum_parts<<<1, CH>>>(f->part_b, NB_BIAS, CH, f->g + OFF_B);
+  train_wgrad0<<<NB_W0, CH>>>(f->dz[cur], f->win, B, LP, W2, f->part_w0);
+  train_sum_parts<<<(KT * 4 * CH + 255) / 256, 256>>>(f->part_w0, NB_W0, (long long) KT * 4 * CH, f->g + OFF_W0);
   if (lr > 0.f) {
     f->t++;
     const float b1 = 0.9f, b2 = 0.999f;

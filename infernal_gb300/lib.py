@@ -38,6 +38,7 @@ EXPORTS = [
     "cmgb_RefTrCYKScan", "cmgb_RefITrInsideScan", "cmgb_RefTrCYKScan_dev", "cmgb_RefITrInsideScan_dev",
     "cmgb_ScanBatch", "cmgb_ScanMulti", "cmgb_Calibrate", "cmgb_filter_trainer_create", "cmgb_filter_trainer_destroy",
     "cmgb_filter_trainer_set", "cmgb_filter_trainer_step", "cmgb_filter_trainer_get", "cmgb_filter_create", "cmgb_filter_destroy", "cmgb_filter_windows",
+    "cmgb_measure_issue_peak", "cmgb_ScanBatch_dev",
 ]
 BATCH_ALGOS = {"cyk": 0, "inside": 1, "finside": 2, "trcyk": 3, "trinside": 4}
 
@@ -99,6 +100,8 @@ def bind(path: str) -> ctypes.CDLL:
         f.restype = I
     lib.cmgb_ScanBatch.argtypes = [P, P, ctypes.c_char_p, I, I, I, P, I64, P, P, I, F, P, I, F, P, P, P, P, P]
     lib.cmgb_ScanBatch.restype = I
+    lib.cmgb_ScanBatch_dev.argtypes = lib.cmgb_ScanBatch.argtypes
+    lib.cmgb_ScanBatch_dev.restype = I
     lib.cmgb_ScanMulti.argtypes = [P, P, I, P, ctypes.c_char_p, I, I, P, I64, P, P, I, P, P, I, P, I, F, P, P, P, P]
     lib.cmgb_ScanMulti.restype = I
     lib.cmgb_Calibrate.argtypes = [P, P, ctypes.c_char_p, I, I64, I64, ctypes.c_uint64, I, P, P]
@@ -118,6 +121,8 @@ def bind(path: str) -> ctypes.CDLL:
     lib.cmgb_filter_destroy.argtypes = [P]
     lib.cmgb_filter_windows.argtypes = [P, P, P, I64, I64, P, I64, ctypes.POINTER(I64), ctypes.POINTER(F), ctypes.c_char_p]
     lib.cmgb_filter_windows.restype = I
+    lib.cmgb_measure_issue_peak.argtypes = [P, I, ctypes.POINTER(ctypes.c_double), ctypes.c_char_p]
+    lib.cmgb_measure_issue_peak.restype = I
     lib.cmgb_autotune.argtypes = [P, P, I, I, I64, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.c_char_p]
     lib.cmgb_autotune.restype = I
     lib.cmgb_FastCYKScan_noalloc.argtypes = [P, P, ctypes.c_char_p, I, P, I64, I64, F, F, P, I, ctypes.POINTER(I),
@@ -290,27 +295,43 @@ class Scanner:
 
     def scan_batch(self, m: cmfile.CMModel, seqs, algo: str = "cyk", qdbidx: int = 1, pass_idx: int = 4,
                    cutoff: float = 0.0, do_null3: bool = True, env_cutoff: float = 0.0, want_hits: bool = True,
-                   notgreedy: bool = False) -> List[ScanResult]:
+                   notgreedy: bool = False, ranges=None, device_buf=None) -> List[ScanResult]:
         """Runs cmgb_ScanBatch over a list of digital sequences (each an Easel
         dsq with sentinels), scanning each over [1, L]; returns one
-        ScanResult per sequence (vsc is None)."""
+        ScanResult per sequence (vsc is None).
+        ranges: instead of seqs, (buffer, offsets, lengths) -- sequences that
+        are sub-ranges of one residue buffer (sequence q: residues
+        buffer[offsets[q] + 1 .. offsets[q] + lengths[q]]);
+        device_buf: (device address, length) of that buffer already in device
+        memory (cmgb_ScanBatch_dev); buffer may then be None."""
         mh = self.model(m, CMGB_NOTGREEDY if notgreedy else 0)
-        parts = [np.ascontiguousarray(x, dtype=np.uint8) for x in seqs]
-        lens = np.array([len(x) - 2 for x in parts], np.int64)
-        offs = np.zeros(len(parts), np.int64)
-        if len(parts) > 1:
-            offs[1:] = np.cumsum([len(x) for x in parts[:-1]])
-        buf = np.concatenate(parts + [np.full(1, cmfile.DSQ_SENTINEL, np.uint8)])
-        nseq = len(parts)
+        if ranges is not None:
+            buf, offs, lens = ranges
+            offs = np.ascontiguousarray(offs, np.int64)
+            lens = np.ascontiguousarray(lens, np.int64)
+            nseq = len(offs)
+        else:
+            parts = [np.ascontiguousarray(x, dtype=np.uint8) for x in seqs]
+            lens = np.array([len(x) - 2 for x in parts], np.int64)
+            offs = np.zeros(len(parts), np.int64)
+            if len(parts) > 1:
+                offs[1:] = np.cumsum([len(x) for x in parts[:-1]])
+            buf = np.concatenate(parts + [np.full(1, cmfile.DSQ_SENTINEL, np.uint8)])
+            nseq = len(parts)
+        if nseq == 0:
+            return []
         nh, ei, ej = np.zeros(nseq, np.int64), np.zeros(nseq, np.int64), np.zeros(nseq, np.int64)
         sc, mode = np.zeros(nseq, np.float32), np.zeros(nseq, np.int32)
         hl = self.lib.cmgb_hitlist_create() if want_hits else None
         err = ctypes.create_string_buffer(256)
         try:
-            st = self.lib.cmgb_ScanBatch(self._ctx, mh, err, BATCH_ALGOS[algo], qdbidx, pass_idx, buf.ctypes.data,
-                                         len(buf), offs.ctypes.data, lens.ctypes.data, nseq, cutoff, hl,
-                                         int(do_null3), env_cutoff, nh.ctypes.data, ei.ctypes.data, ej.ctypes.data,
-                                         sc.ctypes.data, mode.ctypes.data)
+            if device_buf is not None:
+                fn, ptr, blen = self.lib.cmgb_ScanBatch_dev, device_buf[0], device_buf[1]
+            else:
+                fn, ptr, blen = self.lib.cmgb_ScanBatch, buf.ctypes.data, len(buf)
+            st = fn(self._ctx, mh, err, BATCH_ALGOS[algo], qdbidx, pass_idx, ptr, blen, offs.ctypes.data, lens.ctypes.data,
+                    nseq, cutoff, hl, int(do_null3), env_cutoff, nh.ctypes.data, ei.ctypes.data, ej.ctypes.data,
+                    sc.ctypes.data, mode.ctypes.data)
             if st != 0:
                 raise ScanError(st, err.value.decode())
             allhits = []
@@ -408,6 +429,17 @@ class Scanner:
         a, b = I64(), I64()
         self.lib.cmgb_ctx_last_transfer_bytes(self._ctx, ctypes.byref(a), ctypes.byref(b))
         return a.value, b.value
+
+    def issue_peak(self, kind: str = "f32") -> float:
+        """Measured arithmetic issue rate of this device (operations per second,
+        add and max counted separately) for the fp32 ("f32") or int32 ("i32")
+        add + max pair: the scan kernels' roofline denominator."""
+        v = ctypes.c_double()
+        err = ctypes.create_string_buffer(256)
+        st = self.lib.cmgb_measure_issue_peak(self._ctx, {"f32": 0, "i32": 1}[kind], ctypes.byref(v), err)
+        if st != 0:
+            raise ScanError(st, err.value.decode())
+        return v.value
 
     def last_launches(self) -> int:
         return int(self.lib.cmgb_ctx_last_launches(self._ctx))

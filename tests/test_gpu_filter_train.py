@@ -76,23 +76,36 @@ def _motif_batch(rng, B, W, motif):
     return wins, y
 
 
+def _motif_training(gpu, W, B, motif, steps=300):
+    """The motif task from a fixed seed: (loss per step, fp32 weights, exported weights)."""
+    rng = np.random.default_rng(11)
+    tr = prefilter.NativeTrainer(gpu, W, B, seed=1)
+    try:
+        losses = []
+        for it in range(steps):
+            x, y = _motif_batch(rng, B, W, motif)
+            loss, ms = tr.step(x, y, 1.0, 2e-3)
+            losses.append(loss)
+        return np.array(losses, np.float32), tr.get(), tr.weights(), ms
+    finally:
+        tr.close()
+
+
 def test_training_converges_and_loads_into_inference(gpu):
     import torch
     W, B = 64, 64
-    rng = np.random.default_rng(11)
     motif = np.array([2, 2, 2, 0, 1, 1, 1, 3, 0, 2], np.uint8)     # GGGACCCUAG
-    tr = prefilter.NativeTrainer(gpu, W, B, seed=1)
-    try:
-        first = None
-        for it in range(300):
-            x, y = _motif_batch(rng, B, W, motif)
-            loss, ms = tr.step(x, y, 1.0, 2e-3)
-            first = loss if first is None else first
-        print(f"loss {first:.3f} -> {loss:.3f}; last step {ms:.2f} ms")
-        assert loss < 0.5 * first
-        wts = tr.weights()
-    finally:
-        tr.close()
+    losses, w32, wts, ms = _motif_training(gpu, W, B, motif)
+    print(f"loss {losses[0]:.3f} -> {losses[-1]:.3f}; last step {ms:.2f} ms")
+    # the trainer's reductions have a fixed order: a second run from the same
+    # seed on the same batches repeats every loss and weight bit for bit
+    losses2, w32b, _, _ = _motif_training(gpu, W, B, motif)
+    print(f"second run: loss {losses2[0]:.3f} -> {losses2[-1]:.3f}")
+    assert np.array_equal(losses.view(np.uint32), losses2.view(np.uint32))
+    for a, b in zip(w32, w32b):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert losses[-1] < 0.5 * losses[0]
+    rng = np.random.default_rng(12)
     # held-out windows through the inference kernels: window k of a scan starts at 1 + kW
     x, y = _motif_batch(rng, 200, W, motif)
     seq = np.concatenate([[cmfile.DSQ_SENTINEL], x.ravel(), [cmfile.DSQ_SENTINEL]]).astype(np.uint8)
