@@ -1,43 +1,37 @@
-"""Benchmark of the plain GPU QDB scan (CYK filter + Inside on survivors).
+"""Benchmarks of the GPU QDB scanners; one JSON line per run.
 
-Workload (one "step"): a seeded synthetic target of --mb megabases at 40% GC
-with CM-emitted sequences embedded on random strands, scanned on BOTH strands
-with the clen-305 Plant_SRP CM (939 states, 4 bifurcations; the stand-in for
-the synthetic clen-300 multibranch CM of the single-large-CM configuration):
-  1. FastCYKScan, QDB1 bands (beta 1e-7), NULL3, greedy, filter cutoff
-  2. survivor hits padded by W-1 and merged into windows
-     (pli_cyk_seq_filter, src/cm_pipeline.c:3566-3601)
-  3. FastIInsideScan, QDB2 bands (beta 1e-15), NULL3, greedy, on each window.
-The default 10 steps x 2 Mb scan a 20 Mb slice of the configuration's 100 Mb
-target distribution (the rate does not depend on the slice length once every
-SM holds a window).
+Default workload (`--workload learned`, the learned-filter configuration):
+each step is a seeded synthetic target of --mb megabases (GC drawn per 50 kb
+segment from 0.35-0.60) with --hits-per-mb sequences emitted by the
+clen-305 Plant_SRP CM (939 states, 4 bifurcations) embedded on random
+strands, both strands held in device memory.  The learned pre-filter scores
+every window of both strands, the kept regions of both strands get the QDB1
+CYK scan (NULL3, greedy) in one batched launch, and the survivor windows of
+the CYK hits (padded by W-1 and merged: pli_cyk_seq_filter,
+src/cm_pipeline.c:3566-3601) get the QDB2 integer Inside scan in one more
+launch.  The same targets then go through the plain GPU pipeline (the
+single-launch CYK scan of each whole strand, then Inside on its survivor
+windows), which judges what the filter loses: the hits with E <= 0.01 (the
+model's Inside calibration, Z = all residues of the timed steps) that the
+plain pipeline reports and the filtered one misses.
+
+Other workloads: `plain` (the single-large-CM plain scan: Plant_SRP, GC
+0.40, 2 hits per Mb), `cfg1` (Vault, the clen-100 stand-in, 1 Mb at GC 0.50
+with 20 emitted hits, plain CYK -> Inside), `trunc` (the truncated-mode read
+batch: passes 2/3/4 of RefTrCYKScan + RefITrInsideScan on survivors),
+`multi` (the uneven multi-model batch in one persistent launch).
 
 Metric: residues scanned per second (both strands counted) and GCUPS (DP
-cells per second).  `value` uses residues already resident in device memory
-(the *_dev entry points); `e2e` calls the host-buffer C ABI (host->device
-copy of the residues and device->host hit lists inside every call).
+cells per second).  `value` uses residues already resident in device memory;
+`e2e` copies each step's residues from pinned host memory inside the timed
+region and reads every hit back to the host.
 
-`--workload trunc` runs the truncated-mode batch configuration instead: the
-same CM against --reads reads per step of length uniform 100-400 nt (30%
-CM-emitted sequences cut at a random 5' and/or 3' point, the rest iid ACGU at
-50% GC), each read scanned by RefTrCYKScan (QDB1) for passes 2, 3 and 4
-(5'-only, 3'-only, 5'+3' truncation) through the batched entry point
-(cmgb_ScanBatch, one launch per pass), and reads with a CYK survivor rescanned
-by RefITrInsideScan (QDB2) for that pass.  Residues count once per pass.
-
-`--workload multi` runs the uneven multi-model batch: a panel of the
-reference's calibrated CMs (clen 71-307; --cm-slots repeats them up to a
-larger count) against --seqs sequences per step (log-uniform 100-5,000 nt,
-45% GC, 5% carrying an emitted hit, both strands), every (CM, sequence) pair
-by FastCYKScan QDB1 in one multi-model persistent launch (cmgb_ScanMulti),
-timed beside one cmgb_ScanBatch launch per CM over the same sequences.
-Residues count once per (CM, sequence) pair.
-
-`--impl reference` times the reference's scanner on the host cores instead:
-the reference's own FastCYKScan/FastIInsideScan compiled from source
-(oracle/_ref) where that library exists, otherwise the C restatement of them
-(oracle/cm_scan_oracle.c), one process per core, on a bounded sample of the
-same workload.
+`--impl reference` times the reference's scanners on the host cores instead
+(the reference's own FastCYKScan/FastIInsideScan compiled from source,
+oracle/_ref, where that library exists, otherwise the C restatement of them,
+oracle/cm_scan_oracle.c), one process per core, each step a bounded sample
+of the same workload through the same CPU pipeline: CYK QDB1, then Inside
+QDB2 on the survivor windows.
 """
 from __future__ import annotations
 
@@ -81,14 +75,16 @@ def max_over_ranks(values, world, device="cuda"):
     return [float(x) for x in t]
 
 
-def make_step_input(model_glob, step, mb, seed=20261203, hits_per_mb=2.0, gc=0.40):
+def make_step_input(model_glob, step, mb, seed=20261203, hits_per_mb=2.0, gc=0.40, nhits=None):
     """One step's target and its reverse complement: iid background at GC gc
     (or per-50-kb segments of GC drawn from a (low, high) range) with
-    hits_per_mb emitted sequences embedded on random strands."""
+    hits_per_mb emitted sequences (at least one; or exactly nhits) embedded
+    on random strands."""
     from infernal_gb300 import emit
     rng = np.random.default_rng([seed, step])
     L = int(mb * 1_000_000)
-    nhits = max(1, int(round(hits_per_mb * mb)))     # default: 200 hits per 100 Mb
+    if nhits is None:
+        nhits = max(1, int(round(hits_per_mb * mb)))     # default: 200 hits per 100 Mb
     ins = [emit.sample(model_glob, rng) for _ in range(nhits)]
     dsq, spans = emit.make_target(rng, L, gc, ins)
     return dsq, emit.revcomp_dsq(dsq)
@@ -216,135 +212,239 @@ def run_trunc(args, rank, world):
     return out
 
 
-def _overlap(a, b):
-    return max(0, min(a[1], b[1]) - max(a[0], b[0]) + 1)
+CYK_PROFILE = "qdb_scan_cyk_plant_srp_1mb_global.md"     # ncu summary giving the CYK kernel's DRAM bytes per residue
+
+SPECS = {
+    # model, target GC, default Mb per step, hits per Mb, learned filter?
+    "learned": {"model": "Plant_SRP", "gc": (0.35, 0.60), "mb": 5.0, "hits_per_mb": 12.0, "filter": True, "seed": 500000},
+    "plain": {"model": "Plant_SRP", "gc": 0.40, "mb": 2.0, "hits_per_mb": 2.0, "filter": False, "seed": 0},
+    "cfg1": {"model": "Vault", "gc": 0.50, "mb": 1.0, "hits_per_mb": 20.0, "filter": False, "seed": 700000},
+}
 
 
-def run_learned(args, rank, world):
-    """Learned pre-filter + batched CYK -> Inside on the kept regions, against
-    the plain scan of everything on the same targets (which measures the hit loss)."""
+def spec_of(args):
+    sp = dict(SPECS[args.workload])
+    if args.mb is not None:
+        sp["mb"] = args.mb
+    if args.hits_per_mb is not None:
+        sp["hits_per_mb"] = args.hits_per_mb
+    sp["recall"] = args.filter_recall if args.filter_recall is not None else 0.99
+    return sp
+
+
+def load_model(name):
+    from infernal_gb300 import cmfile
+    p = os.path.join(ROOT, "tests", "golden", f"{name}.model.npz")
+    if not os.path.exists(p):
+        p = os.path.join(ROOT, "tests", "golden", "panel", f"{name}.model.npz")
+    return cmfile.load_npz(p)
+
+
+def pipeline_metric(sp):
+    if sp["filter"]:
+        return ("Mres/s scanned (both strands) on 1 GB300: learned pre-filter + batched QDB-CYK -> Inside, "
+                "against the plain GPU scan at <= 1% loss of E <= 0.01 hits")
+    return "Mres/s scanned (both strands) on 1 GB300: plain QDB-CYK -> Inside scan"
+
+
+def pipeline_config(sp, m, world):
+    gc = sp["gc"]
+    gcs = f"GC varying {gc[0]}-{gc[1]} per 50 kb segment" if isinstance(gc, tuple) else f"GC {gc}"
+    w = (f"{m.name} CM (M={m.M}, clen={m.clen}, W={m.W}), {sp['mb']} Mb x 2 strands per step, {gcs}, "
+         f"{sp['hits_per_mb']} emitted hits per Mb embedded on random strands; ")
+    if sp["filter"]:
+        w += (f"learned BF16 window pre-filter at its validation operating point of recall {sp['recall']} "
+              f"(windows holding an E <= 0.01 hit); kept regions of both strands -> ")
+    w += f"QDB1 CYK ({CYK_CUT} bits, NULL3, greedy) -> survivor windows -> QDB2 integer Inside ({INS_CUT} bits)"
+    return {"workload": w, "residues_per_step": int(2 * round(sp["mb"] * 1e6)),
+            "l2": "flushed between timed steps (256 MB write)",
+            "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def kernel_block(name, bound, achieved, peak, unit, note, traffic=None):
+    return {"kernel": name, "bound": bound, "achieved": round(achieved, 4), "peak": round(peak, 3), "unit": unit,
+            "frac": round(achieved / peak, 5) if peak else None, "traffic": traffic, "note": note}
+
+
+def profile_dram_per_residue(name):
+    """DRAM bytes per scanned residue of a kernel, from its committed ncu summary."""
+    import re
+    p = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(p):
+        return None
+    mt = re.search(r"^dram_bytes_per_residue:\s*([0-9.]+)", open(p).read(), re.M)
+    return float(mt.group(1)) if mt else None
+
+
+def run_pipeline(args, rank, world):
+    """learned / plain / cfg1: the CYK -> Inside pipeline over both strands of
+    each step's target, with (learned) or without the pre-filter."""
     import torch
-    from infernal_gb300 import cmfile, lib as L, prefilter
-    m = cmfile.load_npz(os.path.join(ROOT, "tests", "golden", "Plant_SRP.model.npz"))
-    wts = prefilter.load(args.filter or os.path.join(ROOT, "infernal_gb300", "filters", "Plant_SRP.filter.npz"))
-    torch.cuda.set_device(0)
-    sc = L.Scanner(0)
-    filt = prefilter.Prefilter(sc, wts, m.W)
-    if args.filter_recall is not None:
-        filt.use_recall(args.filter_recall)
+    from infernal_gb300 import lib as L, prefilter
+    sp = spec_of(args)
+    m = load_model(sp["model"])
+    dev = 0 if world == 1 else _env_int("LOCAL_RANK", 0)
+    torch.cuda.set_device(dev)
+    sc = L.Scanner(dev)
+    filt = None
+    if sp["filter"]:
+        wts = prefilter.load(args.filter or os.path.join(ROOT, "infernal_gb300", "filters", f"{m.name}.filter.npz"))
+        filt = prefilter.Prefilter(sc, wts, m.W)
+        if filt.points is not None:
+            filt.use_recall(sp["recall"])
     nsteps = args.warmup + args.steps
-    inputs = [make_step_input(m, 500000 + s, args.mb, hits_per_mb=args.hits_per_mb, gc=(0.35, 0.60))
+    inputs = [prefilter.strand_buffer(make_step_input(m, rank_step_seed(rank, sp["seed"] + s), sp["mb"],
+                                                      hits_per_mb=sp["hits_per_mb"], gc=sp["gc"])[0])
               for s in range(nsteps)]
-    Lres = len(inputs[0][0]) - 2
+    nbuf = len(inputs[0])
+    Lres = (nbuf - 3) // 2
+    host = [torch.from_numpy(x).pin_memory() for x in inputs]
+    devb = [h.to("cuda") for h in host]
+    dstage = torch.empty(nbuf, dtype=torch.uint8, device="cuda")        # e2e: each step's copy lands here
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    sc.autotune(m, 1, "cyk"); sc.autotune(m, 2, "inside")
+    tuned = {"cyk_qdb1": sc.autotune(m, 1, "cyk"), "inside_qdb2": sc.autotune(m, 2, "inside")}
+    work = {"cyk": Work(m, 1), "inside": Work(m, 2)}
 
-    def regions_scan(dsq, regs, algo, qdb, cut):
-        """Batched scan of sub-ranges [a, b] of one strand; hits in strand coordinates."""
-        if not regs:
-            return [], 0.0
-        buf = np.ascontiguousarray(dsq, np.uint8)
-        offs = np.array([a - 1 for a, b in regs], np.int64)
-        lens = np.array([b - a + 1 for a, b in regs], np.int64)
-        import ctypes
-        nh = np.zeros(len(regs), np.int64)
-        hl = sc.lib.cmgb_hitlist_create()
-        err = ctypes.create_string_buffer(256)
-        st = sc.lib.cmgb_ScanBatch(sc._ctx, sc.model(m), err, L.BATCH_ALGOS[algo], qdb, 0, buf.ctypes.data, len(buf),
-                                   offs.ctypes.data, lens.ctypes.data, len(regs), cut, hl, 1, cut, nh.ctypes.data,
-                                   None, None, None, None)
-        if st != 0:
-            raise L.ScanError(st, err.value.decode())
-        hits, h, k = [], L.Hit(), 0
-        for q in range(len(regs)):
-            for _ in range(int(nh[q])):
-                sc.lib.cmgb_hitlist_get(hl, k, ctypes.byref(h)); k += 1
-                hits.append((h.start + int(offs[q]), h.stop + int(offs[q]), h.score))
-        sc.lib.cmgb_hitlist_destroy(hl)
-        return hits, float(sc.lib.cmgb_ctx_last_kernel_ms(sc._ctx))
+    def run(ptr):
+        if filt is not None:
+            return prefilter.filtered_scan(sc, filt, m, ptr, nbuf, CYK_CUT, INS_CUT)
+        return prefilter.plain_scan(sc, m, ptr, nbuf, CYK_CUT, INS_CUT)
 
-    def filtered_step(strands, dptrs):
-        out, ms, kept = [], 0.0, 0
-        for dsq, ptr in zip(strands, dptrs):
-            logit, fms = filt.logits(ptr, 1, Lres)
-            ms += fms
-            regs = filt.regions(logit, 1, Lres)
-            kept += sum(b - a + 1 for a, b in regs)
-            cyk, k1 = regions_scan(dsq, regs, "cyk", 1, CYK_CUT)
-            wins = windows_from_hits([(h[0], h[1]) for h in cyk], m.W, Lres)
-            ins, k2 = regions_scan(dsq, wins, "inside", 2, INS_CUT)
-            ms += k1 + k2
-            out.append(ins)
-        return out, ms, kept
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
 
-    def plain_step(strands, dptrs):
-        out = []
-        for dsq, ptr in zip(strands, dptrs):
-            r = sc.scan(m, dsq, 1, Lres, algo="cyk", qdbidx=1, cutoff=CYK_CUT, env_cutoff=CYK_CUT, device_ptr=ptr)
-            ins = []
-            for a, b in windows_from_hits(r.hits, m.W, Lres):
-                r2 = sc.scan(m, dsq, a, b, algo="inside", qdbidx=2, cutoff=INS_CUT, env_cutoff=INS_CUT, device_ptr=ptr)
-                ins += [(h[0], h[1], h[4]) for h in r2.hits]
-            out.append(ins)
-        return out
-
-    dev = [[torch.from_numpy(x).to("cuda") for x in inp] for inp in inputs]
-    torch.cuda.synchronize()
     for s in range(args.warmup):
-        filtered_step(inputs[s], [t.data_ptr() for t in dev[s]])
+        run(devb[s].data_ptr())
+    # timed: residues resident in device memory
     clk = start_clock_sampler(rank)
-    tot, kms, kept, fhits = 0.0, 0.0, 0, []
+    tot, hits, sts = 0.0, [], []
     for s in range(args.warmup, nsteps):
         flush.fill_(float(s))
-        torch.cuda.synchronize()
+        barrier()
         t0 = time.perf_counter()
-        h, k, kp = filtered_step(inputs[s], [t.data_ptr() for t in dev[s]])
-        torch.cuda.synchronize()
+        h, st = run(devb[s].data_ptr())
+        barrier()
         tot += time.perf_counter() - t0
-        kms += k; kept += kp; fhits.append(h)
+        hits.append(h); sts.append(st)
     clocks = stop_clock_sampler(clk)
-    # the hit-loss reference: the plain scan of everything on the same steps (timed too)
-    t0 = time.perf_counter()
-    phits = [plain_step(inputs[s], [t.data_ptr() for t in dev[s]]) for s in range(args.warmup, nsteps)]
-    t_plain = time.perf_counter() - t0
-    # E <= 0.01 at this search size from the CM's local Inside calibration
-    # (ECMLI line of Plant_SRP.c.cm: lambda, mu_extrap, calibration db size,
-    # random hits): E = nrandhits * Z / dbsize * exp(-lambda (S - mu)), Z = residues per step
-    lam, mu, cdb, nrand = 0.70748, -9.17856, 1600000.0, 519142.0
-    e_bits = mu - np.log(0.01 / (nrand * (2 * Lres) / cdb)) / lam
-    nplain = nfound = ne = nef = 0
-    for ph, fh in zip(phits, fhits):
-        for sp, sf in zip(ph, fh):
-            for h in sp:
-                found = any(_overlap(h, g) >= 0.5 * (h[1] - h[0] + 1) for g in sf)
-                nplain += 1; nfound += found
-                if h[2] >= e_bits:
-                    ne += 1; nef += found
+    # e2e: the step's residues copied from pinned host memory inside the timed region
+    t_e2e, h2d, d2h = 0.0, 0, 0
+    for s in range(args.warmup, nsteps):
+        flush.fill_(float(s))
+        barrier()
+        t0 = time.perf_counter()
+        dstage.copy_(host[s], non_blocking=True)
+        torch.cuda.current_stream().synchronize()     # the scans run on the library's own stream
+        h, st = run(dstage.data_ptr())
+        barrier()
+        t_e2e += time.perf_counter() - t0
+        h2d += nbuf + st["h2d"]; d2h += st["d2h"]
+    t_dev, t_e2e = max_over_ranks([tot, t_e2e], world)
     res = 2 * Lres * args.steps
-    value = res / tot / 1e6
+    kms = {k: sum(st["kernel_ms"][k] for st in sts) for k in ("filter", "cyk", "inside")}
+    lens = {k: [n for st in sts for n in st["lengths"][k]] for k in ("cyk", "inside")}
+    ops = {k: sum(work[k].ops(n) for n in lens[k]) for k in lens}
+    cells = {k: sum(work[k].cells(n) for n in lens[k]) for k in lens}
+    launches = sum(st["launches"] for st in sts)
     out = {
-        "metric": "Mres/s scanned (both strands): learned pre-filter + batched QDB-CYK + Inside vs the plain GPU scan",
-        "value": round(value, 3), "unit": "Mres/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(1000 * tot / args.steps, 3), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "bf16 (filter) + f32 (CYK) + int32 (Inside)", "data": "synthetic",
-        "config": {"workload": f"Plant_SRP CM stand-in, {args.mb} Mb x 2 strands per step, GC varying 0.35-0.60 "
-                               f"per 50 kb segment, "
-                               f"{args.hits_per_mb} emitted hits per Mb; filter threshold "
-                               f"{filt.thr:.3f} (validation recall {args.filter_recall or 0.99} of windows with an "
-                               f"E <= 0.01 hit); kept regions scanned by CYK QDB1 ({CYK_CUT} bits) -> Inside QDB2 ({INS_CUT} bits)",
-                   "l2": "flushed between timed steps (256 MB write)", "parallelism": "1 GPU"},
-        "plain_mres_s": round(res / t_plain / 1e6, 3),
-        "speedup_vs_plain": round(t_plain / tot, 2),
-        "fraction_scanned": round(kept / res, 4),
-        "hits_plain": nplain, "hits_found": nfound,
-        "hit_loss": round(1.0 - nfound / nplain, 4) if nplain else None,
-        "e001_bits": round(float(e_bits), 2), "e001_hits_plain": ne, "e001_hits_found": nef,
-        "e001_hit_loss": round(1.0 - nef / ne, 4) if ne else None,
-        "kernel_ms_per_step": round(kms / args.steps, 3),
+        "metric": pipeline_metric(sp),
+        "value": round(res * world / t_dev / 1e6, 3), "unit": "Mres/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1000 * t_dev / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": ("bf16 (filter) + " if filt else "") + "f32 (CYK) + int32 (Inside)", "data": "synthetic",
+        "config": pipeline_config(sp, m, world),
+        "gcups": round((cells["cyk"] + cells["inside"]) * world / t_dev / 1e9, 2),
+        "e2e": {"value": round(res * world / t_e2e / 1e6, 3), "unit": "Mres/s",
+                "h2d_bytes_per_step": int(h2d / args.steps), "d2h_bytes_per_step": int(d2h / args.steps)},
+        "kernel_ms_per_step": {k: round(v / args.steps, 3) for k, v in kms.items()},
+        "fraction_scanned": round(sum(st["kept"] for st in sts) / res, 4),
+        "gpu_launches": launches,
+        "tuned_shapes": {k: {"tile_rows": v[0], "arena": "global" if v[1] == 2 else "shared"} for k, v in tuned.items()},
         "clocks": clocks,
     }
-    filt.close(); sc.close()
+    # roofline: measured issue peaks (this device) and the measured tensor peak
+    peaks, pkind = measured_peaks()
+    f32, i32 = sc.issue_peak("f32") / 1e12, sc.issue_peak("i32") / 1e12
+    blocks = {}
+    if kms["cyk"] > 0:
+        ncall = max(1, sum(st["calls"]["cyk"] for st in sts))
+        tr = profile_dram_per_residue(CYK_PROFILE)
+        blocks["cyk"] = kernel_block("qdb_scan_kernel<CYK>", "fp32 add+max issue", ops["cyk"] / (kms["cyk"] / 1e3) / 1e12,
+                                     f32, "Tops/s", "algorithmic DP operations of the CYK cells scanned, per kernel "
+                                     "second (CUDA events); peak: cmgb_measure_issue_peak fp32 on this device; "
+                                     "traffic: DRAM bytes per residue of the committed ncu summary x residues per launch",
+                                     traffic=round(tr * sum(lens["cyk"]) / ncall) if tr else None)
+    if kms["inside"] > 0:
+        blocks["inside"] = kernel_block("qdb_scan_kernel<IInside>", "int32 add+max issue",
+                                        ops["inside"] / (kms["inside"] / 1e3) / 1e12, i32, "Tops/s",
+                                        "algorithmic operations (adds + ILogsum combines) per kernel second; "
+                                        "peak: cmgb_measure_issue_peak int32 on this device")
+    if filt is not None and kms["filter"] > 0:
+        nwin = sum(-(-Lres // m.W) for _ in range(2)) * args.steps
+        flops = 2.0 * nwin * (2 * m.W) * 9 * 128 * 128 * 5
+        blocks["filter"] = kernel_block("filter_conv_tc (tcgen05)", "tensor", flops / (kms["filter"] / 1e3) / 1e12,
+                                        float(peaks.get("bf16_tflops", 1900.0)), "TFLOP/s",
+                                        f"dilated layers' GEMM FLOPs over the 2W positions of every window; peak: "
+                                        f"{pkind} bf16 burst (MEASURED_PEAKS.json)")
+    dom = max(blocks, key=lambda k: kms[k]) if blocks else None
+    if dom:
+        r = dict(blocks[dom])
+        r["kernels"] = blocks
+        r["dominant_share_of_kernel_time"] = round(kms[dom] / max(1e-9, sum(kms.values())), 3)
+        r["peaks_measured"] = {"fp32_add_max_tops": round(f32, 2), "int32_add_max_tops": round(i32, 2),
+                               "sm_count": torch.cuda.get_device_properties(dev).multi_processor_count}
+        out["roofline"] = r
+    if filt is not None:
+        # the judge: the plain pipeline on the same targets
+        run_plain = lambda ptr: prefilter.plain_scan(sc, m, ptr, nbuf, CYK_CUT, INS_CUT)
+        run_plain(devb[0].data_ptr())
+        t_plain, phits, pk = 0.0, [], 0.0
+        for s in range(args.warmup, nsteps):
+            flush.fill_(float(s))
+            barrier()
+            t0 = time.perf_counter()
+            h, st = run_plain(devb[s].data_ptr())
+            barrier()
+            t_plain += time.perf_counter() - t0
+            phits.append(h); pk += st["kernel_ms"]["cyk"] + st["kernel_ms"]["inside"]
+        e_bits = float(L.bits_at_evalue(m.ecm["ECMLI"], 0.01, float(res)))
+        nplain = nfound = ne = nef = 0
+        for ph, fh in zip(phits, hits):
+            for sp_, sf in zip(ph, fh):
+                for hh in sp_:
+                    found = any(_overlap(hh, g) >= 0.5 * (hh[1] - hh[0] + 1) for g in sf)
+                    nplain += 1; nfound += found
+                    if hh[2] >= e_bits:
+                        ne += 1; nef += found
+        out.update({
+            "plain_mres_s": round(res / t_plain / 1e6, 3),
+            "speedup_vs_plain": round(t_plain / tot, 3),
+            "plain_kernel_ms_per_step": round(pk / args.steps, 3),
+            "e001_bits": round(e_bits, 2), "e001_hits_plain": ne, "e001_hits_found": nef,
+            "e001_hit_loss": round(1.0 - nef / ne, 4) if ne else None,
+            "hits_plain": nplain, "hits_found": nfound,
+            "filter_threshold": round(filt.thr, 4),
+        })
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(m, inputs[args.warmup][: Lres + 2], seconds=args.cpu_seconds)
+    if filt is not None:
+        filt.close()
+    sc.close()
     return out
+
+
+def _overlap(a, b):
+    return max(0, min(a[1], b[1]) - max(a[0], b[0]) + 1)
 
 
 PANEL = ["tRNA", "Vault", "Plant_SRP", "tRNA1415G", "snR75", "tRNA-Sec", "srp-euk", "rnaseP-eubact",
@@ -466,122 +566,6 @@ def run_multi(args, rank, world):
     return out
 
 
-# ----------------------------------------------------------------------------
-def run_ours(args, rank, world):
-    import torch
-    from infernal_gb300 import cmfile, lib as L
-    mpath = os.path.join(ROOT, "tests", "golden", "Plant_SRP.model.npz")
-    m = cmfile.load_npz(mpath)
-    torch.cuda.set_device(0 if world == 1 else _env_int("LOCAL_RANK", 0))
-    dev = torch.cuda.current_device()
-    sc = L.Scanner(dev)
-    keep = []
-    desc = cmfile.make_desc(m, keep=keep)
-    lib = sc.lib
-    import ctypes
-
-    nsteps = args.warmup + args.steps
-    inputs = [make_step_input(m, rank_step_seed(rank, s), args.mb) for s in range(nsteps)]
-    Lres = len(inputs[0][0]) - 2
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-
-    # untimed set-up: the autotuner picks the tile shape of each band set / algorithm
-    tuned = {"cyk_qdb1": sc.autotune(m, 1, "cyk"), "inside_qdb2": sc.autotune(m, 2, "inside")}
-    xfer = [0, 0]
-
-    opr = {1: dp_ops_per_residue(m, 1), 2: dp_ops_per_residue(m, 2)}
-    ops_acc = [0]
-
-    def step(strands, dev_ptrs):
-        """One pass; returns (hits, cells, kernel_ms, launches)."""
-        cells = 0
-        kms = 0.0
-        launches = 0
-        nh = 0
-        xfer[0] = xfer[1] = 0
-        for k, dsq in enumerate(strands):
-            ptr = dev_ptrs[k] if dev_ptrs else None
-            r = sc.scan(m, dsq, 1, Lres, algo="cyk", qdbidx=1, cutoff=CYK_CUT, env_cutoff=CYK_CUT,
-                        device_ptr=ptr)
-            kms += r.kernel_ms; launches += sc.last_launches()
-            hb, db = sc.last_transfer_bytes(); xfer[0] += hb; xfer[1] += db
-            cells += lib.cmgb_count_cells(ctypes.byref(desc), 1, Lres)
-            ops_acc[0] += opr[1] * Lres
-            for a, b in windows_from_hits(r.hits, m.W, Lres):
-                r2 = sc.scan(m, dsq, a, b, algo="inside", qdbidx=2, cutoff=INS_CUT, env_cutoff=INS_CUT,
-                             device_ptr=ptr)
-                kms += r2.kernel_ms; launches += sc.last_launches()
-                hb, db = sc.last_transfer_bytes(); xfer[0] += hb; xfer[1] += db
-                cells += lib.cmgb_count_cells(ctypes.byref(desc), 2, b - a + 1)
-                ops_acc[0] += opr[2] * (b - a + 1)
-                nh += len(r2.hits)
-        return nh, cells, kms, launches
-
-    def barrier():
-        if world > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize()
-
-    def timed(use_dev):
-        dev_inputs = []
-        if use_dev:
-            for s in range(nsteps):
-                dev_inputs.append([torch.from_numpy(x).to("cuda") for x in inputs[s]])
-        torch.cuda.synchronize()
-        for s in range(args.warmup):
-            step(inputs[s], [t.data_ptr() for t in dev_inputs[s]] if use_dev else None)
-        tot, cells, kms, launches, nh = 0.0, 0, 0.0, 0, 0
-        ops_acc[0] = 0
-        for s in range(args.warmup, nsteps):
-            flush.fill_(float(s))                  # evict L2 between timed steps
-            barrier()
-            t0 = time.perf_counter()
-            h, c, k, l = step(inputs[s], [t.data_ptr() for t in dev_inputs[s]] if use_dev else None)
-            barrier()
-            tot += time.perf_counter() - t0
-            cells += c; kms += k; launches += l; nh += h
-        del dev_inputs
-        return tot, cells, kms, launches, nh
-
-    clk = start_clock_sampler(rank)
-    t_dev, cells, kms, launches, nh = timed(True)
-    ops = ops_acc[0]
-    clocks = stop_clock_sampler(clk)
-    t_e2e, _, _, _, _ = timed(False)
-    h2d_step, d2h_step = xfer[0], xfer[1]     # transfers of the last host-buffer step
-    t_dev, t_e2e = max_over_ranks([t_dev, t_e2e], world)
-    res_per_rank = 2 * Lres * args.steps
-    total_res = res_per_rank * world
-    value = total_res / t_dev / 1e6
-    e2e = total_res / t_e2e / 1e6
-    out = {
-        "metric": "Mres/s scanned (both strands), plain GPU QDB-CYK + Inside scan",
-        "value": round(value, 3), "unit": "Mres/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(1000 * t_dev / args.steps, 3), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (CYK) + int32 (Inside)", "data": "synthetic",
-        "config": {"workload": f"Plant_SRP CM stand-in (M={m.M}, clen={m.clen}, W={m.W}, 4 B), "
-                               f"{args.mb} Mb x 2 strands per step, GC 0.40, {max(1, round(2 * args.mb))} emitted hits per step; "
-                               f"CYK QDB1 cutoff {CYK_CUT} bits -> Inside QDB2 cutoff {INS_CUT} bits, NULL3, greedy",
-                   "residues_per_step": 2 * Lres, "l2": "flushed between timed steps (256 MB write)",
-                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
-        "gcups": round(cells * world / t_dev / 1e9, 2),
-        "kernel_gcups": round(cells / (kms / 1e3) / 1e9, 2) if kms > 0 else None,
-        "kernel_ms_per_step": round(kms / args.steps, 3),
-        "e2e": {"value": round(e2e, 3), "unit": "Mres/s", "h2d_bytes_per_step": h2d_step,
-                "d2h_bytes_per_step": d2h_step},
-        "tuned_shapes": {k: {"tile_rows": v[0], "arena": "global" if v[1] == 2 else "shared"} for k, v in tuned.items()},
-        "gpu_launches": launches,
-        "hits_per_step": nh / args.steps,
-        "clocks": clocks,
-    }
-    out["roofline"] = roofline_block(cells, kms, Lres, args)
-    out["alu_roofline"] = alu_roofline(ops, kms, clocks)
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(m, inputs[args.warmup][0], threads=1, seconds=args.cpu_seconds)
-    sc.close()
-    return out
-
-
 def work_per_d(m, qdbidx):
     """(cells[d], ops[d]) for d = 0..W: the DP cells of length d summed over
     the non-E states whose band holds d (QDB bands capped at W, MP from
@@ -649,95 +633,78 @@ def dp_ops_per_residue(m, qdbidx):
     return int(work_per_d(m, qdbidx)[1].sum())
 
 
-def alu_roofline(ops, kms, clocks):
-    """The DP's own roof: FP32/INT32 non-tensor issue (one operation per lane
-    per clock; 152 SMs x 128 lanes)."""
-    mhz = (clocks or {}).get("sm_max_mhz") or 2070.0
-    peak = 152 * 128 * mhz * 1e6 / 1e12
-    ach = ops / (kms / 1e3) / 1e12 if kms > 0 else 0.0
-    return {"bound": "fp32/int32 non-tensor issue", "achieved": round(ach, 4), "peak": round(peak, 2),
-            "unit": "Tops/s", "frac": round(ach / peak, 5),
-            "note": "algorithmic DP operations (adds + max/log-sum combines) per kernel second"}
-
-
-def roofline_block(cells, kms, Lres, args):
-    """The scan kernel is not bandwidth bound: its algorithmic DRAM traffic is
-    the residues (1 byte each) and the hit records; the DP state stays in
-    shared memory / L2.  Reported against the measured HBM copy peak."""
-    peaks = {}
-    try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
-            peaks = json.load(fh)
-    except OSError:
-        pass
-    peak = float(peaks.get("hbm_gbs", 6800.0))
-    alg_bytes = 2 * (Lres + 2) * args.steps
-    ach = alg_bytes / (kms / 1e3) / 1e9 if kms > 0 else 0.0
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", "qdb_scan_cyk_plant_srp_1mb_global.md")
-    if os.path.exists(prof):      # DRAM bytes per residue of one ncu capture of the CYK kernel, scaled
-        import re
-        mt = re.search(r"^dram_bytes_per_residue:\s*([0-9.]+)", open(prof).read(), re.M)
-        if mt:
-            traffic = float(mt.group(1)) * (Lres + 2)     # per CYK launch (one strand)
-    return {"bound": "hbm", "achieved": round(ach, 4), "peak": peak, "unit": "GB/s",
-            "frac": round(ach / peak, 8), "traffic": traffic,
-            "note": "algorithmic bytes = residues only; traffic = the CYK kernel's measured DRAM bytes per residue "
-                    "(ncu, 1 Mb capture: tile-arena re-reads past L2) times the residues of one CYK launch; "
-                    "the DP is bound by ALU issue and latency, see alu_roofline and the cell rate"}
-
-
-def cpu_baseline(m, dsq, threads=1, seconds=10.0):
-    """Times the CPU scanner (reference build if present, else the oracle port)
-    on a prefix of one strand, sized to about `seconds` of work."""
+def cpu_pipeline(m, dsq, n, use_ref):
+    """The CPU pipeline on residues 1..n of one strand: FastCYKScan QDB1
+    (NULL3, greedy, cutoff CYK_CUT), then FastIInsideScan QDB2 on each
+    survivor window (cutoff INS_CUT) -- the reference's scanners when
+    use_ref, else their C restatement."""
     import oracle
+    hits = oracle.scan(m, dsq, 1, n, algo="cyk", qdbidx=1, cutoff=CYK_CUT, env_cutoff=CYK_CUT, reference=use_ref)[0]
+    nwin = 0
+    for a, b in windows_from_hits(hits, m.W, n):
+        oracle.scan(m, dsq, a, b, algo="inside", qdbidx=2, cutoff=INS_CUT, env_cutoff=INS_CUT, reference=use_ref)
+        nwin += 1
+    return nwin
+
+
+def cpu_baseline(m, dsq, seconds=10.0):
+    """The CPU pipeline (reference build if present, else the C restatement)
+    on one host core over a prefix of one strand, sized to about `seconds`."""
+    import oracle
+    oracle.build_oracle()
     use_ref = os.path.exists(oracle.REF_SO)
     n = 2000
     t0 = time.perf_counter()
-    oracle.scan(m, dsq, 1, n, algo="cyk", qdbidx=1, cutoff=CYK_CUT, env_cutoff=CYK_CUT, reference=use_ref)
+    cpu_pipeline(m, dsq, n, use_ref)
     dt = time.perf_counter() - t0
     n2 = int(min(len(dsq) - 2, max(n, n * seconds / max(dt, 1e-3))))
     t0 = time.perf_counter()
-    oracle.scan(m, dsq, 1, n2, algo="cyk", qdbidx=1, cutoff=CYK_CUT, env_cutoff=CYK_CUT, reference=use_ref)
+    nw = cpu_pipeline(m, dsq, n2, use_ref)
     dt = time.perf_counter() - t0
-    return {"value": round(n2 / dt / 1e6, 6), "unit": "Mres/s", "cores": threads,
+    return {"value": round(n2 / dt / 1e6, 6), "unit": "Mres/s", "cores": 1,
             "kind": "reference" if use_ref else "port",
-            "sample": f"FastCYKScan QDB1 over the first {n2} residues of one strand of the step-{0} target"}
+            "sample": f"CYK QDB1 over the first {n2} residues of the first timed step's top strand, then Inside QDB2 "
+                      f"on its {nw} survivor windows, one core"}
 
 
 def _ref_worker(argv):
-    mb, idx, nres, use_ref = argv
-    import oracle
-    from infernal_gb300 import cmfile
-    m = cmfile.load_npz(os.path.join(ROOT, "tests", "golden", "Plant_SRP.model.npz"))
-    dsq, _ = make_step_input(m, 1000 + idx, min(mb, 0.1))
+    workload, mb, hits_per_mb, gc, seed, nres, use_ref = argv
+    sp = SPECS[workload]
+    m = load_model(sp["model"])
+    mb = max(nres / 1e6, 0.002) + 0.001
+    nh = int(np.random.default_rng([seed, 1]).poisson(hits_per_mb * nres / 1e6))   # the workload's hit density
+    dsq, _ = make_step_input(m, seed, mb, hits_per_mb=hits_per_mb, gc=gc, nhits=nh)
     t0 = time.perf_counter()
-    oracle.scan(m, dsq, 1, nres, algo="cyk", qdbidx=1, cutoff=CYK_CUT, env_cutoff=CYK_CUT, reference=use_ref)
+    cpu_pipeline(m, dsq, nres, use_ref)
     return nres, time.perf_counter() - t0
 
 
 def run_reference(args, rank, world):
-    """CPU reference arm: all host cores, one process per core."""
+    """CPU reference arm: the workload's CPU pipeline on all host cores, one
+    process per core, each step a bounded sample of the workload."""
     import multiprocessing as mp
     import oracle
-    from infernal_gb300 import cmfile
+    if args.workload not in SPECS:
+        return {"impl": "reference", "unavailable": f"the {args.workload} workload has no CPU reference arm here"}
     oracle.build_oracle()
     use_ref = os.path.exists(oracle.REF_SO)
     ncpu = len(os.sched_getaffinity(0))
-    m = cmfile.load_npz(os.path.join(ROOT, "tests", "golden", "Plant_SRP.model.npz"))
+    sp = spec_of(args)
+    m = load_model(sp["model"])
     # size the per-process sample from a short single-process probe
-    dsq, _ = make_step_input(m, 999, 0.01)
+    dsq, _ = make_step_input(m, 999, 0.01, hits_per_mb=0.0, gc=sp["gc"])
     t0 = time.perf_counter()
-    oracle.scan(m, dsq, 1, 1500, algo="cyk", qdbidx=1, cutoff=CYK_CUT, reference=use_ref)
+    cpu_pipeline(m, dsq, 1500, use_ref)
     rate = 1500 / (time.perf_counter() - t0)
-    per_step_s = max(2.0, args.ref_step_seconds)
-    nres = int(max(1500, min(90000, rate * per_step_s)))
+    nres = int(max(1500, min(200000, rate * max(2.0, args.ref_step_seconds))))
     ctx = mp.get_context("spawn")
     times = []
     with ctx.Pool(ncpu) as pool:
         for s in range(args.warmup + args.steps):
+            jobs = [(args.workload, sp["mb"], sp["hits_per_mb"], sp["gc"], 900000 + s * ncpu + k, nres, use_ref)
+                    for k in range(ncpu)]
             t0 = time.perf_counter()
-            res = pool.map(_ref_worker, [(args.mb, s * ncpu + k, nres, use_ref) for k in range(ncpu)])
+            res = pool.map(_ref_worker, jobs)
             dt = time.perf_counter() - t0
             if s >= args.warmup:
                 times.append((sum(r[0] for r in res), dt))
@@ -745,14 +712,15 @@ def run_reference(args, rank, world):
     tot_t = sum(t[1] for t in times)
     v = tot_res / tot_t / 1e6
     return {
-        "impl": "reference", "metric": "Mres/s scanned (both strands), plain GPU QDB-CYK + Inside scan",
+        "impl": "reference", "metric": pipeline_metric(sp),
         "value": round(v, 6), "unit": "Mres/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1000 * tot_t / args.steps, 3), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (CYK)", "data": "synthetic",
-        "config": {"workload": "same model and target distribution as the GPU arm; CYK QDB1 filter scan per core",
-                   "parallelism": f"{ncpu} host processes"},
+        "vs_baseline": None, "dtype": "f32 (CYK) + int32 (Inside)", "data": "synthetic",
+        "config": pipeline_config(sp, m, 1),
         "cpu_baseline": {"value": round(v, 6), "unit": "Mres/s", "cores": ncpu, "kind": "reference" if use_ref else "port",
-                         "sample": f"{nres} residues per process per step, {ncpu} processes"},
+                         "sample": f"per step {ncpu} processes, each: CYK QDB1 over {nres} residues of a fresh target of "
+                                   f"this workload's distribution, then Inside QDB2 on its survivor windows "
+                                   f"(the reference has no learned filter: its pipeline scans everything)"},
         "e2e": {"value": round(v, 6), "unit": "Mres/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -810,23 +778,24 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--mb", type=float, default=2.0, help="megabases of target per step (scanned on both strands)")
+    ap.add_argument("--mb", type=float, default=None, help="megabases of target per step, scanned on both strands "
+                                                           "(default: the workload's)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="plain", choices=["plain", "trunc", "learned", "multi"],
-                    help="plain: the single-large-CM scan (default); trunc: the truncated-mode read batch; "
-                         "learned: the pre-filtered pipeline against the plain scan; multi: the uneven "
-                         "multi-model batch")
+    ap.add_argument("--workload", default="learned", choices=["learned", "plain", "cfg1", "trunc", "multi"],
+                    help="learned: the pre-filtered pipeline against the plain scan (default); plain: the "
+                         "single-large-CM plain scan; cfg1: the clen-100 plain scan; trunc: the truncated-mode read "
+                         "batch; multi: the uneven multi-model batch")
     ap.add_argument("--seqs", type=int, default=300, help="sequences per step of the multi workload (x 2 strands)")
     ap.add_argument("--cm-slots", type=int, default=0, help="CM slots of the multi workload (default: the panel)")
     ap.add_argument("--reads", type=int, default=5000, help="reads per step of the trunc workload")
-    ap.add_argument("--hits-per-mb", type=float, default=2.0, help="embedded hits per Mb (learned workload)")
-    ap.add_argument("--filter", default=None, help="learned workload: filter weights (default: the shipped Plant_SRP filter)")
+    ap.add_argument("--hits-per-mb", type=float, default=None, help="embedded hits per Mb (default: the workload's)")
+    ap.add_argument("--filter", default=None, help="learned workload: filter weights (default: the shipped filter)")
     ap.add_argument("--filter-recall", type=float, default=None,
                     help="learned workload: the filter's stored validation operating point to use "
-                         "(recall of windows holding an E <= 0.01 hit; default: the file's threshold, 0.99)")
+                         "(recall of windows holding an E <= 0.01 hit; default 0.99)")
     args = ap.parse_args()
     world = _env_int("WORLD_SIZE", 1)
     rank = _env_int("RANK", 0)
@@ -840,12 +809,10 @@ def main():
         torch.distributed.init_process_group("nccl")
     if args.workload == "trunc":
         out = run_trunc(args, rank, world)
-    elif args.workload == "learned":
-        out = run_learned(args, rank, world)
     elif args.workload == "multi":
         out = run_multi(args, rank, world)
     else:
-        out = run_ours(args, rank, world)
+        out = run_pipeline(args, rank, world)
     if rank == 0:
         print(json.dumps(out))
     if world > 1:

@@ -18,8 +18,8 @@ no batch normalisation); only the exported arrays are used at scan time.
 
 ``filtered_scan`` is the pipeline: filter all windows of both strands, keep
 those above the threshold, merge them into regions and run the plain
-CYK -> Inside scan on the regions only.  The plain scan on everything stays
-the measure of what the filter misses.
+CYK -> Inside scan on the regions only.  The plain scan on everything
+(``plain_scan``) stays the measure of what the filter misses.
 
     python -m infernal_gb300.prefilter train <model> <out.npz> [n_windows] [steps]
     python -m infernal_gb300.prefilter train-native <model> <out.npz> [n_windows] [steps]
@@ -334,6 +334,7 @@ class NativeTrainer:
 # scan-time use
 class Prefilter:
     """The network on one device context (cmgb_filter_*)."""
+    LAUNCHES = 7          # kernels per logits() call: layer 0, five convolutions, read-out
 
     def __init__(self, scanner: "lib.Scanner", weights: dict, W: int):
         self.sc, self.lib = scanner, scanner.lib
@@ -387,6 +388,104 @@ class Prefilter:
             else:
                 regs.append([a, b])
         return [(a, b) for a, b in regs]
+
+
+# ---------------------------------------------------------------------------
+# the two pipelines on both strands of one target
+def strand_buffer(dsq: np.ndarray) -> np.ndarray:
+    """Both strands of a target in one residue buffer: sentinel, top strand
+    (L residues), sentinel, reverse complement, sentinel (2L + 3 bytes).
+    Strand s's Easel dsq starts at byte s * (L + 1)."""
+    L = len(dsq) - 2
+    rev = emit.revcomp_dsq(dsq)
+    buf = np.empty(2 * L + 3, np.uint8)
+    buf[: L + 2] = dsq
+    buf[L + 1:] = rev
+    return buf
+
+
+def _ranges_scan(sc: "lib.Scanner", m, d_buf: int, nbuf: int, spans, algo: str, qdb: int, cut: float, stats: dict):
+    """One batched launch over sub-ranges of the two-strand buffer; spans are
+    (strand, a, b) in strand coordinates; returns per-span hit lists in
+    strand coordinates (start, stop, score)."""
+    if not spans:
+        return []
+    L = (nbuf - 3) // 2
+    offs = np.array([s * (L + 1) + a - 1 for s, a, b in spans], np.int64)
+    lens = np.array([b - a + 1 for s, a, b in spans], np.int64)
+    rs = sc.scan_batch(m, None, algo=algo, qdbidx=qdb, cutoff=cut, env_cutoff=cut, ranges=(None, offs, lens),
+                       device_buf=(d_buf, nbuf))
+    stats["kernel_ms"][algo] += rs[0].kernel_ms
+    stats["launches"] += sc.last_launches()
+    stats["calls"][algo] += 1
+    h2d, d2h = sc.last_transfer_bytes()
+    stats["h2d"] += h2d; stats["d2h"] += d2h
+    stats["lengths"][algo] += [int(x) for x in lens]
+    return [[(h[0] + a - 1, h[1] + a - 1, h[4]) for h in r.hits] for (s, a, b), r in zip(spans, rs)]
+
+
+def _new_stats():
+    return {"kernel_ms": {"filter": 0.0, "cyk": 0.0, "inside": 0.0}, "launches": 0, "h2d": 0, "d2h": 0,
+            "lengths": {"cyk": [], "inside": []}, "calls": {"cyk": 0, "inside": 0}, "kept": 0}
+
+
+def _final_stage(sc, m, d_buf, nbuf, cyk_hits, ins_cut, stats):
+    """Survivor windows of each strand's CYK hits (pipeline.cyk_windows) and
+    the Inside scan of all of them in one launch; hits per strand."""
+    from .pipeline import cyk_windows
+    L = (nbuf - 3) // 2
+    spans = [(s, a, b) for s in (0, 1) for a, b in cyk_windows(cyk_hits[s], m.W, L)]
+    out = [[], []]
+    for (s, a, b), hs in zip(spans, _ranges_scan(sc, m, d_buf, nbuf, spans, "inside", 2, ins_cut, stats)):
+        out[s] += hs
+    return out
+
+
+def filtered_scan(sc: "lib.Scanner", filt: "Prefilter", m, d_buf: int, nbuf: int, cyk_cut: float, ins_cut: float):
+    """The learned pipeline over both strands of a target in device memory
+    (strand_buffer layout, nbuf bytes at device address d_buf): the filter
+    scores every window of each strand, kept windows merge into regions, the
+    regions of both strands get the QDB1 CYK scan in one batched launch
+    (NULL3, greedy, cutoff cyk_cut), and the survivor windows of the CYK hits
+    (padded by W-1 and merged, as the reference pipeline) get the QDB2 Inside
+    scan in one more launch.  Returns (hits per strand as (start, stop,
+    score) in strand coordinates, statistics)."""
+    L = (nbuf - 3) // 2
+    st = _new_stats()
+    spans = []
+    for s in (0, 1):
+        logit, ms = filt.logits(d_buf + s * (L + 1), 1, L)
+        st["kernel_ms"]["filter"] += ms
+        st["launches"] += filt.LAUNCHES
+        st["d2h"] += 4 * len(logit)
+        spans += [(s, a, b) for a, b in filt.regions(logit, 1, L)]
+    st["kept"] = sum(b - a + 1 for _, a, b in spans)
+    cyk = [[], []]
+    for (s, a, b), hs in zip(spans, _ranges_scan(sc, m, d_buf, nbuf, spans, "cyk", 1, cyk_cut, st)):
+        cyk[s] += [(h[0], h[1]) for h in hs]
+    return _final_stage(sc, m, d_buf, nbuf, cyk, ins_cut, st), st
+
+
+def plain_scan(sc: "lib.Scanner", m, d_buf: int, nbuf: int, cyk_cut: float, ins_cut: float):
+    """The plain GPU pipeline on the same buffer: the single-launch QDB1 CYK
+    scan of each whole strand (cmgb_FastCYKScan_dev), then the survivor
+    windows of both strands in one batched Inside launch.  The judge of what
+    the filter loses.  Returns (hits per strand, statistics)."""
+    L = (nbuf - 3) // 2
+    st = _new_stats()
+    cyk = [[], []]
+    for s in (0, 1):
+        r = sc.scan(m, None, 1, L, algo="cyk", qdbidx=1, cutoff=cyk_cut, env_cutoff=cyk_cut,
+                    device_ptr=d_buf + s * (L + 1))
+        st["kernel_ms"]["cyk"] += r.kernel_ms
+        st["launches"] += sc.last_launches()
+        h2d, d2h = sc.last_transfer_bytes()
+        st["h2d"] += h2d; st["d2h"] += d2h
+        st["lengths"]["cyk"].append(L)
+        st["calls"]["cyk"] += 1
+        cyk[s] = [(h[0], h[1]) for h in r.hits]
+    st["kept"] = 2 * L
+    return _final_stage(sc, m, d_buf, nbuf, cyk, ins_cut, st), st
 
 
 def _windows_job(args):
