@@ -15,8 +15,10 @@
  * cmgb_model) instead of a CM_t, the rolling scan matrix lives on the GPU
  * (cmgb_ctx) instead of a CM_SCAN_MX, and hits are appended to a
  * cmgb_hitlist instead of a CM_TOPHITS.  An Infernal build binds the
- * reference names to these calls with a ~100 line adapter that reads the
- * CM_t fields listed below.
+ * reference names to these calls with the adapter in
+ * infernal_gb300/adapter/infernal_gb300_adapter.c, which defines
+ * FastCYKScan() & co. with the reference prototypes and copies the CM_t
+ * fields listed below.
  *
  * All pointers are plain host pointers, all sizes plain integers; nothing in
  * this header depends on CUDA, PyTorch or Easel headers.

@@ -42,9 +42,20 @@ def build_oracle(force: bool = False) -> str:
     return ORACLE_SO
 
 
-def build_ref(ref_root: str = "/root/reference") -> Optional[str]:
-    """Builds oracle/_ref from the reference tree when it exists here."""
-    if not os.path.isdir(os.path.join(ref_root, "src")):
+REF_ROOT_ENV = "INFERNAL_REF_ROOT"      # where the reference tree is, in a container that has it
+
+
+def reference_root() -> Optional[str]:
+    """The reference tree's location: the INFERNAL_REF_ROOT environment variable."""
+    return os.environ.get(REF_ROOT_ENV) or None
+
+
+def build_ref(ref_root: Optional[str] = None) -> Optional[str]:
+    """Builds oracle/_ref from the reference tree at ref_root (default: the
+    INFERNAL_REF_ROOT environment variable) when that tree exists; returns
+    the library path, or None without a tree."""
+    ref_root = ref_root or reference_root()
+    if not ref_root or not os.path.isdir(os.path.join(ref_root, "src")):
         return None
     subprocess.check_call([os.path.join(HERE, "build_ref.sh"), ref_root], stdout=subprocess.DEVNULL)
     return REF_SO

@@ -335,12 +335,35 @@ enum { REFH_FASTCYK = 0, REFH_REFCYK = 1, REFH_FASTIINS = 2, REFH_REFIINS = 3,
  * hits_out receives at most max_hits hits in hit-list order; *ret_nhits is
  * the full count.  vsc_out (M floats) may be NULL.  Returns the scanner's
  * status code; errbuf receives its message. */
+int refh_scan_full(const cmgb_model_desc *m, int nodes, int algo, int qdbidx,
+                   const uint8_t *dsq, int64_t i0, int64_t j0, float cutoff,
+                   int do_null3, float env_cutoff, int pass_idx, int want_hits,
+                   cmgb_hit *hits_out, int64_t max_hits, int64_t *ret_nhits,
+                   int64_t *ret_envi, int64_t *ret_envj, float *vsc_out, float *ret_sc,
+                   int *ret_mode, int64_t *extra_out, char *errbuf);
+
 int refh_scan(const cmgb_model_desc *m, int nodes, int algo, int qdbidx,
               const uint8_t *dsq, int64_t i0, int64_t j0, float cutoff,
               int do_null3, float env_cutoff, int pass_idx, int want_hits,
               cmgb_hit *hits_out, int64_t max_hits, int64_t *ret_nhits,
               int64_t *ret_envi, int64_t *ret_envj, float *vsc_out, float *ret_sc,
               int *ret_mode, char *errbuf)
+{
+  return refh_scan_full(m, nodes, algo, qdbidx, dsq, i0, j0, cutoff, do_null3, env_cutoff, pass_idx, want_hits,
+                        hits_out, max_hits, ret_nhits, ret_envi, ret_envj, vsc_out, ret_sc, ret_mode, NULL, errbuf);
+}
+
+/* As refh_scan; extra_out (when not NULL) receives, per hit, the other
+ * CM_HIT fields a scanner call leaves behind, as REFH_NEXTRA integers:
+ * srcL, flags, hit_idx, hmmonly, cm_idx, seq_idx, pass_idx, in_rc, glocal,
+ * has_evalue, and the bit patterns of pvalue and evalue (doubles). */
+#define REFH_NEXTRA 12
+int refh_scan_full(const cmgb_model_desc *m, int nodes, int algo, int qdbidx,
+                   const uint8_t *dsq, int64_t i0, int64_t j0, float cutoff,
+                   int do_null3, float env_cutoff, int pass_idx, int want_hits,
+                   cmgb_hit *hits_out, int64_t max_hits, int64_t *ret_nhits,
+                   int64_t *ret_envi, int64_t *ret_envj, float *vsc_out, float *ret_sc,
+                   int *ret_mode, int64_t *extra_out, char *errbuf)
 {
   static int tables_ready = 0;
   if (!tables_ready) { init_ilogsum(); FLogsumInit(); tables_ready = 1; }
@@ -379,6 +402,13 @@ int refh_scan(const cmgb_model_desc *m, int nodes, int algo, int qdbidx,
         hits_out[h].start = th->unsrt[h].start; hits_out[h].stop = th->unsrt[h].stop;
         hits_out[h].root  = th->unsrt[h].root;  hits_out[h].mode = th->unsrt[h].mode;
         hits_out[h].score = th->unsrt[h].score;
+        if (extra_out) {
+          const CM_HIT *x = &th->unsrt[h];
+          int64_t *e = extra_out + h * REFH_NEXTRA;
+          e[0] = x->srcL; e[1] = x->flags; e[2] = x->hit_idx; e[3] = x->hmmonly; e[4] = x->cm_idx; e[5] = x->seq_idx;
+          e[6] = x->pass_idx; e[7] = x->in_rc; e[8] = x->glocal; e[9] = x->has_evalue;
+          memcpy(&e[10], &x->pvalue, sizeof(double)); memcpy(&e[11], &x->evalue, sizeof(double));
+        }
       }
     } else *ret_nhits = 0;
     if (vsc_out && vsc) memcpy(vsc_out, vsc, sizeof(float) * m->M);

@@ -1,6 +1,7 @@
 """Generates the golden vectors of the scan parity tests.
 
-Run in a container where the reference tree exists (default /root/reference):
+Run in a container where the reference tree exists (its location in the
+INFERNAL_REF_ROOT environment variable, or as the first argument):
 
     python tests/golden/gen_golden.py [reference_root]
 
@@ -116,7 +117,10 @@ RUNS = [  # (algo, qdbidx, cutoff, null3, env_cutoff, notgreedy, which cases)
 ]
 
 
-def main(ref_root="/root/reference"):
+def main(ref_root=None):
+    ref_root = ref_root or oracle.reference_root()
+    if not ref_root:
+        raise SystemExit("set INFERNAL_REF_ROOT (or pass the reference tree's location)")
     so = oracle.build_ref(ref_root)
     if so is None:
         raise SystemExit(f"reference tree not found under {ref_root}")

@@ -1,6 +1,7 @@
 """Stores the targets of the reference's known-answer sensitivity test.
 
-Run in a container where the reference tree exists (default /root/reference):
+Run in a container where the reference tree exists (its location in the
+INFERNAL_REF_ROOT environment variable, or as the first argument):
 
     python tests/golden/gen_known_answers.py [reference_root]
 
@@ -43,7 +44,10 @@ TR_FILE = "tremitted-Vault.fa"
 TR_HITS = [("Vault-1", 1, 63, 33.2), ("Vault-2", 1, 59, 25.5)]
 
 
-def main(ref_root="/root/reference"):
+def main(ref_root=None):
+    ref_root = ref_root or os.environ.get("INFERNAL_REF_ROOT")
+    if not ref_root:
+        raise SystemExit("set INFERNAL_REF_ROOT (or pass the reference tree's location)")
     arrays, meta = {}, []
     for model, fa, fbeta, beta, (a, b), line in CASES:
         seq = cmfile.read_fasta(os.path.join(ref_root, "testsuite", fa))[0][1].upper().replace("T", "U")

@@ -1,6 +1,7 @@
 """Writes the model panel of the multi-model batched workload.
 
-Run in a container where the reference tree exists (default /root/reference):
+Run in a container where the reference tree exists (its location in the
+INFERNAL_REF_ROOT environment variable, or as the first argument):
 
     python tests/golden/gen_panel.py [reference_root]
 
@@ -28,7 +29,10 @@ PANEL = {"tRNA1415G": "testsuite", "snR75": "testsuite", "tRNA-Sec": "testsuite"
          "tRNA5-hand": "tutorial"}
 
 
-def main(ref_root="/root/reference"):
+def main(ref_root=None):
+    ref_root = ref_root or os.environ.get("INFERNAL_REF_ROOT")
+    if not ref_root:
+        raise SystemExit("set INFERNAL_REF_ROOT (or pass the reference tree's location)")
     os.makedirs(os.path.join(HERE, "panel"), exist_ok=True)
     for name, sub in PANEL.items():
         m = cmfile.load(os.path.join(ref_root, sub, f"{name}.c.cm"))

@@ -1,6 +1,7 @@
 """Generates golden vectors for the model panel (tests/golden/panel).
 
-Run in a container where the reference tree exists (default /root/reference):
+Run in a container where the reference tree exists (its location in the
+INFERNAL_REF_ROOT environment variable, or as the first argument):
 
     python tests/golden/gen_panel_golden.py [reference_root]
 
@@ -29,7 +30,10 @@ import oracle  # noqa: E402
 PANEL = ["tRNA1415G", "snR75", "tRNA-Sec", "srp-euk", "rnaseP-eubact", "5S_rRNA", "Cobalamin", "tRNA5", "tRNA5-hand"]
 
 
-def main(ref_root="/root/reference"):
+def main(ref_root=None):
+    ref_root = ref_root or oracle.reference_root()
+    if not ref_root:
+        raise SystemExit("set INFERNAL_REF_ROOT (or pass the reference tree's location)")
     if oracle.build_ref(ref_root) is None:
         raise SystemExit(f"reference tree not found under {ref_root}")
     rng = np.random.default_rng(20261207)
