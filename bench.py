@@ -254,7 +254,7 @@ def pipeline_config(sp, m, world):
          f"{sp['hits_per_mb']} emitted hits per Mb embedded on random strands; ")
     if sp["filter"]:
         w += (f"learned BF16 window pre-filter at its validation operating point of recall {sp['recall']} "
-              f"(windows holding an E <= 0.01 hit); kept regions of both strands -> ")
+              f"(windows holding a hit with E <= 0.01 at this search's size); kept regions of both strands -> ")
     w += f"QDB1 CYK ({CYK_CUT} bits, NULL3, greedy) -> survivor windows -> QDB2 integer Inside ({INS_CUT} bits)"
     return {"workload": w, "residues_per_step": int(2 * round(sp["mb"] * 1e6)),
             "l2": "flushed between timed steps (256 MB write)",
@@ -295,11 +295,14 @@ def run_pipeline(args, rank, world):
     torch.cuda.set_device(dev)
     sc = L.Scanner(dev)
     filt = None
+    # E <= 0.01 at this search's size (every residue of the timed steps, both
+    # strands) by the model's Inside calibration: the hits the filter must keep
+    e_bits = float(L.bits_at_evalue(m.ecm["ECMLI"], 0.01, 2.0 * round(sp["mb"] * 1e6) * args.steps))
     if sp["filter"]:
         wts = prefilter.load(args.filter or os.path.join(ROOT, "infernal_gb300", "filters", f"{m.name}.filter.npz"))
         filt = prefilter.Prefilter(sc, wts, m.W)
         if filt.points is not None:
-            filt.use_recall(sp["recall"])
+            filt.use_recall(sp["recall"], bits=e_bits)
     nsteps = args.warmup + args.steps
     inputs = [prefilter.strand_buffer(make_step_input(m, rank_step_seed(rank, sp["seed"] + s), sp["mb"],
                                                       hits_per_mb=sp["hits_per_mb"], gc=sp["gc"])[0])
@@ -417,7 +420,6 @@ def run_pipeline(args, rank, world):
             barrier()
             t_plain += time.perf_counter() - t0
             phits.append(h); pk += st["kernel_ms"]["cyk"] + st["kernel_ms"]["inside"]
-        e_bits = float(L.bits_at_evalue(m.ecm["ECMLI"], 0.01, float(res)))
         nplain = nfound = ne = nef = 0
         for ph, fh in zip(phits, hits):
             for sp_, sf in zip(ph, fh):
@@ -445,6 +447,176 @@ def run_pipeline(args, rank, world):
 
 def _overlap(a, b):
     return max(0, min(a[1], b[1]) - max(a[0], b[0]) + 1)
+
+
+MULTI_SPEC = {"models": ["Vault", "tRNA", "5S_rRNA", "Plant_SRP"], "gc": (0.35, 0.60), "mb": 2.0, "hits_per_mb": 30.0,
+              "seed": 800000}
+
+
+def multi_config(sp, models, world, recall):
+    names = ", ".join(f"{m.name} (clen {m.clen}, W {m.W})" for m in models)
+    return {"workload": f"{len(models)} CMs [{names}] against {sp['mb']} Mb x 2 strands per step, GC varying "
+                        f"{sp['gc'][0]}-{sp['gc'][1]} per 50 kb segment, {sp['hits_per_mb']} emitted hits per Mb (the "
+                        f"models in turn) on random strands; one BF16 filter trunk with a read-out per CM at its validation "
+                        f"operating point of recall {recall}; every model's kept regions of both strands -> QDB1 CYK "
+                        f"({CYK_CUT} bits) in one multi-model launch -> survivor windows -> QDB2 Inside ({INS_CUT} bits) in one "
+                        f"multi-model launch",
+            "residues_per_step": int(2 * round(sp["mb"] * 1e6)), "l2": "flushed between timed steps (256 MB write)",
+            "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"}
+
+
+def make_step_input_multi(models, step, mb, seed, hits_per_mb, gc):
+    """One step's target with hits emitted by the models in turn."""
+    from infernal_gb300 import emit
+    rng = np.random.default_rng([seed, step])
+    L = int(mb * 1_000_000)
+    nhits = max(len(models), int(round(hits_per_mb * mb)))
+    ins = [emit.sample(models[k % len(models)], rng) for k in range(nhits)]
+    dsq, spans = emit.make_target(rng, L, gc, ins)
+    return dsq
+
+
+def run_pipeline_multi(args, rank, world):
+    """learned-multi: several CMs, one filter trunk with a head per CM, against
+    the plain multi-model scan of the same targets."""
+    import torch
+    from infernal_gb300 import lib as L, prefilter
+    sp = dict(MULTI_SPEC)
+    if args.mb is not None:
+        sp["mb"] = args.mb
+    if args.hits_per_mb is not None:
+        sp["hits_per_mb"] = args.hits_per_mb
+    recall = args.filter_recall if args.filter_recall is not None else 0.99
+    models = [load_model(n) for n in sp["models"]]
+    K = len(models)
+    dev = 0 if world == 1 else _env_int("LOCAL_RANK", 0)
+    torch.cuda.set_device(dev)
+    sc = L.Scanner(dev)
+    wts = prefilter.load(args.filter or os.path.join(ROOT, "infernal_gb300", "filters", "multi4.filter.npz"))
+    Wf = int(wts["W"])
+    filt = prefilter.Prefilter(sc, wts, Wf)
+    Z = 2.0 * round(sp["mb"] * 1e6) * args.steps
+    e_bits = [float(L.bits_at_evalue(m.ecm["ECMLI"], 0.01, Z)) for m in models]
+    pts = wts["recall_points"]                         # [K][rows][5]
+    thr = []
+    for k in range(K):
+        p = pts[k]
+        levels = np.unique(p[:, 0])
+        lv = levels[levels <= e_bits[k]].max() if (levels <= e_bits[k]).any() else levels.min()
+        row = p[(p[:, 0] == lv) & (np.abs(p[:, 1] - recall) < 1e-9)]
+        thr.append(float(row[0, 2]))
+    filt.thr = np.array(thr)
+    nsteps = args.warmup + args.steps
+    inputs = [prefilter.strand_buffer(make_step_input_multi(models, rank_step_seed(rank, sp["seed"] + s), sp["mb"], sp["seed"],
+                                                            sp["hits_per_mb"], sp["gc"])) for s in range(nsteps)]
+    nbuf = len(inputs[0])
+    Lres = (nbuf - 3) // 2
+    host = [torch.from_numpy(x).pin_memory() for x in inputs]
+    devb = [h.to("cuda") for h in host]
+    dstage = torch.empty(nbuf, dtype=torch.uint8, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for m in models:
+        sc.autotune(m, 1, "cyk"); sc.autotune(m, 2, "inside")
+    work = {(k, a): Work(m, 1 if a == "cyk" else 2) for k, m in enumerate(models) for a in ("cyk", "inside")}
+    run = lambda ptr: prefilter.filtered_scan_multi(sc, filt, models, ptr, nbuf)
+    run_plain = lambda ptr: prefilter.plain_scan_multi(sc, models, ptr, nbuf)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for s in range(args.warmup):
+        run(devb[s].data_ptr())
+    clk = start_clock_sampler(rank)
+    tot, hits, sts = 0.0, [], []
+    for s in range(args.warmup, nsteps):
+        flush.fill_(float(s)); barrier()
+        t0 = time.perf_counter()
+        h, st = run(devb[s].data_ptr())
+        barrier()
+        tot += time.perf_counter() - t0
+        hits.append(h); sts.append(st)
+    clocks = stop_clock_sampler(clk)
+    t_e2e, h2d, d2h = 0.0, 0, 0
+    for s in range(args.warmup, nsteps):
+        flush.fill_(float(s)); barrier()
+        t0 = time.perf_counter()
+        dstage.copy_(host[s], non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        h, st = run(dstage.data_ptr())
+        barrier()
+        t_e2e += time.perf_counter() - t0
+        h2d += nbuf + st["h2d"]; d2h += st["d2h"]
+    run_plain(devb[0].data_ptr())
+    t_plain, phits, pk = 0.0, [], 0.0
+    for s in range(args.warmup, nsteps):
+        flush.fill_(float(s)); barrier()
+        t0 = time.perf_counter()
+        h, st = run_plain(devb[s].data_ptr())
+        barrier()
+        t_plain += time.perf_counter() - t0
+        phits.append(h); pk += st["kernel_ms"]["cyk"] + st["kernel_ms"]["inside"]
+    t_dev, t_e2e, t_plain = max_over_ranks([tot, t_e2e, t_plain], world)
+    res = 2 * Lres * args.steps
+    kms = {a: sum(st["kernel_ms"][a] for st in sts) for a in ("filter", "cyk", "inside")}
+    cells = sum(work[(k, a)].cells(n) for st in sts for a in ("cyk", "inside") for k, n in st["lengths"][a])
+    ops = {a: sum(work[(k, a)].ops(n) for st in sts for k, n in st["lengths"][a]) for a in ("cyk", "inside")}
+    per = {}
+    for k, m in enumerate(models):
+        ne = nef = 0
+        for ph, fh in zip(phits, hits):
+            for s_ in (0, 1):
+                for hh in ph[k][s_]:
+                    if hh[2] >= e_bits[k]:
+                        ne += 1
+                        nef += any(_overlap(hh, g) >= 0.5 * (hh[1] - hh[0] + 1) for g in fh[k][s_])
+        per[m.name] = {"e001_bits": round(e_bits[k], 2), "hits_plain": ne, "hits_found": nef, "threshold": round(thr[k], 4)}
+    ne = sum(v["hits_plain"] for v in per.values()); nef = sum(v["hits_found"] for v in per.values())
+    peaks, pkind = measured_peaks()
+    f32, i32 = sc.issue_peak("f32") / 1e12, sc.issue_peak("i32") / 1e12
+    blocks = {}
+    if kms["cyk"] > 0:
+        blocks["cyk"] = kernel_block("qdb_scan_kernel<CYK, multi-model>", "fp32 add+max issue", ops["cyk"] / (kms["cyk"] / 1e3) / 1e12,
+                                     f32, "Tops/s", "algorithmic DP operations of every model's CYK cells scanned, per kernel "
+                                     "second; peak: cmgb_measure_issue_peak fp32 on this device")
+    if kms["inside"] > 0:
+        blocks["inside"] = kernel_block("qdb_scan_kernel<IInside, multi-model>", "int32 add+max issue",
+                                        ops["inside"] / (kms["inside"] / 1e3) / 1e12, i32, "Tops/s",
+                                        "algorithmic operations per kernel second; peak: cmgb_measure_issue_peak int32")
+    if kms["filter"] > 0:
+        nwin = 2 * (-(-Lres // Wf)) * args.steps
+        flops = 2.0 * nwin * (2 * Wf) * 9 * 128 * 128 * 5
+        blocks["filter"] = kernel_block("filter_conv_tc (tcgen05)", "tensor", flops / (kms["filter"] / 1e3) / 1e12,
+                                        float(peaks.get("bf16_tflops", 1900.0)), "TFLOP/s",
+                                        f"dilated layers' GEMM FLOPs over the 2W positions of every window; peak: {pkind} bf16 burst")
+    out = {
+        "metric": ("Mres/s scanned (both strands) on 1 GB300: learned pre-filter (one trunk, a head per CM) + batched "
+                   "multi-model QDB-CYK -> Inside, against the plain multi-model GPU scan at <= 1% loss of E <= 0.01 hits"),
+        "value": round(res * world / t_dev / 1e6, 3), "unit": "Mres/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1000 * t_dev / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (filter) + f32 (CYK) + int32 (Inside)", "data": "synthetic",
+        "config": multi_config(sp, models, world, recall),
+        "gcups": round(cells * world / t_dev / 1e9, 2),
+        "e2e": {"value": round(res * world / t_e2e / 1e6, 3), "unit": "Mres/s",
+                "h2d_bytes_per_step": int(h2d / args.steps), "d2h_bytes_per_step": int(d2h / args.steps)},
+        "kernel_ms_per_step": {k: round(v / args.steps, 3) for k, v in kms.items()},
+        "fraction_scanned": round(sum(st["kept"] for st in sts) / (res * K), 4),
+        "gpu_launches": sum(st["launches"] for st in sts),
+        "plain_mres_s": round(res / t_plain / 1e6, 3), "speedup_vs_plain": round(t_plain / tot, 3),
+        "plain_kernel_ms_per_step": round(pk / args.steps, 3),
+        "e001_hits_plain": ne, "e001_hits_found": nef, "e001_hit_loss": round(1.0 - nef / ne, 4) if ne else None,
+        "per_model": per, "clocks": clocks,
+    }
+    if blocks:
+        dom = max(blocks, key=lambda k: kms[k])
+        r = dict(blocks[dom]); r["kernels"] = blocks
+        r["dominant_share_of_kernel_time"] = round(kms[dom] / max(1e-9, sum(kms.values())), 3)
+        r["peaks_measured"] = {"fp32_add_max_tops": round(f32, 2), "int32_add_max_tops": round(i32, 2),
+                               "sm_count": torch.cuda.get_device_properties(dev).multi_processor_count}
+        out["roofline"] = r
+    filt.close(); sc.close()
+    return out
 
 
 PANEL = ["tRNA", "Vault", "Plant_SRP", "tRNA1415G", "snR75", "tRNA-Sec", "srp-euk", "rnaseP-eubact",
@@ -667,6 +839,20 @@ def cpu_baseline(m, dsq, seconds=10.0):
                       f"on its {nw} survivor windows, one core"}
 
 
+def _ref_worker_multi(argv):
+    names, mb, hits_per_mb, gc, seed, nres, use_ref = argv
+    models = [load_model(n) for n in names]
+    nh = int(np.random.default_rng([seed, 1]).poisson(hits_per_mb * nres / 1e6))
+    from infernal_gb300 import emit
+    rng = np.random.default_rng([seed, 2])
+    ins = [emit.sample(models[k % len(models)], rng) for k in range(nh)]
+    dsq, _ = emit.make_target(rng, nres + 1000, gc, ins)
+    t0 = time.perf_counter()
+    for m in models:
+        cpu_pipeline(m, dsq, nres, use_ref)
+    return nres, time.perf_counter() - t0
+
+
 def _ref_worker(argv):
     workload, mb, hits_per_mb, gc, seed, nres, use_ref = argv
     sp = SPECS[workload]
@@ -684,11 +870,13 @@ def run_reference(args, rank, world):
     process per core, each step a bounded sample of the workload."""
     import multiprocessing as mp
     import oracle
-    if args.workload not in SPECS:
+    if args.workload not in SPECS and args.workload != "learned-multi":
         return {"impl": "reference", "unavailable": f"the {args.workload} workload has no CPU reference arm here"}
     oracle.build_oracle()
     use_ref = os.path.exists(oracle.REF_SO)
     ncpu = len(os.sched_getaffinity(0))
+    if args.workload == "learned-multi":
+        return run_reference_multi(args, world, use_ref, ncpu)
     sp = spec_of(args)
     m = load_model(sp["model"])
     # size the per-process sample from a short single-process probe
@@ -721,6 +909,47 @@ def run_reference(args, rank, world):
                          "sample": f"per step {ncpu} processes, each: CYK QDB1 over {nres} residues of a fresh target of "
                                    f"this workload's distribution, then Inside QDB2 on its survivor windows "
                                    f"(the reference has no learned filter: its pipeline scans everything)"},
+        "e2e": {"value": round(v, 6), "unit": "Mres/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def run_reference_multi(args, world, use_ref, ncpu):
+    """CPU reference arm of learned-multi: every model's CYK -> Inside pipeline
+    over the same bounded sample, one process per core (no filter: the
+    reference scans everything with every model)."""
+    import multiprocessing as mp
+    sp = dict(MULTI_SPEC)
+    if args.mb is not None:
+        sp["mb"] = args.mb
+    if args.hits_per_mb is not None:
+        sp["hits_per_mb"] = args.hits_per_mb
+    recall = args.filter_recall if args.filter_recall is not None else 0.99
+    models = [load_model(n) for n in sp["models"]]
+    t0 = time.perf_counter()
+    _ref_worker_multi((sp["models"], sp["mb"], 0.0, sp["gc"], 998, 1000, use_ref))
+    rate = 1000 / (time.perf_counter() - t0)
+    nres = int(max(1000, min(100000, rate * max(2.0, args.ref_step_seconds))))
+    times = []
+    with mp.get_context("spawn").Pool(ncpu) as pool:
+        for s in range(args.warmup + args.steps):
+            jobs = [(sp["models"], sp["mb"], sp["hits_per_mb"], sp["gc"], 950000 + s * ncpu + k, nres, use_ref) for k in range(ncpu)]
+            t0 = time.perf_counter()
+            res = pool.map(_ref_worker_multi, jobs)
+            dt = time.perf_counter() - t0
+            if s >= args.warmup:
+                times.append((sum(r[0] for r in res), dt))
+    v = sum(t[0] for t in times) / sum(t[1] for t in times) / 1e6
+    return {
+        "impl": "reference", "metric": ("Mres/s scanned (both strands) on 1 GB300: learned pre-filter (one trunk, a head per "
+                                        "CM) + batched multi-model QDB-CYK -> Inside, against the plain multi-model GPU scan "
+                                        "at <= 1% loss of E <= 0.01 hits"),
+        "value": round(v, 6), "unit": "Mres/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1000 * sum(t[1] for t in times) / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (CYK) + int32 (Inside)", "data": "synthetic",
+        "config": multi_config(sp, models, 1, recall),
+        "cpu_baseline": {"value": round(v, 6), "unit": "Mres/s", "cores": ncpu, "kind": "reference" if use_ref else "port",
+                         "sample": f"per step {ncpu} processes, each: every model's CYK QDB1 over {nres} residues of a fresh "
+                                   f"target of this workload's distribution, then Inside QDB2 on its survivor windows"},
         "e2e": {"value": round(v, 6), "unit": "Mres/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -784,7 +1013,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="learned", choices=["learned", "plain", "cfg1", "trunc", "multi"],
+    ap.add_argument("--workload", default="learned", choices=["learned", "learned-multi", "plain", "cfg1", "trunc", "multi"],
                     help="learned: the pre-filtered pipeline against the plain scan (default); plain: the "
                          "single-large-CM plain scan; cfg1: the clen-100 plain scan; trunc: the truncated-mode read "
                          "batch; multi: the uneven multi-model batch")
@@ -811,6 +1040,8 @@ def main():
         out = run_trunc(args, rank, world)
     elif args.workload == "multi":
         out = run_multi(args, rank, world)
+    elif args.workload == "learned-multi":
+        out = run_pipeline_multi(args, rank, world)
     else:
         out = run_pipeline(args, rank, world)
     if rank == 0:

@@ -181,8 +181,8 @@ void cmgb_model_destroy(cmgb_model *model);
 
 /* Autotuner: times candidate shapes (tile rows = rolling-row depth, and
  * shared- vs global-memory tiles) for band set qdbidx and algo (0 CYK,
- * 1 integer Inside, 2 float Inside) on a seeded iid sample of sample_len residues (0: a size
- * that fills the device) and stores the fastest in the model; scans on a
+ * 1 integer Inside, 2 float Inside) on a seeded iid sample of sample_len residues (0: enough
+ * windows of 8 W residues for two per resident CTA) and stores the fastest in the model; scans on a
  * context whose tile_rows is 0 use it.  Returns the choice when the
  * pointers are non-NULL. */
 int  cmgb_autotune(cmgb_ctx *ctx, cmgb_model *model, int qdbidx, int algo, int64_t sample_len,
@@ -314,7 +314,8 @@ int cmgb_ScanBatch_dev(cmgb_ctx *ctx, cmgb_model *model, char *errbuf, int algo,
  * pli_dispatch_cm_search per model and window).  Job k scans sequence
  * job_seq[k] (laid out as in cmgb_ScanBatch) with models[job_model[k]] and
  * that model's cutoff cutoffs[job_model[k]]; (model, sequence) pairs must be
- * distinct.  Long sequences are cut into windows as in cmgb_ScanBatch, and
+ * distinct, and the sequences of one model must not overlap in the buffer
+ * (those of different models may).  Long sequences are cut into windows as in cmgb_ScanBatch, and
  * every window of every job enters one work queue, largest band area
  * (model cells per residue x window rows) first.  algo is one of the
  * standard scanners (CMGB_ALGO_CYK, _IINSIDE, _FINSIDE).  Each job's results
@@ -328,6 +329,14 @@ int cmgb_ScanMulti(cmgb_ctx *ctx, cmgb_model *const *models, int nmodels, const 
                    const int64_t *lengths, int nseq, const int *job_model, const int *job_seq, int njobs,
                    cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
                    int64_t *ret_nhits, int64_t *ret_envi, int64_t *ret_envj, float *ret_sc);
+/* The same with the residue buffer already in device memory (d_seqs, a
+ * device address); sequences whose candidate hits need NULL3 compositions are
+ * read back individually. */
+int cmgb_ScanMulti_dev(cmgb_ctx *ctx, cmgb_model *const *models, int nmodels, const float *cutoffs, char *errbuf,
+                       int algo, int qdbidx, const uint8_t *d_seqs, int64_t seqs_len, const int64_t *offsets,
+                       const int64_t *lengths, int nseq, const int *job_model, const int *job_seq, int njobs,
+                       cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
+                       int64_t *ret_nhits, int64_t *ret_envi, int64_t *ret_envj, float *ret_sc);
 
 /* ---- E-value calibration ----
  * cmcalibrate's exponential tail fit for one search mode of a configured
@@ -373,6 +382,14 @@ int  cmgb_filter_create(cmgb_ctx *ctx, int W, const float *w0, const uint16_t *w
 void cmgb_filter_destroy(cmgb_filter *filter);
 int  cmgb_filter_windows(cmgb_ctx *ctx, cmgb_filter *filter, const uint8_t *d_dsq, int64_t i0, int64_t j0,
                          float *ret_logits, int64_t max_windows, int64_t *ret_nwin, float *ret_ms, char *errbuf);
+/* One network for several CMs: the convolutions are shared, every CM has its
+ * own read-out (head).  wout holds nheads rows of 128 weights + bias;
+ * cmgb_filter_windows then writes nheads logits per window (window-major:
+ * ret_logits[win * nheads + h], room for max_windows * nheads floats).
+ * cmgb_filter_create is the one-head case. */
+#define CMGB_FILTER_MAX_HEADS 64
+int  cmgb_filter_create_heads(cmgb_ctx *ctx, int W, int nheads, const float *w0, const uint16_t *w, const float *bias,
+                              const float *wout, cmgb_filter **ret_filter, char *errbuf);
 
 /* Training of the same network without batch normalisation (convolution,
  * bias, ReLU; the result loads into cmgb_filter_create as is), all on the
@@ -394,6 +411,15 @@ int  cmgb_filter_trainer_step(cmgb_filter_trainer *trainer, const uint8_t *windo
                               float lr, float weight_decay, float *ret_loss, float *ret_ms, char *errbuf);
 int  cmgb_filter_trainer_get(cmgb_filter_trainer *trainer, float *w0, float *w, float *bias, float *wout,
                              float *gw0, float *gw, float *gb, float *gwout, char *errbuf);
+/* The several-head trainer: labels are [batch][nheads] (window-major), one
+ * positive-class weight per head, the loss sums the heads' terms (each
+ * averaged over the batch as above); wout / gwout hold nheads rows of 129.
+ * cmgb_filter_trainer_create / _step are the one-head case. */
+int  cmgb_filter_trainer_create_heads(cmgb_ctx *ctx, int W, int batch, int nheads, uint64_t seed,
+                                      cmgb_filter_trainer **ret, char *errbuf);
+int  cmgb_filter_trainer_step_heads(cmgb_filter_trainer *trainer, const uint8_t *windows, const float *labels,
+                                    const float *pos_weights, float lr, float weight_decay, float *ret_loss, float *ret_ms,
+                                    char *errbuf);
 
 /* ---- allocation-free CYK scan ----
  * This entry point has no counterpart in the reference.  It is for callers

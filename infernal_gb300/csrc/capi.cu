@@ -35,9 +35,9 @@ template <int ALG, bool GL, bool MULTI = false>
 static void launch_qdb(int grid, int nt, size_t smem, cudaStream_t, const KParams &kp)
 {
   std::vector<std::vector<float>> sm(grid, std::vector<float>(smem / 4 + 16));
-  std::vector<std::barrier<> *> bars;
+  std::vector<EmuBarrier *> bars;
   std::vector<EmuWarp *> warps;
-  for (int b = 0; b < grid; b++) bars.push_back(new std::barrier<>(nt));
+  for (int b = 0; b < grid; b++) bars.push_back(new EmuBarrier(nt));
   for (int b = 0; b < grid * (nt / 32); b++) warps.push_back(new EmuWarp);
   std::vector<std::thread> th;
   for (int b = 0; b < grid; b++)
@@ -54,9 +54,9 @@ template <int ALG, bool GL>
 static void launch_tr(int grid, int nt, size_t smem, cudaStream_t, const TrKParams &kp)
 {
   std::vector<std::vector<float>> sm(grid, std::vector<float>(smem / 4 + 16));
-  std::vector<std::barrier<> *> bars;
+  std::vector<EmuBarrier *> bars;
   std::vector<EmuWarp *> warps;
-  for (int b = 0; b < grid; b++) bars.push_back(new std::barrier<>(nt));
+  for (int b = 0; b < grid; b++) bars.push_back(new EmuBarrier(nt));
   for (int b = 0; b < grid * (nt / 32); b++) warps.push_back(new EmuWarp);
   std::vector<std::thread> th;
   for (int b = 0; b < grid; b++)
@@ -1234,17 +1234,48 @@ static int scan_batch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo, int qd
 // ---------------------------------------------------------------------------
 // Multi-model batched scans: the windows of every (model, sequence) job in
 // one work queue, one persistent launch per tile placement.
+// seqs: host residues (copied per launch) or, when d_seqs is given,
+// residues already in device memory (sequences whose candidates need NULL3
+// compositions are read back individually).
+static int scan_multi(cmgb_ctx *c, cmgb_model *const *models, int nmodels, const float *cutoffs, char *errbuf,
+                      int algo, int qdbidx, const uint8_t *seqs, const uint8_t *d_seqs, int64_t seqs_len, const int64_t *offsets,
+                      const int64_t *lengths, int nseq, const int *job_model, const int *job_seq, int njobs,
+                      cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
+                      int64_t *ret_nhits, int64_t *ret_envi, int64_t *ret_envj, float *ret_sc);
+
 extern "C" int cmgb_ScanMulti(cmgb_ctx *c, cmgb_model *const *models, int nmodels, const float *cutoffs, char *errbuf,
                               int algo, int qdbidx, const uint8_t *seqs, int64_t seqs_len, const int64_t *offsets,
                               const int64_t *lengths, int nseq, const int *job_model, const int *job_seq, int njobs,
                               cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
                               int64_t *ret_nhits, int64_t *ret_envi, int64_t *ret_envj, float *ret_sc)
 {
+  if (!seqs) ERRF(CMGB_EINCOMPAT, "ScanMulti, no jobs");
+  return scan_multi(c, models, nmodels, cutoffs, errbuf, algo, qdbidx, seqs, nullptr, seqs_len, offsets, lengths, nseq,
+                    job_model, job_seq, njobs, hitlist, do_null3, env_cutoff, ret_nhits, ret_envi, ret_envj, ret_sc);
+}
+
+extern "C" int cmgb_ScanMulti_dev(cmgb_ctx *c, cmgb_model *const *models, int nmodels, const float *cutoffs, char *errbuf,
+                                  int algo, int qdbidx, const uint8_t *d_seqs, int64_t seqs_len, const int64_t *offsets,
+                                  const int64_t *lengths, int nseq, const int *job_model, const int *job_seq, int njobs,
+                                  cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
+                                  int64_t *ret_nhits, int64_t *ret_envi, int64_t *ret_envj, float *ret_sc)
+{
+  if (!d_seqs) ERRF(CMGB_EINCOMPAT, "ScanMulti, no jobs");
+  return scan_multi(c, models, nmodels, cutoffs, errbuf, algo, qdbidx, nullptr, d_seqs, seqs_len, offsets, lengths, nseq,
+                    job_model, job_seq, njobs, hitlist, do_null3, env_cutoff, ret_nhits, ret_envi, ret_envj, ret_sc);
+}
+
+static int scan_multi(cmgb_ctx *c, cmgb_model *const *models, int nmodels, const float *cutoffs, char *errbuf,
+                      int algo, int qdbidx, const uint8_t *seqs, const uint8_t *d_seqs, int64_t seqs_len, const int64_t *offsets,
+                      const int64_t *lengths, int nseq, const int *job_model, const int *job_seq, int njobs,
+                      cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
+                      int64_t *ret_nhits, int64_t *ret_envi, int64_t *ret_envj, float *ret_sc)
+{
   static const char *fn = "ScanMulti";
   if (!c || !models || nmodels < 1 || !cutoffs) ERRF(CMGB_EINVAL, "%s, NULL context, models or cutoffs", fn);
   if (algo < CMGB_ALGO_CYK || algo > CMGB_ALGO_FINSIDE) ERRF(CMGB_EINVAL, "%s, algorithm %d is not a standard scanner", fn, algo);
   if (qdbidx < 0 || qdbidx > 2) ERRF(CMGB_EINCOMPAT, "%s, qdbidx is invalid", fn);
-  if (!seqs || !offsets || !lengths || nseq < 1 || !job_model || !job_seq || njobs < 1) ERRF(CMGB_EINCOMPAT, "%s, no jobs", fn);
+  if ((!seqs && !d_seqs) || !offsets || !lengths || nseq < 1 || !job_model || !job_seq || njobs < 1) ERRF(CMGB_EINCOMPAT, "%s, no jobs", fn);
   for (int k = 0; k < nmodels; k++)
     if (!models[k] || models[k]->ctx != c) ERRF(CMGB_EINCOMPAT, "%s, model %d is NULL or belongs to another context", fn, k);
   for (int q = 0; q < nseq; q++)
@@ -1331,7 +1362,7 @@ extern "C" int cmgb_ScanMulti(cmgb_ctx *c, cmgb_model *const *models, int nmodel
     if (smem + 64 > c->max_smem_optin) ERRF(CMGB_ERANGE, "%s, %d bytes of shared memory per CTA exceed the device", fn, smem);
 
     auto al = [](size_t x) { return (x + 255) & ~(size_t) 255; };
-    const size_t o_ws = al((size_t) seqs_len), o_we = o_ws + al(sizeof(long long) * nw), o_ws0 = o_we + al(sizeof(long long) * nw);
+    const size_t o_ws = d_seqs ? 0 : al((size_t) seqs_len), o_we = o_ws + al(sizeof(long long) * nw), o_ws0 = o_we + al(sizeof(long long) * nw);
     const size_t o_cm = o_ws0 + al(sizeof(long long) * nw), o_kp = o_cm + al(sizeof(int) * nw);
     const size_t o_out = o_kp + al(sizeof(KParams) * (size_t) nmodels);
     const size_t out_bytes = sizeof(long long) * 2 * nw + sizeof(unsigned) * nw;
@@ -1375,7 +1406,7 @@ extern "C" int cmgb_ScanMulti(cmgb_ctx *c, cmgb_model *const *models, int nmodel
         kp.st = plan[mi]->d_states; kp.plan = plan[mi]->plan; kp.rec = plan[mi]->d_rec; kp.arena = c->d_arena;
         kp.plan.smem_elems = max_elems; kp.plan.carry_elems = max_carry; kp.plan.ring_elems = max_ring; kp.plan.arena_elems = max_arena;
         kp.oesc = m->d_oesc; kp.ioesc = m->d_ioesc; kp.ilog = c->d_ilog; kp.flog = c->d_flog;
-        kp.dsq = blk; kp.i0 = 1; kp.j0 = seqs_len - 2; kp.nwin = nw;
+        kp.dsq = d_seqs ? d_seqs : blk; kp.i0 = 1; kp.j0 = seqs_len - 2; kp.nwin = nw;
         kp.queue = &c->d_ctl->queue; kp.carry = c->d_carry; kp.ring = c->d_ring;
         kp.cand = c->d_cand; kp.ncand = &c->d_ctl->ncand; kp.cand_cap = c->cand_cap;
         kp.cand_cut = hitlist ? cutoffs[mi] : 3.0e38f; kp.cand_pos = (hitlist && !greedy) ? 1 : 0; kp.env_cut = ecut;
@@ -1392,7 +1423,7 @@ extern "C" int cmgb_ScanMulti(cmgb_ctx *c, cmgb_model *const *models, int nmodel
       k0.multi = reinterpret_cast<const KParams *>(blk + o_kp);
       k0.item_cm = reinterpret_cast<const int *>(blk + o_cm);
       std::memset(h, 0, sizeof(Control));
-      CUDA_TRY(cudaMemcpyAsync(blk, seqs, (size_t) seqs_len, cudaMemcpyHostToDevice, c->stream));
+      if (!d_seqs) CUDA_TRY(cudaMemcpyAsync(blk, seqs, (size_t) seqs_len, cudaMemcpyHostToDevice, c->stream));
       CUDA_TRY(cudaMemcpyAsync(blk + o_ws, ws.data(), sizeof(long long) * nw, cudaMemcpyHostToDevice, c->stream));
       CUDA_TRY(cudaMemcpyAsync(blk + o_we, we.data(), sizeof(long long) * nw, cudaMemcpyHostToDevice, c->stream));
       CUDA_TRY(cudaMemcpyAsync(blk + o_ws0, ws0.data(), sizeof(long long) * nw, cudaMemcpyHostToDevice, c->stream));
@@ -1400,7 +1431,7 @@ extern "C" int cmgb_ScanMulti(cmgb_ctx *c, cmgb_model *const *models, int nmodel
       CUDA_TRY(cudaMemcpyAsync(blk + o_kp, kps.data(), sizeof(KParams) * kps.size(), cudaMemcpyHostToDevice, c->stream));
       CUDA_TRY(cudaMemcpyAsync(blk + o_out, out_init.data(), out_bytes, cudaMemcpyHostToDevice, c->stream));
       CUDA_TRY(cudaMemcpyAsync(c->d_ctl, h, sizeof(Control), cudaMemcpyHostToDevice, c->stream));
-      h2d += seqs_len + (int64_t) (3 * sizeof(long long) * nw + sizeof(int) * nw + sizeof(KParams) * kps.size() + out_bytes + sizeof(Control));
+      h2d += (d_seqs ? 0 : seqs_len) + (int64_t) (3 * sizeof(long long) * nw + sizeof(int) * nw + sizeof(KParams) * kps.size() + out_bytes + sizeof(Control));
       CUDA_TRY(cudaEventRecord(c->ev0, c->stream));
       launch_any(alg, gl, grid, c->threads, (size_t) smem, c->stream, k0, true);
       CUDA_TRY(cudaGetLastError());
@@ -1428,14 +1459,18 @@ extern "C" int cmgb_ScanMulti(cmgb_ctx *c, cmgb_model *const *models, int nmodel
       d2h += (int64_t) sizeof(Cand) * n;
       std::vector<Cand> raw((size_t) n);
       CUDA_TRY(cudaMemcpy(raw.data(), c->d_cand, sizeof(Cand) * (size_t) n, cudaMemcpyDeviceToHost));
-      std::vector<int> by_off(nseq);
-      for (int q = 0; q < nseq; q++) by_off[q] = q;
-      std::sort(by_off.begin(), by_off.end(), [&](int a, int b) { return offsets[a] < offsets[b]; });
+      // per model, its jobs' sequences by offset: sequences of different
+      // models may overlap (each model scanning its own regions of one buffer)
+      std::vector<std::vector<int>> mseq((size_t) nmodels);
+      for (int k = 0; k < njobs; k++) mseq[job_model[k]].push_back(job_seq[k]);
+      for (auto &v : mseq) std::sort(v.begin(), v.end(), [&](int a, int b) { return offsets[a] < offsets[b]; });
       for (int i = 0; i < n; i++) {
         const Cand &cc = raw[i];
-        int lo = 0, hi = nseq - 1;   // last sequence whose offset is below j
-        while (lo < hi) { const int mid = (lo + hi + 1) / 2; if (offsets[by_off[mid]] < cc.j) lo = mid; else hi = mid - 1; }
-        const int k = job_of(cc.pad, by_off[lo]);
+        const std::vector<int> &sq = mseq[cc.pad];
+        if (sq.empty()) ERRF(CMGB_EINCOMPAT, "%s, a candidate cell matches no job", fn);
+        int lo = 0, hi = (int) sq.size() - 1;   // the model's last sequence whose offset is below j
+        while (lo < hi) { const int mid = (lo + hi + 1) / 2; if (offsets[sq[mid]] < cc.j) lo = mid; else hi = mid - 1; }
+        const int k = job_of(cc.pad, sq[lo]);
         if (k < 0) ERRF(CMGB_EINCOMPAT, "%s, a candidate cell matches no job", fn);
         CandHost x; x.j = cc.j; x.d = cc.d; x.sc = cc.sc; x.r = cc.r; x.mode = CMGB_TRMODE_J;
         per[k].push_back(x);
@@ -1449,6 +1484,19 @@ extern "C" int cmgb_ScanMulti(cmgb_ctx *c, cmgb_model *const *models, int nmodel
       bestj[k] = std::max(bestj[k], best[w]);
     }
   }
+  // device-resident residues: host copies of the sequences whose candidates need NULL3 compositions
+  std::vector<uint8_t> hres;
+  if (d_seqs && hitlist && do_null3) {
+    std::vector<char> need((size_t) nseq, 0);
+    for (int k = 0; k < njobs; k++) if (!per[k].empty()) need[job_seq[k]] = 1;
+    for (int q = 0; q < nseq; q++) {
+      if (!need[q]) continue;
+      if (hres.empty()) hres.assign((size_t) seqs_len, (uint8_t) 255);
+      CUDA_TRY(cudaMemcpy(hres.data() + offsets[q] + 1, d_seqs + offsets[q] + 1, (size_t) lengths[q], cudaMemcpyDeviceToHost));
+      d2h += lengths[q];
+    }
+  }
+  const uint8_t *hseq = d_seqs ? (hres.empty() ? nullptr : hres.data()) : seqs;
   c->last_ms = total_ms;
   c->last_launches = launches;
   c->last_h2d = h2d; c->last_d2h = d2h;
@@ -1465,7 +1513,7 @@ extern "C" int cmgb_ScanMulti(cmgb_ctx *c, cmgb_model *const *models, int nmodel
       ResolveArgs ra;
       ra.null = m->null.data(); ra.K = m->K; ra.null3_omega = m->null3_omega; ra.do_null3 = do_null3;
       ra.greedy = (m->flags & CMGB_NOTGREEDY) ? 0 : 1; ra.cutoff = cutoffs[job_model[k]];
-      ra.i0 = off + 1; ra.j0 = off + lengths[q]; ra.dsq = seqs;
+      ra.i0 = off + 1; ra.j0 = off + lengths[q]; ra.dsq = hseq;
       resolve_hits(per[k], ra, hitlist->h);
       for (size_t x = (size_t) before; x < hitlist->h.size(); x++) { hitlist->h[x].start -= off; hitlist->h[x].stop -= off; }
     }
@@ -1481,7 +1529,9 @@ extern "C" int cmgb_autotune(cmgb_ctx *c, cmgb_model *m, int qdbidx, int algo, i
                              int *ret_tile_rows, int *ret_arena, char *errbuf)
 {
   if (!c || !m || qdbidx < 0 || qdbidx > 2 || algo < 0 || algo > 2) ERRF(CMGB_EINVAL, "cmgb_autotune: invalid argument");
-  if (sample_len <= 0) sample_len = (int64_t) c->nsm * 1500;
+  // default sample: enough windows of 8 W residues for every resident CTA
+  // (up to two per SM) to scan two, so each candidate shape is timed on a full grid
+  if (sample_len <= 0) sample_len = std::max<int64_t>((int64_t) c->nsm * 1500, (int64_t) c->nsm * 4 * 8 * m->W);
   std::vector<uint8_t> dsq((size_t) sample_len + 2);
   uint64_t x = 0x9E3779B97F4A7C15ULL;
   for (int64_t i = 1; i <= sample_len; i++) {            // 40% GC, splitmix-style generator

@@ -5,14 +5,16 @@
 // length <= W lies inside the first-half-start window), one-hot ACGU input,
 // six convolutions of kernel 9 with dilations 1, 2, 4, 8, 16, 32 (4 -> 128
 // channels, then 128 -> 128), ReLU after each, max-pool over the window's
-// positions, a linear 128 -> 1 read-out.  Each window is zero-padded at its
-// ends, as the training network's 'same' padding.  Weights and activations
-// are BF16, accumulation FP32.
+// positions, a linear 128 -> 1 read-out per head (one head per CM when one
+// network filters for several CMs: the convolutions are shared, each CM has
+// its own read-out and threshold).  Each window is zero-padded at its ends,
+// as the training network's 'same' padding.  Weights and activations are
+// BF16, accumulation FP32.
 //
 // Layout in HBM: activations [nwin][LP][128] bf16 with LP = 2W rounded up to
 // the 128-row tile (rows >= 2W hold zeros); layer 0 weights [9][4][128] f32
 // (a gather: the input is one-hot); layers 1-5 weights [5][9][128 co][128 ci]
-// bf16, biases [6][128] f32, read-out [128] + 1 f32.
+// bf16, biases [6][128] f32, read-out [heads][128 + 1] f32.
 //
 // Layers 1-5 are implicit GEMMs (M = window positions, N = 128 output
 // channels, K = 9 taps x 128 input channels) on the fifth-generation tensor
@@ -43,11 +45,11 @@ constexpr int DIL[NL] = {1, 2, 4, 8, 16, 32};
 }
 
 struct cmgb_filter_s {
-  int W = 0, LP = 0;
+  int W = 0, LP = 0, H = 1;           // H: read-out heads
   float *d_w0 = nullptr;              // [9][4][128]
   unsigned short *d_w = nullptr;      // [5][9][128][128] bf16 bits
   float *d_b = nullptr;               // [6][128]
-  float *d_out = nullptr;             // [129]
+  float *d_out = nullptr;             // [H][129]
   unsigned short *d_act[2] = {nullptr, nullptr};
   size_t act_rows = 0;
   float *d_logit = nullptr; size_t logit_n = 0;
@@ -216,42 +218,48 @@ __global__ void __launch_bounds__(128, 1) filter_conv_tc(const unsigned short *i
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(taddr), "r"(128) : "memory");
 }
 
-// Read-out: max over the window's positions per channel, then the linear layer.
-__global__ void filter_readout(const unsigned short *act, int LP, int W2, const float *wout, float *logit)
+// Read-out: max over the window's positions per channel, then each head's
+// linear layer (logit[win][h]; the same tree sum per head).
+__global__ void filter_readout(const unsigned short *act, int LP, int W2, const float *wout, int H, float *logit)
 {
   __shared__ float red[CH];
   const int win = blockIdx.x, co = threadIdx.x;
   const unsigned short *a = act + (size_t) win * LP * CH + co;
   float m = 0.f;   // activations are ReLU outputs (>= 0)
   for (int i = 0; i < W2; i++) { const float v = bf2f(a[(size_t) i * CH]); m = v > m ? v : m; }
-  red[co] = m * wout[co];
-  __syncthreads();
-  for (int s = CH / 2; s > 0; s >>= 1) { if (co < s) red[co] += red[co + s]; __syncthreads(); }
-  if (co == 0) logit[win] = red[0] + wout[CH];
+  for (int h = 0; h < H; h++) {
+    const float *wo = wout + (size_t) h * (CH + 1);
+    red[co] = m * wo[co];
+    __syncthreads();
+    for (int s = CH / 2; s > 0; s >>= 1) { if (co < s) red[co] += red[co + s]; __syncthreads(); }
+    if (co == 0) logit[(size_t) win * H + h] = red[0] + wo[CH];
+    __syncthreads();
+  }
 }
 #endif
 
-extern "C" int cmgb_filter_create(cmgb_ctx *ctx, int W, const float *w0, const uint16_t *w, const float *bias,
-                                  const float *wout, cmgb_filter **ret, char *errbuf)
+extern "C" int cmgb_filter_create_heads(cmgb_ctx *ctx, int W, int nheads, const float *w0, const uint16_t *w,
+                                        const float *bias, const float *wout, cmgb_filter **ret, char *errbuf)
 {
   (void) ctx;
   *ret = nullptr;
 #ifdef CMGB_HOST_EMULATION
-  (void) W; (void) w0; (void) w; (void) bias; (void) wout;
+  (void) W; (void) nheads; (void) w0; (void) w; (void) bias; (void) wout;
   FERR(CMGB_ENODEV, "filter: not available in the host emulation");
 #else
-  if (W < 1 || !w0 || !w || !bias || !wout) FERR(CMGB_EINVAL, "filter: invalid arguments");
+  if (W < 1 || nheads < 1 || nheads > CMGB_FILTER_MAX_HEADS || !w0 || !w || !bias || !wout)
+    FERR(CMGB_EINVAL, "filter: invalid arguments");
   std::unique_ptr<cmgb_filter> f(new cmgb_filter);
-  f->W = W;
+  f->W = W; f->H = nheads;
   f->LP = ((2 * W + TILE - 1) / TILE) * TILE;
   FCUDA(cudaMalloc(&f->d_w0, sizeof(float) * KT * 4 * CH));
   FCUDA(cudaMalloc(&f->d_w, sizeof(unsigned short) * 5 * KT * CH * CH));
   FCUDA(cudaMalloc(&f->d_b, sizeof(float) * NL * CH));
-  FCUDA(cudaMalloc(&f->d_out, sizeof(float) * (CH + 1)));
+  FCUDA(cudaMalloc(&f->d_out, sizeof(float) * (CH + 1) * nheads));
   FCUDA(cudaMemcpy(f->d_w0, w0, sizeof(float) * KT * 4 * CH, cudaMemcpyHostToDevice));
   FCUDA(cudaMemcpy(f->d_w, w, sizeof(unsigned short) * 5 * KT * CH * CH, cudaMemcpyHostToDevice));
   FCUDA(cudaMemcpy(f->d_b, bias, sizeof(float) * NL * CH, cudaMemcpyHostToDevice));
-  FCUDA(cudaMemcpy(f->d_out, wout, sizeof(float) * (CH + 1), cudaMemcpyHostToDevice));
+  FCUDA(cudaMemcpy(f->d_out, wout, sizeof(float) * (CH + 1) * nheads, cudaMemcpyHostToDevice));
   FCUDA(cudaMalloc(&f->d_err, sizeof(int)));
   FCUDA(cudaMemset(f->d_err, 0, sizeof(int)));
   const int maxsm = 16 * (TILE + 8 * DIL[NL - 1]) * 16 + 16 * CH * 16 + 64;
@@ -259,6 +267,12 @@ extern "C" int cmgb_filter_create(cmgb_ctx *ctx, int W, const float *w0, const u
   *ret = f.release();
   return CMGB_OK;
 #endif
+}
+
+extern "C" int cmgb_filter_create(cmgb_ctx *ctx, int W, const float *w0, const uint16_t *w, const float *bias,
+                                  const float *wout, cmgb_filter **ret, char *errbuf)
+{
+  return cmgb_filter_create_heads(ctx, W, 1, w0, w, bias, wout, ret, errbuf);
 }
 
 extern "C" void cmgb_filter_destroy(cmgb_filter *f)
@@ -293,10 +307,10 @@ extern "C" int cmgb_filter_windows(cmgb_ctx *ctx, cmgb_filter *f, const uint8_t 
     FCUDA(cudaMalloc(&f->d_act[1], rows * CH * sizeof(unsigned short)));
     f->act_rows = rows;
   }
-  if ((size_t) nwin > f->logit_n) {
+  if ((size_t) nwin * f->H > f->logit_n) {
     cudaFree(f->d_logit); f->d_logit = nullptr;
-    FCUDA(cudaMalloc(&f->d_logit, sizeof(float) * nwin));
-    f->logit_n = nwin;
+    FCUDA(cudaMalloc(&f->d_logit, sizeof(float) * nwin * f->H));
+    f->logit_n = (size_t) nwin * f->H;
   }
   cudaEvent_t e0, e1;
   FCUDA(cudaEventCreate(&e0)); FCUDA(cudaEventCreate(&e1));
@@ -313,10 +327,10 @@ extern "C" int cmgb_filter_windows(cmgb_ctx *ctx, cmgb_filter *f, const uint8_t 
     FCUDA(cudaGetLastError());
     cur ^= 1;
   }
-  filter_readout<<<nwin, CH>>>(f->d_act[cur], f->LP, (int) (2 * W), f->d_out, f->d_logit);
+  filter_readout<<<nwin, CH>>>(f->d_act[cur], f->LP, (int) (2 * W), f->d_out, f->H, f->d_logit);
   FCUDA(cudaGetLastError());
   FCUDA(cudaEventRecord(e1));
-  FCUDA(cudaMemcpy(ret_logits, f->d_logit, sizeof(float) * nwin, cudaMemcpyDeviceToHost));
+  FCUDA(cudaMemcpy(ret_logits, f->d_logit, sizeof(float) * nwin * f->H, cudaMemcpyDeviceToHost));
   int herr = 0;
   FCUDA(cudaMemcpy(&herr, f->d_err, sizeof(int), cudaMemcpyDeviceToHost));
   if (herr) FERR(CMGB_ENODEV, "filter: a bounded tensor-core wait ran out");
@@ -357,17 +371,19 @@ constexpr int NB_W0 = 128;     // partial slots of layer 0's weight gradient (po
 constexpr size_t OFF_W0 = 0;                                   // [9][4][128]
 constexpr size_t OFF_W = OFF_W0 + (size_t) KT * 4 * CH;        // [5][9][128 co][128 ci]
 constexpr size_t OFF_B = OFF_W + (size_t) 5 * KT * CH * CH;    // [6][128]
-constexpr size_t OFF_WOUT = OFF_B + (size_t) NL * CH;          // [128] + bias
-constexpr size_t NPARAM = OFF_WOUT + CH + 1;
+constexpr size_t OFF_WOUT = OFF_B + (size_t) NL * CH;          // [heads][128 + bias]
+inline size_t nparam(int H) { return OFF_WOUT + (size_t) H * (CH + 1); }
 }
 
 struct cmgb_filter_trainer_s {
-  int W = 0, LP = 0, B = 0;
+  int W = 0, LP = 0, B = 0, H = 1;                  // H: read-out heads
+  size_t np = 0;                                    // parameters
+  float *posw = nullptr;                            // [H] positive-class weights
   long long t = 0;                                  // AdamW steps taken
-  float *p = nullptr, *g = nullptr, *m1 = nullptr, *m2 = nullptr;   // [NPARAM] each
+  float *p = nullptr, *g = nullptr, *m1 = nullptr, *m2 = nullptr;   // [np] each
   unsigned short *wbf = nullptr, *wtbf = nullptr;   // [5][9][128][128]
   unsigned char *win = nullptr;                     // [B][2W]
-  float *y = nullptr, *pooled = nullptr, *logit = nullptr, *dlogit = nullptr, *loss = nullptr;
+  float *y = nullptr, *pooled = nullptr, *logit = nullptr, *dlogit = nullptr, *loss = nullptr;   // y, logit, dlogit: [B][H]
   int *argm = nullptr;
   unsigned short *act[NL] = {nullptr};              // [B][LP][128]
   unsigned short *dz[2] = {nullptr, nullptr};
@@ -379,8 +395,8 @@ struct cmgb_filter_trainer_s {
 };
 
 #ifndef CMGB_HOST_EMULATION
-// max over positions (first arg-max) per channel, then the read-out
-__global__ void train_readout_fwd(const unsigned short *act, int LP, int W2, const float *wout, float *pooled, int *argm,
+// max over positions (first arg-max) per channel, then each head's read-out
+__global__ void train_readout_fwd(const unsigned short *act, int LP, int W2, const float *wout, int H, float *pooled, int *argm,
                                   float *logit)
 {
   __shared__ float red[CH];
@@ -389,24 +405,28 @@ __global__ void train_readout_fwd(const unsigned short *act, int LP, int W2, con
   float m = 0.f; int am = 0;
   for (int i = 0; i < W2; i++) { const float v = bf2f(a[(size_t) i * CH]); if (v > m) { m = v; am = i; } }
   pooled[b * CH + c] = m; argm[b * CH + c] = am;
-  red[c] = m * wout[c];
-  __syncthreads();
-  for (int s = CH / 2; s > 0; s >>= 1) { if (c < s) red[c] += red[c + s]; __syncthreads(); }
-  if (c == 0) logit[b] = red[0] + wout[CH];
+  for (int h = 0; h < H; h++) {
+    const float *wo = wout + (size_t) h * (CH + 1);
+    red[c] = m * wo[c];
+    __syncthreads();
+    for (int s = CH / 2; s > 0; s >>= 1) { if (c < s) red[c] += red[c + s]; __syncthreads(); }
+    if (c == 0) logit[(size_t) b * H + h] = red[0] + wo[CH];
+    __syncthreads();
+  }
 }
 
-// loss = mean_b [ -w y log s(z) - (1 - y) log(1 - s(z)) ],  dz = d loss / d z
-__global__ void train_loss(const float *logit, const float *y, float posw, int B, float *dlogit, float *loss)
+// loss = (1/B) sum_b sum_h [ -w_h y log s(z) - (1 - y) log(1 - s(z)) ],  dz = d loss / d z
+__global__ void train_loss(const float *logit, const float *y, const float *posw_h, int B, int H, float *dlogit, float *loss)
 {
   __shared__ float red[256];
   float acc = 0.f;
-  for (int b = threadIdx.x; b < B; b += blockDim.x) {
-    const float z = logit[b], t = y[b];
+  for (int q = threadIdx.x; q < B * H; q += blockDim.x) {
+    const float z = logit[q], t = y[q], posw = posw_h[q % H];
     const float ls = z >= 0.f ? -log1pf(expf(-z)) : z - log1pf(expf(z));        // log s(z)
     const float l1s = z >= 0.f ? -z - log1pf(expf(-z)) : -log1pf(expf(z));      // log (1 - s(z))
     const float s = 1.f / (1.f + expf(-z));
     acc += -posw * t * ls - (1.f - t) * l1s;
-    dlogit[b] = (posw * t * (s - 1.f) + (1.f - t) * s) / (float) B;
+    dlogit[q] = (posw * t * (s - 1.f) + (1.f - t) * s) / (float) B;
   }
   red[threadIdx.x] = acc;
   __syncthreads();
@@ -424,24 +444,28 @@ __global__ void train_sum_parts(const float *part, int nparts, long long n, floa
   }
 }
 
-// read-out backward: the layer-5 gradient at the arg-max cells (one block per window)
-__global__ void train_readout_bwd(const float *dlogit, const float *pooled, const int *argm, const float *wout, int LP,
+// read-out backward: the layer-5 gradient at the arg-max cells (one block
+// per window), summed over the heads in head order
+__global__ void train_readout_bwd(const float *dlogit, const float *pooled, const int *argm, const float *wout, int H, int LP,
                                   unsigned short *dz5)
 {
   const int b = blockIdx.x, c = threadIdx.x;
-  const float d = dlogit[b], pv = pooled[b * CH + c];
-  if (pv > 0.f) dz5[((size_t) b * LP + argm[b * CH + c]) * CH + c] = f2bf(d * wout[c]);
+  const float pv = pooled[b * CH + c];
+  float d = dlogit[(size_t) b * H] * wout[c];
+  for (int h = 1; h < H; h++) d += dlogit[(size_t) b * H + h] * wout[(size_t) h * (CH + 1) + c];
+  if (pv > 0.f) dz5[((size_t) b * LP + argm[b * CH + c]) * CH + c] = f2bf(d);
 }
 
-// read-out weight gradients: thread c < 128 sums dlogit[b] * pooled[b][c] over
-// the batch in window order, thread 128 the bias term (CH + 1 threads)
-__global__ void train_readout_wgrad(const float *dlogit, const float *pooled, int B, float *g_wout)
+// read-out weight gradients, block h = head: thread c < 128 sums
+// dlogit[b][h] * pooled[b][c] over the batch in window order, thread 128 the
+// bias term (CH + 1 threads)
+__global__ void train_readout_wgrad(const float *dlogit, const float *pooled, int B, int H, float *g_wout)
 {
-  const int c = threadIdx.x;
+  const int h = blockIdx.x, c = threadIdx.x;
   float s = 0.f;
-  if (c < CH) for (int b = 0; b < B; b++) s += dlogit[b] * pooled[(size_t) b * CH + c];
-  else for (int b = 0; b < B; b++) s += dlogit[b];
-  g_wout[c] = s;
+  if (c < CH) for (int b = 0; b < B; b++) s += dlogit[(size_t) b * H + h] * pooled[(size_t) b * CH + c];
+  else for (int b = 0; b < B; b++) s += dlogit[(size_t) b * H + h];
+  g_wout[(size_t) h * (CH + 1) + c] = s;
 }
 
 // bias gradient, partial: block k sums rows k, k + gridDim.x, .. of dz into part[k][c]
@@ -546,25 +570,30 @@ __global__ void train_pack(const float *w, unsigned short *wbf, unsigned short *
 }
 #endif
 
-extern "C" int cmgb_filter_trainer_create(cmgb_ctx *ctx, int W, int batch, uint64_t seed, cmgb_filter_trainer **ret, char *errbuf)
+extern "C" int cmgb_filter_trainer_create_heads(cmgb_ctx *ctx, int W, int batch, int nheads, uint64_t seed,
+                                                cmgb_filter_trainer **ret, char *errbuf)
 {
   (void) ctx;
   *ret = nullptr;
 #ifdef CMGB_HOST_EMULATION
-  (void) W; (void) batch; (void) seed;
+  (void) W; (void) batch; (void) nheads; (void) seed;
   FERR(CMGB_ENODEV, "filter trainer: not available in the host emulation");
 #else
-  if (W < 16 || batch < 1 || batch > 65535) FERR(CMGB_EINVAL, "filter trainer: invalid W or batch");
+  if (W < 16 || batch < 1 || batch > 65535 || nheads < 1 || nheads > CMGB_FILTER_MAX_HEADS)
+    FERR(CMGB_EINVAL, "filter trainer: invalid W, batch or head count");
   std::unique_ptr<cmgb_filter_trainer> f(new cmgb_filter_trainer);
-  f->W = W; f->B = batch; f->LP = ((2 * W + TILE - 1) / TILE) * TILE;
+  f->W = W; f->B = batch; f->H = nheads; f->LP = ((2 * W + TILE - 1) / TILE) * TILE;
+  f->np = nparam(nheads);
+  const size_t NPARAM = f->np;
   const size_t act = (size_t) batch * f->LP * CH * sizeof(unsigned short);
   FCUDA(cudaMalloc(&f->p, NPARAM * sizeof(float))); FCUDA(cudaMalloc(&f->g, NPARAM * sizeof(float)));
   FCUDA(cudaMalloc(&f->m1, NPARAM * sizeof(float))); FCUDA(cudaMalloc(&f->m2, NPARAM * sizeof(float)));
   FCUDA(cudaMemset(f->m1, 0, NPARAM * sizeof(float))); FCUDA(cudaMemset(f->m2, 0, NPARAM * sizeof(float)));
   FCUDA(cudaMalloc(&f->wbf, (size_t) 5 * KT * CH * CH * 2)); FCUDA(cudaMalloc(&f->wtbf, (size_t) 5 * KT * CH * CH * 2));
   FCUDA(cudaMalloc(&f->win, (size_t) batch * 2 * W));
-  FCUDA(cudaMalloc(&f->y, sizeof(float) * batch)); FCUDA(cudaMalloc(&f->pooled, sizeof(float) * batch * CH));
-  FCUDA(cudaMalloc(&f->logit, sizeof(float) * batch)); FCUDA(cudaMalloc(&f->dlogit, sizeof(float) * batch));
+  FCUDA(cudaMalloc(&f->y, sizeof(float) * batch * nheads)); FCUDA(cudaMalloc(&f->pooled, sizeof(float) * batch * CH));
+  FCUDA(cudaMalloc(&f->logit, sizeof(float) * batch * nheads)); FCUDA(cudaMalloc(&f->dlogit, sizeof(float) * batch * nheads));
+  FCUDA(cudaMalloc(&f->posw, sizeof(float) * nheads));
   FCUDA(cudaMalloc(&f->loss, sizeof(float))); FCUDA(cudaMalloc(&f->argm, sizeof(int) * batch * CH));
   for (int l = 0; l < NL; l++) FCUDA(cudaMalloc(&f->act[l], act));
   FCUDA(cudaMalloc(&f->dz[0], act)); FCUDA(cudaMalloc(&f->dz[1], act));
@@ -584,7 +613,8 @@ extern "C" int cmgb_filter_trainer_create(cmgb_ctx *ctx, int W, int batch, uint6
   const double a0 = std::sqrt(6.0 / (4 * KT)), a1 = std::sqrt(6.0 / (CH * KT)), a2 = std::sqrt(6.0 / CH);
   for (size_t i = OFF_W0; i < OFF_W; i++) h[i] = (float) (a0 * uni());
   for (size_t i = OFF_W; i < OFF_B; i++) h[i] = (float) (a1 * uni());
-  for (size_t i = OFF_WOUT; i < OFF_WOUT + CH; i++) h[i] = (float) (a2 * uni());
+  for (int hd = 0; hd < nheads; hd++)
+    for (size_t i = OFF_WOUT + (size_t) hd * (CH + 1); i < OFF_WOUT + (size_t) hd * (CH + 1) + CH; i++) h[i] = (float) (a2 * uni());
   FCUDA(cudaMemcpy(f->p, h.data(), NPARAM * sizeof(float), cudaMemcpyHostToDevice));
   train_pack<<<512, 256>>>(f->p + OFF_W, f->wbf, f->wtbf);
   FCUDA(cudaGetLastError());
@@ -596,6 +626,11 @@ extern "C" int cmgb_filter_trainer_create(cmgb_ctx *ctx, int W, int batch, uint6
 #endif
 }
 
+extern "C" int cmgb_filter_trainer_create(cmgb_ctx *ctx, int W, int batch, uint64_t seed, cmgb_filter_trainer **ret, char *errbuf)
+{
+  return cmgb_filter_trainer_create_heads(ctx, W, batch, 1, seed, ret, errbuf);
+}
+
 extern "C" void cmgb_filter_trainer_destroy(cmgb_filter_trainer *f)
 {
   if (!f) return;
@@ -604,7 +639,7 @@ extern "C" void cmgb_filter_trainer_destroy(cmgb_filter_trainer *f)
   cudaFree(f->win); cudaFree(f->y); cudaFree(f->pooled); cudaFree(f->logit); cudaFree(f->dlogit); cudaFree(f->loss);
   cudaFree(f->argm); for (int l = 0; l < NL; l++) cudaFree(f->act[l]);
   cudaFree(f->dz[0]); cudaFree(f->dz[1]); cudaFree(f->err);
-  cudaFree(f->part_w); cudaFree(f->part_b); cudaFree(f->part_w0);
+  cudaFree(f->part_w); cudaFree(f->part_b); cudaFree(f->part_w0); cudaFree(f->posw);
 #endif
   delete f;
 }
@@ -622,8 +657,8 @@ extern "C" int cmgb_filter_trainer_set(cmgb_filter_trainer *f, const float *w0, 
   FCUDA(cudaMemcpy(f->p + OFF_W0, w0, sizeof(float) * (OFF_W - OFF_W0), cudaMemcpyHostToDevice));
   FCUDA(cudaMemcpy(f->p + OFF_W, w, sizeof(float) * (OFF_B - OFF_W), cudaMemcpyHostToDevice));
   FCUDA(cudaMemcpy(f->p + OFF_B, bias, sizeof(float) * (OFF_WOUT - OFF_B), cudaMemcpyHostToDevice));
-  FCUDA(cudaMemcpy(f->p + OFF_WOUT, wout, sizeof(float) * (CH + 1), cudaMemcpyHostToDevice));
-  FCUDA(cudaMemset(f->m1, 0, NPARAM * sizeof(float))); FCUDA(cudaMemset(f->m2, 0, NPARAM * sizeof(float)));
+  FCUDA(cudaMemcpy(f->p + OFF_WOUT, wout, sizeof(float) * (CH + 1) * f->H, cudaMemcpyHostToDevice));
+  FCUDA(cudaMemset(f->m1, 0, f->np * sizeof(float))); FCUDA(cudaMemset(f->m2, 0, f->np * sizeof(float)));
   f->t = 0;
   train_pack<<<512, 256>>>(f->p + OFF_W, f->wbf, f->wtbf);
   FCUDA(cudaGetLastError());
@@ -634,20 +669,23 @@ extern "C" int cmgb_filter_trainer_set(cmgb_filter_trainer *f, const float *w0, 
 // One step on a batch: windows (host, [batch][2W] residue codes 0-3, others
 // read as missing), labels (host, [batch] 0/1), the positive-class weight and
 // the learning rate (0: gradients only, no update).
-extern "C" int cmgb_filter_trainer_step(cmgb_filter_trainer *f, const uint8_t *windows, const float *labels, float pos_weight,
-                                        float lr, float weight_decay, float *ret_loss, float *ret_ms, char *errbuf)
+extern "C" int cmgb_filter_trainer_step_heads(cmgb_filter_trainer *f, const uint8_t *windows, const float *labels,
+                                              const float *pos_weights, float lr, float weight_decay, float *ret_loss,
+                                              float *ret_ms, char *errbuf)
 {
 #ifdef CMGB_HOST_EMULATION
-  (void) f; (void) windows; (void) labels; (void) pos_weight; (void) lr; (void) weight_decay; (void) ret_loss; (void) ret_ms;
+  (void) f; (void) windows; (void) labels; (void) pos_weights; (void) lr; (void) weight_decay; (void) ret_loss; (void) ret_ms;
   FERR(CMGB_ENODEV, "filter trainer: not available in the host emulation");
 #else
-  if (!f || !windows || !labels) FERR(CMGB_EINVAL, "filter trainer: invalid arguments");
-  const int B = f->B, W = f->W, LP = f->LP, W2 = 2 * W;
+  if (!f || !windows || !labels || !pos_weights) FERR(CMGB_EINVAL, "filter trainer: invalid arguments");
+  const int B = f->B, W = f->W, LP = f->LP, W2 = 2 * W, H = f->H;
+  const size_t NPARAM = f->np;
   const size_t actb = (size_t) B * LP * CH * sizeof(unsigned short);
   cudaEvent_t e0, e1;
   FCUDA(cudaEventCreate(&e0)); FCUDA(cudaEventCreate(&e1));
   FCUDA(cudaMemcpy(f->win, windows, (size_t) B * W2, cudaMemcpyHostToDevice));
-  FCUDA(cudaMemcpy(f->y, labels, sizeof(float) * B, cudaMemcpyHostToDevice));
+  FCUDA(cudaMemcpy(f->y, labels, sizeof(float) * B * H, cudaMemcpyHostToDevice));
+  FCUDA(cudaMemcpy(f->posw, pos_weights, sizeof(float) * H, cudaMemcpyHostToDevice));
   FCUDA(cudaEventRecord(e0));
   // forward
   filter_layer0<<<dim3(64, B), CH>>>(f->win, 0, (long long) B * W2 - 1, W, W2, B, LP, f->p + OFF_W0, f->p + OFF_B, f->act[0]);
@@ -657,13 +695,13 @@ extern "C" int cmgb_filter_trainer_step(cmgb_filter_trainer *f, const uint8_t *w
     filter_conv_tc<<<dim3(LP / TILE, B), 128, sm>>>(f->act[l - 1], f->act[l], LP, W2, d, f->wbf + (size_t) (l - 1) * KT * CH * CH,
                                                     f->p + OFF_B + l * CH, f->err, nullptr);
   }
-  train_readout_fwd<<<B, CH>>>(f->act[NL - 1], LP, W2, f->p + OFF_WOUT, f->pooled, f->argm, f->logit);
-  train_loss<<<1, 256>>>(f->logit, f->y, pos_weight, B, f->dlogit, f->loss);
+  train_readout_fwd<<<B, CH>>>(f->act[NL - 1], LP, W2, f->p + OFF_WOUT, H, f->pooled, f->argm, f->logit);
+  train_loss<<<1, 256>>>(f->logit, f->y, f->posw, B, H, f->dlogit, f->loss);
   // backward
   FCUDA(cudaMemset(f->g, 0, NPARAM * sizeof(float)));
   FCUDA(cudaMemset(f->dz[0], 0, actb));
-  train_readout_bwd<<<B, CH>>>(f->dlogit, f->pooled, f->argm, f->p + OFF_WOUT, LP, f->dz[0]);
-  train_readout_wgrad<<<1, CH + 1>>>(f->dlogit, f->pooled, B, f->g + OFF_WOUT);
+  train_readout_bwd<<<B, CH>>>(f->dlogit, f->pooled, f->argm, f->p + OFF_WOUT, H, LP, f->dz[0]);
+  train_readout_wgrad<<<H, CH + 1>>>(f->dlogit, f->pooled, B, H, f->g + OFF_WOUT);
   int cur = 0;
   const long long nw = (long long) KT * CH * CH;
   for (int l = NL - 1; l >= 1; l--) {
@@ -703,6 +741,14 @@ extern "C" int cmgb_filter_trainer_step(cmgb_filter_trainer *f, const uint8_t *w
 #endif
 }
 
+extern "C" int cmgb_filter_trainer_step(cmgb_filter_trainer *f, const uint8_t *windows, const float *labels, float pos_weight,
+                                        float lr, float weight_decay, float *ret_loss, float *ret_ms, char *errbuf)
+{
+  if (!f) FERR(CMGB_EINVAL, "filter trainer: invalid arguments");
+  std::vector<float> pw((size_t) f->H, pos_weight);
+  return cmgb_filter_trainer_step_heads(f, windows, labels, pw.data(), lr, weight_decay, ret_loss, ret_ms, errbuf);
+}
+
 // Copies out the fp32 master weights (set's layout) and, when gw0 != NULL, the
 // last step's gradients in the same layout (gw0, gw, gb, gwout).
 extern "C" int cmgb_filter_trainer_get(cmgb_filter_trainer *f, float *w0, float *w, float *bias, float *wout,
@@ -715,7 +761,7 @@ extern "C" int cmgb_filter_trainer_get(cmgb_filter_trainer *f, float *w0, float 
   if (!f) FERR(CMGB_EINVAL, "filter trainer: invalid arguments");
   const float *src[2] = {f->p, f->g};
   float *dst[2][4] = {{w0, w, bias, wout}, {gw0, gw, gb, gwout}};
-  const size_t off[5] = {OFF_W0, OFF_W, OFF_B, OFF_WOUT, NPARAM};
+  const size_t off[5] = {OFF_W0, OFF_W, OFF_B, OFF_WOUT, f->np};
   for (int k = 0; k < 2; k++)
     for (int j = 0; j < 4; j++)
       if (dst[k][j]) FCUDA(cudaMemcpy(dst[k][j], src[k] + off[j], sizeof(float) * (off[j + 1] - off[j]), cudaMemcpyDeviceToHost));

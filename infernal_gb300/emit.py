@@ -61,6 +61,67 @@ def sample(m: cf.CMModel, rng: np.random.Generator, max_len: int = 100000) -> st
     return walk(0)
 
 
+class Sampler:
+    """The same generative walk as :func:`sample`, from per-state cumulative
+    emission and transition tables drawn with a ``random.Random`` stream:
+    about fifty times faster, for bulk training data.  (Its random stream is
+    not ``sample``'s: the two give different sequences for one seed.)"""
+
+    def __init__(self, m: cf.CMModel):
+        import bisect
+        self._bisect = bisect.bisect_right
+        K = m.K
+        T = m.t_global if m.t_global is not None else m.t
+        self.st = [int(x) for x in m.sttype]
+        self.cf = [int(x) for x in m.cfirst]
+        self.cn = [int(x) for x in m.cnum]
+        self.ecum, self.tcum = [], []
+        for v in range(m.M):
+            st = self.st[v]
+            if st == cf.MP_st:
+                p = m.e[v, : K * K].astype(np.float64)
+            elif st in (cf.ML_st, cf.IL_st, cf.MR_st, cf.IR_st):
+                p = m.e[v, :K].astype(np.float64)
+            else:
+                p = None
+            self.ecum.append(list(np.cumsum(p / p.sum())) if p is not None else None)
+            if st in (cf.E_st, cf.B_st):
+                self.tcum.append(None)
+            else:
+                t = T[v, : self.cn[v]].astype(np.float64)
+                self.tcum.append(list(np.cumsum(t / t.sum())))
+
+    def _pick(self, cum, u):
+        k = self._bisect(cum, u)
+        return k if k < len(cum) else len(cum) - 1
+
+    def sample(self, rnd, max_len: int = 100000) -> str:
+        alph = "ACGU"
+        st, cfr, cn, ecum, tcum, pick = self.st, self.cf, self.cn, self.ecum, self.tcum, self._pick
+
+        def walk(v: int) -> str:
+            left: List[str] = []
+            right: List[str] = []
+            while True:
+                t = st[v]
+                if t == cf.E_st:
+                    return "".join(left) + "".join(reversed(right))
+                if t == cf.B_st:
+                    return "".join(left) + walk(cfr[v]) + walk(cn[v]) + "".join(reversed(right))
+                if t == cf.MP_st:
+                    x = pick(ecum[v], rnd.random())
+                    left.append(alph[x // 4]); right.append(alph[x % 4])
+                elif t == cf.ML_st or t == cf.IL_st:
+                    left.append(alph[pick(ecum[v], rnd.random())])
+                elif t == cf.MR_st or t == cf.IR_st:
+                    right.append(alph[pick(ecum[v], rnd.random())])
+                v = cfr[v] + pick(tcum[v], rnd.random())
+                if len(left) + len(right) > max_len:
+                    raise RuntimeError("runaway emission")
+
+        return walk(0)
+
+
 def background(rng: np.random.Generator, L: int, gc: float) -> np.ndarray:
     """iid residues (digital codes 0..3) with P(G)=P(C)=gc/2."""
     p = np.array([(1 - gc) / 2, gc / 2, gc / 2, (1 - gc) / 2])

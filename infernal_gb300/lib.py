@@ -38,7 +38,8 @@ EXPORTS = [
     "cmgb_RefTrCYKScan", "cmgb_RefITrInsideScan", "cmgb_RefTrCYKScan_dev", "cmgb_RefITrInsideScan_dev",
     "cmgb_ScanBatch", "cmgb_ScanMulti", "cmgb_Calibrate", "cmgb_filter_trainer_create", "cmgb_filter_trainer_destroy",
     "cmgb_filter_trainer_set", "cmgb_filter_trainer_step", "cmgb_filter_trainer_get", "cmgb_filter_create", "cmgb_filter_destroy", "cmgb_filter_windows",
-    "cmgb_measure_issue_peak", "cmgb_ScanBatch_dev",
+    "cmgb_measure_issue_peak", "cmgb_ScanBatch_dev", "cmgb_filter_create_heads", "cmgb_filter_trainer_create_heads",
+    "cmgb_filter_trainer_step_heads", "cmgb_ScanMulti_dev",
 ]
 BATCH_ALGOS = {"cyk": 0, "inside": 1, "finside": 2, "trcyk": 3, "trinside": 4}
 
@@ -104,6 +105,8 @@ def bind(path: str) -> ctypes.CDLL:
     lib.cmgb_ScanBatch_dev.restype = I
     lib.cmgb_ScanMulti.argtypes = [P, P, I, P, ctypes.c_char_p, I, I, P, I64, P, P, I, P, P, I, P, I, F, P, P, P, P]
     lib.cmgb_ScanMulti.restype = I
+    lib.cmgb_ScanMulti_dev.argtypes = lib.cmgb_ScanMulti.argtypes
+    lib.cmgb_ScanMulti_dev.restype = I
     lib.cmgb_Calibrate.argtypes = [P, P, ctypes.c_char_p, I, I64, I64, ctypes.c_uint64, I, P, P]
     lib.cmgb_Calibrate.restype = I
     lib.cmgb_filter_trainer_create.argtypes = [P, I, I, ctypes.c_uint64, ctypes.POINTER(P), ctypes.c_char_p]
@@ -121,6 +124,12 @@ def bind(path: str) -> ctypes.CDLL:
     lib.cmgb_filter_destroy.argtypes = [P]
     lib.cmgb_filter_windows.argtypes = [P, P, P, I64, I64, P, I64, ctypes.POINTER(I64), ctypes.POINTER(F), ctypes.c_char_p]
     lib.cmgb_filter_windows.restype = I
+    lib.cmgb_filter_create_heads.argtypes = [P, I, I, P, P, P, P, ctypes.POINTER(P), ctypes.c_char_p]
+    lib.cmgb_filter_create_heads.restype = I
+    lib.cmgb_filter_trainer_create_heads.argtypes = [P, I, I, I, ctypes.c_uint64, ctypes.POINTER(P), ctypes.c_char_p]
+    lib.cmgb_filter_trainer_create_heads.restype = I
+    lib.cmgb_filter_trainer_step_heads.argtypes = [P, P, P, P, F, F, P, P, ctypes.c_char_p]
+    lib.cmgb_filter_trainer_step_heads.restype = I
     lib.cmgb_measure_issue_peak.argtypes = [P, I, ctypes.POINTER(ctypes.c_double), ctypes.c_char_p]
     lib.cmgb_measure_issue_peak.restype = I
     lib.cmgb_autotune.argtypes = [P, P, I, I, I64, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.c_char_p]
@@ -351,21 +360,30 @@ class Scanner:
         return out
 
     def scan_multi(self, models, seqs, jobs=None, algo: str = "cyk", qdbidx: int = 1, cutoffs=None,
-                   do_null3: bool = True, env_cutoff: float = 0.0, want_hits: bool = True) -> List[ScanResult]:
+                   do_null3: bool = True, env_cutoff: float = 0.0, want_hits: bool = True,
+                   ranges=None, device_buf=None) -> List[ScanResult]:
         """Runs cmgb_ScanMulti: every (model index, sequence index) pair of
         jobs (default: all models x all sequences) in one persistent launch per
-        tile placement; returns one ScanResult per job, in job order."""
+        tile placement; returns one ScanResult per job, in job order.
+        ranges / device_buf: sequences as sub-ranges of one residue buffer, as
+        in scan_batch (cmgb_ScanMulti_dev when the buffer is on the device)."""
         if algo not in ("cyk", "inside", "finside"):
             raise ValueError("scan_multi runs the standard scanners only")
         mhs = [self.model(m, 0) for m in models]
         nm = len(models)
-        parts = [np.ascontiguousarray(x, dtype=np.uint8) for x in seqs]
-        lens = np.array([len(x) - 2 for x in parts], np.int64)
-        offs = np.zeros(len(parts), np.int64)
-        if len(parts) > 1:
-            offs[1:] = np.cumsum([len(x) for x in parts[:-1]])
-        buf = np.concatenate(parts + [np.full(1, cmfile.DSQ_SENTINEL, np.uint8)])
-        nseq = len(parts)
+        if ranges is not None:
+            buf, offs, lens = ranges
+            offs = np.ascontiguousarray(offs, np.int64)
+            lens = np.ascontiguousarray(lens, np.int64)
+            nseq = len(offs)
+        else:
+            parts = [np.ascontiguousarray(x, dtype=np.uint8) for x in seqs]
+            lens = np.array([len(x) - 2 for x in parts], np.int64)
+            offs = np.zeros(len(parts), np.int64)
+            if len(parts) > 1:
+                offs[1:] = np.cumsum([len(x) for x in parts[:-1]])
+            buf = np.concatenate(parts + [np.full(1, cmfile.DSQ_SENTINEL, np.uint8)])
+            nseq = len(parts)
         if jobs is None:
             jobs = [(a, b) for a in range(nm) for b in range(nseq)]
         jm = np.array([a for a, _ in jobs], np.int32)
@@ -378,10 +396,15 @@ class Scanner:
         hl = self.lib.cmgb_hitlist_create() if want_hits else None
         err = ctypes.create_string_buffer(256)
         try:
-            st = self.lib.cmgb_ScanMulti(self._ctx, harr, nm, cut.ctypes.data, err, BATCH_ALGOS[algo], qdbidx,
-                                         buf.ctypes.data, len(buf), offs.ctypes.data, lens.ctypes.data, nseq,
-                                         jm.ctypes.data, js.ctypes.data, nj, hl, int(do_null3), env_cutoff,
-                                         nh.ctypes.data, ei.ctypes.data, ej.ctypes.data, sc.ctypes.data)
+            if nj == 0:
+                return []
+            if device_buf is not None:
+                fn, ptr, blen = self.lib.cmgb_ScanMulti_dev, device_buf[0], device_buf[1]
+            else:
+                fn, ptr, blen = self.lib.cmgb_ScanMulti, buf.ctypes.data, len(buf)
+            st = fn(self._ctx, harr, nm, cut.ctypes.data, err, BATCH_ALGOS[algo], qdbidx, ptr, blen, offs.ctypes.data,
+                    lens.ctypes.data, nseq, jm.ctypes.data, js.ctypes.data, nj, hl, int(do_null3), env_cutoff,
+                    nh.ctypes.data, ei.ctypes.data, ej.ctypes.data, sc.ctypes.data)
             if st != 0:
                 raise ScanError(st, err.value.decode())
             allhits = []

@@ -1,13 +1,34 @@
 // Test-only host-thread emulation of one CUDA thread block: every CUDA thread
-// is an OS thread, __syncthreads() is a std::barrier, shared memory is a
-// heap buffer.  Included by capi.cu only when CMGB_HOST_EMULATION is defined
-// (the CPU test build in tests/emu); the product never defines it.
+// is an OS thread, __syncthreads() is a barrier, shared memory is a heap
+// buffer.  Included by capi.cu only when CMGB_HOST_EMULATION is defined (the
+// CPU test build in tests/emu); the product never defines it.
 #pragma once
-#include <barrier>
+#include <atomic>
+#include <sched.h>
 #include <thread>
 #include <vector>
 
-inline thread_local std::barrier<> *cmgb_emu_bar = nullptr;
+// A generation-counting barrier that spins briefly and then yields the CPU:
+// the emulated threads outnumber the cores and meet at a barrier every few
+// microseconds, where a futex-based barrier spends its time in the kernel.
+struct EmuBarrier {
+  std::atomic<int> count{0}, gen{0};
+  const int n;
+  explicit EmuBarrier(int n_) : n(n_) {}
+  void arrive_and_wait()
+  {
+    const int g = gen.load(std::memory_order_acquire);
+    if (count.fetch_add(1, std::memory_order_acq_rel) + 1 == n) {
+      count.store(0, std::memory_order_relaxed);
+      gen.fetch_add(1, std::memory_order_release);
+      return;
+    }
+    for (int i = 0; gen.load(std::memory_order_acquire) == g; i++)
+      if (i > 64) sched_yield();
+  }
+};
+
+inline thread_local EmuBarrier *cmgb_emu_bar = nullptr;
 inline void cmgb_emu_sync() { cmgb_emu_bar->arrive_and_wait(); }
 inline unsigned cmgb_emu_maxu(unsigned *p, unsigned v)
 {
@@ -37,7 +58,7 @@ inline unsigned long long cmgb_emu_maxull(unsigned long long *p, unsigned long l
 // warp-level primitives: the 32 threads of an emulated warp meet at a
 // per-warp barrier and exchange values through a slot array
 struct EmuWarp {
-  std::barrier<> bar{32};
+  EmuBarrier bar{32};
   long long slot[32];
 };
 inline thread_local EmuWarp *cmgb_emu_warp = nullptr;

@@ -30,8 +30,14 @@ def _torch_grads(ws, wins, y, posw):
     for l in range(1, 6):
         d = DIL[l]
         a = bf(F.relu(F.conv1d(a, bf(w[l - 1]).permute(1, 2, 0), bias[l], padding=4 * d, dilation=d)))
-    z = a.max(dim=2).values @ wout[:128] + wout[128]
-    loss = F.binary_cross_entropy_with_logits(z, torch.tensor(y), pos_weight=torch.tensor(posw))
+    pooled = a.max(dim=2).values
+    if wout.dim() == 1:                    # one head: labels [B]
+        z = pooled @ wout[:128] + wout[128]
+        loss = F.binary_cross_entropy_with_logits(z, torch.tensor(y), pos_weight=torch.tensor(posw))
+    else:                                  # [H][129]: labels [B][H], a pos weight per head, the heads' losses summed
+        z = pooled @ wout[:, :128].T + wout[:, 128]
+        loss = sum(F.binary_cross_entropy_with_logits(z[:, h], torch.tensor(y[:, h]), pos_weight=torch.tensor(posw[h]))
+                   for h in range(wout.shape[0]))
     loss.backward()
     return float(loss), [t.grad.numpy() for t in (w0, w, bias, wout)]
 
@@ -65,6 +71,61 @@ def test_gradients_match_autograd(gpu):
     for l in range(5):                     # per dilated layer too
         rel = np.linalg.norm(gs[1][l] - ref[1][l]) / max(np.linalg.norm(ref[1][l]), 1e-12)
         assert rel < 0.05, l
+
+
+def test_gradients_match_autograd_heads(gpu):
+    """Three read-out heads on the one-head test's trunk and windows (same
+    trainer seed, so the same arg-max cells), labels and positive weights per
+    head: loss and gradients against PyTorch autograd with the one-head
+    test's tolerances."""
+    W, B, H = 336, 8, 3
+    rng = np.random.default_rng(5)
+    tr = prefilter.NativeTrainer(gpu, W, B, seed=3, heads=H)
+    try:
+        wins = rng.integers(0, 4, (B, 2 * W)).astype(np.uint8)
+        y = np.stack([np.array([1, 0] * (B // 2), np.float32), (rng.random(B) < 0.5).astype(np.float32),
+                      (rng.random(B) < 0.5).astype(np.float32)], axis=1)
+        posw = np.array([3.0, 2.0, 0.5], np.float32)
+        ws = tr.get()
+        assert ws[3].shape == (H, 129)
+        loss, _ = tr.step(wins, y, posw, 0.0)
+        _, gs = tr.get(grads=True)
+    finally:
+        tr.close()
+    ref_loss, ref = _torch_grads(ws, wins, y, posw)
+    assert abs(loss - ref_loss) < 1e-3 * max(1.0, abs(ref_loss))
+    for name, g, r in zip(("w0", "w", "bias", "wout"), gs, ref):
+        rel = np.linalg.norm(g - r) / max(np.linalg.norm(r), 1e-12)
+        print(f"{name}: relative error {rel:.4f}")
+        assert rel < (0.01 if name == "wout" else 0.05), name
+
+
+def test_identical_heads_repeat_the_one_head_network(gpu):
+    """Three identical heads with identical labels and weights: every head's
+    read-out gradient equals the one-head trainer's bit for bit (same
+    forward, same per-window loss gradient), the loss is three times the
+    one-head loss, and the trunk gradients are three times the one-head ones
+    up to the BF16 rounding of the input gradients."""
+    W, B = 128, 8
+    rng = np.random.default_rng(8)
+    wins = rng.integers(0, 4, (B, 2 * W)).astype(np.uint8)
+    y = (rng.random(B) < 0.5).astype(np.float32)
+    t1 = prefilter.NativeTrainer(gpu, W, B, seed=9)
+    t3 = prefilter.NativeTrainer(gpu, W, B, seed=9, heads=3)
+    try:
+        w1 = t1.get()
+        t3.set(w1[0], w1[1], w1[2], np.stack([w1[3]] * 3))
+        l1, _ = t1.step(wins, y, 1.5, 0.0)
+        l3, _ = t3.step(wins, np.repeat(y[:, None], 3, axis=1), 1.5, 0.0)
+        _, g1 = t1.get(grads=True)
+        _, g3 = t3.get(grads=True)
+    finally:
+        t1.close(); t3.close()
+    assert abs(l3 - 3 * l1) <= 1e-5 * abs(3 * l1)
+    for h in range(3):
+        assert np.array_equal(g3[3][h].view(np.uint32), g1[3].view(np.uint32))
+    for a, b in zip(g3[:3], g1[:3]):
+        assert np.linalg.norm(a - 3 * b) <= 0.01 * np.linalg.norm(3 * b)
 
 
 def _motif_batch(rng, B, W, motif):

@@ -91,6 +91,58 @@ def test_multi_equals_batch_gpu(gpu, models, algo, qdb):
     _check(gpu, ms, seqs, sub, algo, qdb, [3.0, 0.0, 5.0])
 
 
+def _overlapping_regions_case(models, rng, n=6000):
+    """One residue buffer of n residues and, per model, its own
+    non-overlapping regions; regions of different models overlap."""
+    body = "".join(rng.choice(list("ACGU"), n))
+    for k, m in enumerate(models):
+        e = emit.sample(m, rng)
+        pos = n // 12 + (3 * n // 10) * k
+        body = body[:pos] + e + body[pos + len(e):]
+    buf = cmfile.digitize(body[:n])
+    spans = []                                  # (model, offset, length)
+    for k in range(len(models)):
+        spans += [(k, 0, 5 * n // 12), (k, 13 * n // 30 + (n // 60) * k, n // 2 - (n // 60) * k)]
+    spans += [(0, n - n // 20, n // 24)]
+    return buf, spans
+
+
+def test_multi_overlapping_regions_emulated(emu, models):
+    """Per-model regions that overlap across models: each candidate goes to
+    the job of its own model; every job equals the model's batch scan of the
+    same region."""
+    ms = [models["tRNA"], models["Vault"]]
+    buf, spans = _overlapping_regions_case(ms, np.random.default_rng(31), n=1200)
+    offs = np.array([o for _, o, _ in spans], np.int64)
+    lens = np.array([n for _, _, n in spans], np.int64)
+    jobs = [(k, q) for q, (k, _, _) in enumerate(spans)]
+    rs = emu.scan_multi(ms, None, jobs=jobs, algo="cyk", qdbidx=1, cutoffs=[0.0, 0.0], env_cutoff=2.0, ranges=(buf, offs, lens))
+    for (k, q), r in zip(jobs, rs):
+        b = emu.scan_batch(ms[k], None, algo="cyk", qdbidx=1, cutoff=0.0, env_cutoff=2.0, ranges=(buf, offs[q:q + 1], lens[q:q + 1]))
+        assert r.hits == b[0].hits and (r.envi, r.envj, r.sc) == (b[0].envi, b[0].envj, b[0].sc)
+    assert sum(len(r.hits) for r in rs) > 0
+
+
+@pytest.mark.gpu
+def test_multi_device_buffer_equals_host_buffer_gpu(gpu, models):
+    """cmgb_ScanMulti_dev (residues already in device memory, NULL3 on) equals
+    cmgb_ScanMulti on the same overlapping per-model regions."""
+    torch = pytest.importorskip("torch")
+    ms = [models["tRNA"], models["Vault"], models["Plant_SRP"]]
+    buf, spans = _overlapping_regions_case(ms, np.random.default_rng(32))
+    offs = np.array([o for _, o, _ in spans], np.int64)
+    lens = np.array([n for _, _, n in spans], np.int64)
+    jobs = [(k, q) for q, (k, _, _) in enumerate(spans)]
+    d = torch.from_numpy(buf).cuda()
+    torch.cuda.synchronize()
+    host = gpu.scan_multi(ms, None, jobs=jobs, algo="cyk", qdbidx=1, cutoffs=[0.0] * 3, env_cutoff=2.0, ranges=(buf, offs, lens))
+    dev = gpu.scan_multi(ms, None, jobs=jobs, algo="cyk", qdbidx=1, cutoffs=[0.0] * 3, env_cutoff=2.0,
+                         ranges=(None, offs, lens), device_buf=(d.data_ptr(), len(buf)))
+    assert [r.hits for r in host] == [r.hits for r in dev]
+    assert [(r.envi, r.envj, r.sc) for r in host] == [(r.envi, r.envj, r.sc) for r in dev]
+    assert sum(len(r.hits) for r in host) > 0
+
+
 @pytest.mark.gpu
 def test_multi_autotuned_shapes_gpu(gpu, models):
     """Models tuned to different tile shapes and placements share a launch."""

@@ -94,6 +94,20 @@ def test_scan_models_equals_per_model_search_emulated(emu):
     assert got == want and got
 
 
+def test_scan_models_both_strands_emulated(emu):
+    """Both strands: the emitted sequence sits on the minus strand, so its hit
+    is found on the reverse complement and mapped back to top-strand
+    coordinates (sfrom > sto), as the per-model search maps it."""
+    from infernal_gb300 import emit
+    ms, targets = _scan_models_case()
+    name, d = targets[0]
+    rc = [(name, emit.revcomp_dsq(d))]
+    got = pipeline.scan_models(emu, ms, rc, E=10.0)
+    want = _per_model(emu, ms, rc, 10.0)
+    assert got == want and got
+    assert any(h.strand == "-" and h.sfrom > h.sto for _, h in got)
+
+
 @pytest.mark.gpu
 def test_scan_models_equals_per_model_search_gpu():
     from infernal_gb300 import emit
