@@ -3,6 +3,8 @@
     python -m infernal_gb300.profile_case <model> <length> <cyk|inside|finside> [tile_rows arena]
     python -m infernal_gb300.profile_case <model> <nreads> <trcyk|trinside> [tile_rows arena]
     python -m infernal_gb300.profile_case <model> <length> filter
+    python -m infernal_gb300.profile_case <model> <length> learned
+
 
 <model> is a configured model under tests/golden (tRNA, Vault, Plant_SRP).
 The standard scanners scan one target of <length> residues; the truncated
@@ -37,7 +39,27 @@ def main(argv):
     if len(argv) > 5:
         sc.set_shape(int(argv[4]), 0, 0, 0, int(argv[5]))
         shape = (int(argv[4]), int(argv[5]))
-    if algo == "filter":
+    if algo == "learned":
+        # the default bench line's step on a <length>-residue target (both
+        # strands): filter, CYK on the kept regions, Inside on survivors
+        import torch
+        from . import prefilter
+        wts = prefilter.load(os.path.join(ROOT, "infernal_gb300", "filters", f"{name}.filter.npz"))
+        f = prefilter.Prefilter(sc, wts, m.W)
+        ins = [emit.sample(m, rng) for _ in range(max(1, L // 80000))]
+        dsq, _ = emit.make_target(rng, L, (0.35, 0.60), ins)
+        buf = prefilter.strand_buffer(dsq)
+        d = torch.from_numpy(buf).cuda()
+        torch.cuda.synchronize()
+        if shape is None:
+            sc.autotune(m, 1, "cyk"); sc.autotune(m, 2, "inside")
+        for _ in range(2):
+            t = time.time()
+            hits, st = prefilter.filtered_scan(sc, f, m, d.data_ptr(), len(buf), prefilter.CYK_CUT, prefilter.INS_CUT)
+            print(f"{name} L={L} learned kernel_ms={st['kernel_ms']} kept={st['kept']} cyk_residues={sum(st['lengths']['cyk'])} "
+                  f"hits={sum(len(x) for x in hits)} wall_s={time.time() - t:.2f}")
+        f.close()
+    elif algo == "filter":
         import torch
         from . import prefilter
         wts = prefilter.load(os.path.join(ROOT, "infernal_gb300", "filters", f"{name}.filter.npz"))
