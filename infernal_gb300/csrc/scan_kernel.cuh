@@ -26,6 +26,7 @@
 // indexing is checked on machines without a GPU.
 #pragma once
 #include <cmath>
+#include <type_traits>
 #include "scan_plan.h"
 
 #ifndef CMGB_HOST_EMULATION
@@ -246,6 +247,51 @@ struct CellWalk {
   CMGB_DEV void next() { d += sdd; r += sr; if (d > hi) { d -= wp; r++; } }
 };
 
+// Column-fixed walk over a phase's cells: with wp <= nt columns, thread tid
+// owns column tid % wp and rows tid / wp + 1, + rs, ... (rs = nt / wp rows
+// per pass; threads past rs * wp idle); wider phases give each thread the
+// columns tid, tid + nt, ... and every row.
+struct ColWalk { int c0, cstep, r0, rs; };
+CMGB_DEV ColWalk col_walk(int wp, int tid, int nt)
+{
+  ColWalk w;
+  if (wp <= nt) {
+    w.rs = nt / wp; w.c0 = tid % wp; w.r0 = tid / wp + 1; w.cstep = wp;
+    if (w.r0 > w.rs) w.c0 = wp;
+  } else { w.rs = 1; w.c0 = tid; w.r0 = 1; w.cstep = nt; }
+  return w;
+}
+
+// Terms a self-loop chain prefetches ahead of its dependent steps.
+#define CMGB_CHUNK 8
+// Rows whose child values a generic-cell loop loads before it computes and
+// stores any of them (the stores would otherwise hold back the next loads).
+#define CMGB_RB 4
+
+// The children terms cv[o] + tv[o] of a non-B cell and its local-end
+// term folded in the order of the reference's per-child-count recurrences
+// (src/cm_dpsearch.c:307-542); WITH0 adds child 0 last (inserts fold their
+// self-loop separately).
+template <class R, int CN, bool WITH0, class T>
+CMGB_DEV T fold_children(const T (&cv)[CMGB_MAXC], const T (&tv)[CMGB_MAXC], T initv, const unsigned short *tbl)
+{
+#define CMGB_CH(o) R::add(cv[o], tv[o])
+  T sc;
+  if (CN == 2) sc = R::comb(CMGB_CH(1), initv, tbl);
+  else if (CN == 3) { sc = R::comb(CMGB_CH(2), CMGB_CH(1), tbl); sc = R::comb(sc, initv, tbl); }
+  else if (CN == 4) { sc = R::comb(CMGB_CH(3), CMGB_CH(2), tbl); sc = R::comb(sc, initv, tbl); sc = R::comb(sc, CMGB_CH(1), tbl); }
+  else if (CN == 5) {
+    sc = R::comb(CMGB_CH(4), CMGB_CH(3), tbl); sc = R::comb(sc, initv, tbl); sc = R::comb(sc, CMGB_CH(1), tbl);
+    sc = R::comb(sc, CMGB_CH(2), tbl);
+  } else {
+    sc = R::comb(CMGB_CH(5), initv, tbl); sc = R::comb(sc, CMGB_CH(4), tbl); sc = R::comb(sc, CMGB_CH(3), tbl);
+    sc = R::comb(sc, CMGB_CH(2), tbl); sc = R::comb(sc, CMGB_CH(1), tbl);
+  }
+  if (WITH0) sc = R::comb(sc, CMGB_CH(0), tbl);
+#undef CMGB_CH
+  return sc;
+}
+
 template <int ALG, bool GL, bool MULTI>
 CMGB_DEV void qdb_scan_body(const KParams &p0, float *smf, int tid, int nt, int bid)
 {
@@ -282,7 +328,6 @@ CMGB_DEV void qdb_scan_body(const KParams &p0, float *smf, int tid, int nt, int 
     T *sm = GL ? reinterpret_cast<T *>(p.arena) + (size_t) bid * P.arena_elems : reinterpret_cast<T *>(smf);
     T *acc = sm + P.acc_off;
     int *bestr = reinterpret_cast<int *>(sm) + P.bestr_off;
-    T *tmp = sm + P.tmp_off;
     unsigned char *res = reinterpret_cast<unsigned char *>(smf + P.res_off);
     int *sdesc = reinterpret_cast<int *>(smf) + P.desc_off;
     T *carry0 = reinterpret_cast<T *>(p.carry) + (size_t) bid * 2 * P.carry_elems;
@@ -352,6 +397,15 @@ CMGB_DEV void qdb_scan_body(const KParams &p0, float *smf, int tid, int nt, int 
       }
       for (int k = tid; k < TT * accw; k += nt) { acc[k] = R::acc_init(); bestr[k] = -1; }
       CMGB_SYNC();
+      // carry row of the phase about to run, held in registers (elements tid
+      // and tid + nt); each phase loads the next phase's while it works, so
+      // no phase starts behind a global-memory read
+      T pre0 = R::imp(), pre1 = R::imp();
+      {
+        const StateInfo &s0i = *reinterpret_cast<const StateInfo *>(sdesc + (int) (g & 1) * slot_words);
+        const int c0 = s0i.carry, w0 = s0i.hi - s0i.lo + 1;
+        if (c0 >= 0) { if (tid < w0) pre0 = cin[c0 + tid]; if (tid + nt < w0) pre1 = cin[c0 + tid + nt]; }
+      }
 
       for (int k = 0; k < NP; k++, g++) {
         // the record of this phase is in slot g&1 (thread 0 saw its copy
@@ -360,17 +414,23 @@ CMGB_DEV void qdb_scan_body(const KParams &p0, float *smf, int tid, int nt, int 
         const StateInfo &si = *reinterpret_cast<const StateInfo *>(sdesc + slot * slot_words);
         const T *esc = reinterpret_cast<const T *>(sdesc + slot * slot_words + P.desc_words);
         if (tid == 0) cmgb_tma_load(sdesc + (slot ^ 1) * slot_words, p.rec + si.next_off, (unsigned) si.next_bytes, mbar + (slot ^ 1));
-        // every descriptor field the phase needs, read once into registers
-        // (shared-memory stores in the loops would otherwise force re-reads)
+        const T cpre0 = pre0, cpre1 = pre1;
+        {
+          const int nc = si.next_carry, nw = si.next_cw;
+          if (nc >= 0) {
+            pre0 = tid < nw ? cin[nc + tid] : R::imp();
+            pre1 = tid + nt < nw ? cin[nc + tid + nt] : R::imp();
+          }
+        }
+        // the descriptor fields every phase kind needs, read once into
+        // registers (shared-memory stores in the loops would otherwise force
+        // re-reads); the branches read their own fields where they start
         const int v = si.v, kind = si.kind, lo = si.lo, hi = si.hi, dn = si.dn, dxW = si.dxW;
         const int cnum = si.cnum, sd = si.sd, emit = si.emit, stride = si.stride, buf = si.buf;
         const int rdo = si.right, has_begin = si.has_begin, carry = si.carry, ringo = si.ring;
         const bool hasend = INS ? (bool) si.has_iend : (bool) si.has_end;
         const float endsc_f = si.endsc;
         const int iendsc_i = si.iendsc;
-        const int banded = si.banded, dn_y = si.dn_y, dx_y = si.dx_y, dn_w = si.dn_w, dx_w = si.dx_w;
-        const int wpa = si.wp_all, sra = si.sr_all, sdda = si.sdd_all, wpb = si.wp_band, srb = si.sr_band, sddb = si.sdd_band;
-        const float inva = si.inv_all, invb = si.inv_band;
         const T beg = R::beginsc(si);
         const T imp = R::imp(), i0v = R::init0(si);
         float vbest = CMGB_IMP;
@@ -379,9 +439,18 @@ CMGB_DEV void qdb_scan_body(const KParams &p0, float *smf, int tid, int nt, int 
 #pragma unroll
         for (int o = 0; o < CMGB_MAXC; o++) { tv[o] = R::tsc(si, o); cb[o] = si.cbuf[o] - si.clo[o]; cs[o] = si.cstr[o]; }
 #define INIT(dd) R::init_h(hasend, endsc_f, iendsc_i, (dd), el, iel)
+        // row 0 of the state's tile buffer: its last row of the previous tile
+#define CMGB_CARRY_IN() do { \
+          const int cw_ = hi - lo + 1; \
+          if (tid < cw_) sm[buf + tid] = cpre0; \
+          if (tid + nt < cw_) sm[buf + tid + nt] = cpre1; \
+          for (int x = tid + 2 * nt; x < cw_; x += nt) sm[buf + x] = cin[carry + x]; \
+        } while (0)
 
         if (kind == SK_ROOT) {
           // ---- root: children fold, local-begin accumulator, candidates ----
+          const int wpb = si.wp_band, srb = si.sr_band, sddb = si.sdd_band;
+          const float invb = si.inv_band;
           for (CellWalk c(tid, dn, dxW, wpb, srb, sddb, invb); c.r <= nrows; c.next()) {
             const int r = c.r, d = c.d, jp = jp0 + r;
             if (d > jp) continue;
@@ -407,96 +476,151 @@ CMGB_DEV void qdb_scan_body(const KParams &p0, float *smf, int tid, int nt, int 
             }
           }
         } else if (kind == SK_IL || kind == SK_IR) {
-          // ---- inserts: (1) every term but the self-loop, all band cells in parallel, into tmp ----
-          for (int x = tid; x < hi - lo + 1; x += nt) sm[buf + x] = cin[carry + x];
+          // the insert scratch sits in shared memory or, for wide models with a
+          // global arena, in the arena; each placement gets its own instance so
+          // every access has a known address space (a generic pointer would
+          // keep the chains' scratch loads behind their global stores)
+          auto insert_phase = [&](T *tmp) {
+            // ---- inserts: (1) every term but the self-loop, all band cells in parallel, into tmp ----
+            CMGB_CARRY_IN();
+  #pragma unroll
+            for (int o = 0; o < CMGB_MAXC; o++) cb[o] -= 1;   // children are read at d-1
+            if (dn <= dxW) {
+              const ColWalk cw = col_walk(dxW - dn + 1, tid, nt);
+              auto terms = [&](auto cn_) {
+                constexpr int CN = decltype(cn_)::value;
+                for (int c = cw.c0; c < dxW - dn + 1; c += cw.cstep) {
+                  const int d = dn + c;
+                  const T initv = INIT(d - 1);
+                  const int rin = d - jp0;       // rows r >= rin hold band cells (d <= jp)
+                  int co[CMGB_MAXC];
+  #pragma unroll
+                  for (int o = 0; o < CMGB_MAXC; o++) co[o] = cb[o] + (cw.r0 - rdo) * cs[o] + d;
+                  int to = cw.r0 * tstr + d - lo;
+                  int cst[CMGB_MAXC];
 #pragma unroll
-          for (int o = 0; o < CMGB_MAXC; o++) cb[o] -= 1;   // children are read at d-1
-          for (CellWalk c(tid, dn, dxW, wpb, srb, sddb, invb); c.r <= nrows; c.next()) {
-            const int r = c.r, d = c.d;
-            if (d > jp0 + r) continue;
-            const int crow = r - rdo;
-            T sc;
-            switch (cnum) {
-#define CH(o) R::add(sm[cb[o] + crow * cs[o] + d], tv[o])
-            case 2: sc = R::comb(CH(1), INIT(d - 1), tbl); break;
-            case 3: sc = R::comb(CH(2), CH(1), tbl); sc = R::comb(sc, INIT(d - 1), tbl); break;
-            case 4: sc = R::comb(CH(3), CH(2), tbl); sc = R::comb(sc, INIT(d - 1), tbl); sc = R::comb(sc, CH(1), tbl); break;
-            case 5: sc = R::comb(CH(4), CH(3), tbl); sc = R::comb(sc, INIT(d - 1), tbl); sc = R::comb(sc, CH(1), tbl);
-                    sc = R::comb(sc, CH(2), tbl); break;
-            default: sc = R::comb(CH(5), INIT(d - 1), tbl); sc = R::comb(sc, CH(4), tbl); sc = R::comb(sc, CH(3), tbl);
-                     sc = R::comb(sc, CH(2), tbl); sc = R::comb(sc, CH(1), tbl); break;
-#undef CH
+                  for (int o = 0; o < CMGB_MAXC; o++) cst[o] = cw.rs * cs[o];
+                  const int tst = cw.rs * tstr;
+                  for (int r = cw.r0; r <= nrows; r += CMGB_RB * cw.rs) {
+                    T cv[CMGB_RB][CMGB_MAXC];
+#pragma unroll
+                    for (int k = 0; k < CMGB_RB; k++) {
+                      const bool lv = r + k * cw.rs <= nrows;
+#pragma unroll
+                      for (int o = 1; o < CMGB_MAXC; o++) if (o < CN) cv[k][o] = lv ? sm[co[o] + k * cst[o]] : imp;
+                      cv[k][0] = imp;
+                    }
+#pragma unroll
+                    for (int k = 0; k < CMGB_RB; k++) {
+                      const int rk = r + k * cw.rs;
+                      if (rk <= nrows && rk >= rin) tmp[to + k * tst] = fold_children<R, CN, false>(cv[k], tv, initv, tbl);
+                    }
+                    to += CMGB_RB * tst;
+#pragma unroll
+                    for (int o = 0; o < CMGB_MAXC; o++) co[o] += CMGB_RB * cst[o];
+                  }
+                }
+              };
+              switch (cnum) {
+                case 2: terms(std::integral_constant<int, 2>()); break;
+                case 3: terms(std::integral_constant<int, 3>()); break;
+                case 4: terms(std::integral_constant<int, 4>()); break;
+                case 5: terms(std::integral_constant<int, 5>()); break;
+                default: terms(std::integral_constant<int, 6>()); break;
+              }
             }
-            tmp[r * tstr + d - lo] = sc;
-          }
-          CMGB_SYNC();
-          // ---- (2) the self-loop chains ----
-          const T tself = tv[0];
-          if (kind == SK_IR) {
-            // IR(r,d) <- IR(r-1,d-1): one thread per diagonal, T short steps
-            const T e0 = 0;
-            (void) e0;
-            const int ndiag = hi - lo + 1 + TT;
-            for (int q = tid; q < ndiag; q += nt) {
-              const int cdg = lo - TT + q;
-              T x = (cdg >= lo && cdg <= hi) ? sm[buf + cdg - lo] : imp;
-              for (int r = 1; r <= nrows; r++) {
-                const int d = cdg + r;
-                if (d < lo || d > hi) { x = imp; continue; }
+            CMGB_SYNC();
+            // ---- (2) the self-loop chains.  Each row (IL) or diagonal (IR)
+            // splits into a pad run, its band run and a pad run, found up front,
+            // so a chain step is only its own recurrence; the scratch terms and
+            // emission scores are prefetched CMGB_CHUNK steps at a time ----
+            const T tself = tv[0];
+            if (kind == SK_IR) {
+              // IR(r,d) <- IR(r-1,d-1): one thread per diagonal cdg = d - r.  Its
+              // cells in [lo, hi] are rows ra..rz; d <= jp holds on a whole
+              // diagonal or on none of it (cdg <= jp0), so its band cells are
+              // one run b0..b1
+              const int ndiag = hi - lo + 1 + TT;
+              const int dstep = stride + 1, tstep = tstr + 1;
+              const int rvs = own_jp - jp0;
+              for (int q = tid; q < ndiag; q += nt) {
+                const int cdg = lo - TT + q;
+                const int ra = lo - cdg > 1 ? lo - cdg : 1, rz = hi - cdg < nrows ? hi - cdg : nrows;
+                if (ra > rz) continue;
+                const int b0 = dn - cdg > ra ? dn - cdg : ra;
+                const int b1 = cdg > jp0 ? ra - 1 : (dxW - cdg < rz ? dxW - cdg : rz);
+                T *out = sm + buf + ra * stride + cdg + ra - lo;
+                if (b0 > b1) {   // no band cell on this diagonal
+                  for (int r = ra; r <= rz; r++, out += dstep) *out = cdg + r == 0 ? i0v : imp;
+                } else {
+                  T x = (ra == 1 && cdg >= lo) ? sm[buf + cdg - lo] : imp;   // the diagonal's row-0 cell
+                  for (int r = ra; r < b0; r++, out += dstep) { x = cdg + r == 0 ? i0v : imp; *out = x; }
+                  for (int r = b0; r <= b1; r += CMGB_CHUNK, out += CMGB_CHUNK * dstep) {
+                    const int n = b1 - r + 1;
+                    const T *tp = tmp + r * tstr + cdg + r - lo;
+                    T tt[CMGB_CHUNK], ee[CMGB_CHUNK];
+#pragma unroll
+                    for (int u = 0; u < CMGB_CHUNK; u++) {
+                      tt[u] = u < n ? tp[u * tstep] : imp;
+                      ee[u] = u < n ? esc[res[W + r + u - 1]] : (T) 0;
+                    }
+#pragma unroll
+                    for (int u = 0; u < CMGB_CHUNK; u++) {
+                      const T nx = R::add(R::comb(tt[u], R::add(x, tself), tbl), ee[u]);
+                      if (u < n) {
+                        x = nx;
+                        out[u * dstep] = x;
+                        if (want_vsc && r + u >= rvs) { const float f = R::score(x); vbest = vbest > f ? vbest : f; }
+                      }
+                    }
+                  }
+                  out = sm + buf + (b1 + 1) * stride + cdg + b1 + 1 - lo;
+                  for (int r = b1 + 1; r <= rz; r++, out += dstep) *out = cdg + r == 0 ? i0v : imp;
+                }
+                // the diagonal's row-TT cell is the next tile's carry
+                if (TT <= nrows && TT >= ra && TT <= rz) cout[carry + cdg + TT - lo] = sm[buf + TT * stride + cdg + TT - lo];
+              }
+            } else {
+              // IL(r,d) <- IL(r,d-1): one thread per row, serial in d over the band
+              for (int r = 1 + tid; r <= nrows; r += nt) {
                 const int jp = jp0 + r;
                 const int dx = jp < dxW ? jp : dxW;
-                T val;
-                if (d < dn || d > dx) val = d == 0 ? i0v : imp;
-                else {
-                  val = R::add(R::comb(tmp[r * tstr + d - lo], R::add(x, tself), tbl), esc[res[W + r - 1]]);
-                  if (want_vsc && jp >= own_jp) { const float f = R::score(val); vbest = vbest > f ? vbest : f; }
-                }
-                sm[buf + r * stride + d - lo] = val;
-                if (r == TT) cout[carry + d - lo] = val;
-                x = val;
-              }
-            }
-          } else {
-            // IL(r,d) <- IL(r,d-1): one warp per row; each lane owns a run of C
-            // consecutive cells; carries cross lanes in rounds until no carry
-            // changes, which reproduces the sequential chain exactly
-            for (int r = 1 + warp; r <= nrows; r += nwarp) {
-              const int jp = jp0 + r;
-              const int dx = jp < dxW ? jp : dxW;
-              T *row = sm + buf + r * stride - lo;
-              const T *trow = tmp + r * tstr - lo;
-              for (int d = lo + lane; d <= hi; d += 32) if (d < dn || d > dx) row[d] = d == 0 ? i0v : imp;
-              const int n = dx - dn + 1;
-              if (n > 0) {
-                const T start = (dn - 1 == 0) ? i0v : imp;   // the cell just before the band
-                const int C = (n + 31) >> 5;
-                const int d0 = dn + lane * C;
-                const int d1 = (d0 + C - 1 < dx) ? d0 + C - 1 : dx;
-                T carry_in = lane == 0 ? start : imp;
-                for (int round = 0; round < 33; round++) {
-                  T x = carry_in;
-                  for (int d = d0; d <= d1; d++) {
-                    x = R::add(R::comb(trow[d], R::add(x, tself), tbl), esc[res[W + r - d]]);
-                    row[d] = x;
+                T *row = sm + buf + r * stride - lo;
+                const T *trow = tmp + r * tstr - lo;
+                const bool last = r == TT;
+                T *crow = cout + carry - lo;
+                const int pad_hi = dn - 1 < hi ? dn - 1 : hi;
+                for (int d = lo; d <= pad_hi; d++) { const T pv = d == 0 ? i0v : imp; row[d] = pv; if (last) crow[d] = pv; }
+                for (int d = (dx + 1 > dn ? dx + 1 : dn); d <= hi; d++) { const T pv = d == 0 ? i0v : imp; row[d] = pv; if (last) crow[d] = pv; }
+                const bool vs = want_vsc && jp >= own_jp;
+                T x = (dn - 1 == 0) ? i0v : imp;   // the cell just before the band
+                for (int d0 = dn; d0 <= dx; d0 += CMGB_CHUNK) {
+                  const int n = dx - d0 + 1;
+                  T tt[CMGB_CHUNK], ee[CMGB_CHUNK];
+#pragma unroll
+                  for (int u = 0; u < CMGB_CHUNK; u++) {
+                    tt[u] = u < n ? trow[d0 + u] : imp;
+                    ee[u] = u < n ? esc[res[W + r - d0 - u]] : (T) 0;
                   }
-                  const T out = (d0 <= d1) ? x : carry_in;
-                  T nc = cmgb_shfl_up(out, 1);
-                  if (lane == 0) nc = start;
-                  const bool changed = (d0 <= d1) && (nc != carry_in);
-                  carry_in = nc;
-                  if (!cmgb_any(changed)) break;
+#pragma unroll
+                  for (int u = 0; u < CMGB_CHUNK; u++) {
+                    const T nx = R::add(R::comb(tt[u], R::add(x, tself), tbl), ee[u]);
+                    if (u < n) {
+                      x = nx;
+                      row[d0 + u] = x;
+                      if (last) crow[d0 + u] = x;
+                      if (vs) { const float f = R::score(x); vbest = vbest > f ? vbest : f; }
+                    }
+                  }
                 }
-                __syncwarp_portable();
-                if (want_vsc && jp >= own_jp)
-                  for (int d = dn + lane; d <= dx; d += 32) { const float f = R::score(row[d]); vbest = vbest > f ? vbest : f; }
               }
-              __syncwarp_portable();
-              if (r == TT) for (int d = lo + lane; d <= hi; d += 32) cout[carry + d - lo] = row[d];
             }
-          }
+          };
+          if (!GL || P.tmp_smem) insert_phase(reinterpret_cast<T *>(smf) + P.tmp_off);
+          else insert_phase(sm + P.tmp_off);
           if (has_begin) {
             CMGB_SYNC();
-            for (CellWalk c(tid, dn, dxW, wpb, srb, sddb, invb); c.r <= nrows; c.next()) {
+            for (CellWalk c(tid, dn, dxW, si.wp_band, si.sr_band, si.sdd_band, si.inv_band); c.r <= nrows; c.next()) {
               const int r = c.r, d = c.d, jp = jp0 + r;
               if (d > jp || d < rdn || d > (jp < rdxW ? jp : rdxW)) continue;
               const T cc = R::add(sm[buf + r * stride + d - lo], beg);
@@ -507,70 +631,95 @@ CMGB_DEV void qdb_scan_body(const KParams &p0, float *smf, int tid, int nt, int 
         } else {
           // ---- generic, BEGL_S and B: all cells of the phase in parallel ----
           const bool begl = kind == SK_BEGL;
-          if (!begl) for (int x = tid; x < hi - lo + 1; x += nt) sm[buf + x] = cin[carry + x];
+          if (!begl) CMGB_CARRY_IN();
 #pragma unroll
           for (int o = 0; o < CMGB_MAXC; o++) cb[o] -= sd;
           if (kind == SK_GEN) {
-            // Two cells per iteration: their child loads and folds are
-            // independent, so each warp keeps two dependency chains in flight.
-            // Both are evaluated at a length clamped into the band (child reads
-            // stay inside the children's buffers); pad cells then take their
-            // constant value.
-            auto gval = [&](int r, int d) -> T {
-              const int crow = r - rdo;
-              T sc;
-#define CH(o) R::add(sm[cb[o] + crow * cs[o] + d], tv[o])
-              switch (cnum) {
-              case 2: sc = R::comb(CH(1), INIT(d - sd), tbl); sc = R::comb(sc, CH(0), tbl); break;
-              case 3: sc = R::comb(CH(2), CH(1), tbl); sc = R::comb(sc, INIT(d - sd), tbl); sc = R::comb(sc, CH(0), tbl); break;
-              case 4: sc = R::comb(CH(3), CH(2), tbl); sc = R::comb(sc, INIT(d - sd), tbl); sc = R::comb(sc, CH(1), tbl);
-                      sc = R::comb(sc, CH(0), tbl); break;
-              case 5: sc = R::comb(CH(4), CH(3), tbl); sc = R::comb(sc, INIT(d - sd), tbl); sc = R::comb(sc, CH(1), tbl);
-                      sc = R::comb(sc, CH(2), tbl); sc = R::comb(sc, CH(0), tbl); break;
-              default: sc = R::comb(CH(5), INIT(d - sd), tbl); sc = R::comb(sc, CH(4), tbl); sc = R::comb(sc, CH(3), tbl);
-                       sc = R::comb(sc, CH(2), tbl); sc = R::comb(sc, CH(1), tbl); sc = R::comb(sc, CH(0), tbl); break;
-              }
-#undef CH
-              if (emit == 3)      sc = R::add(sc, esc[res[W + r - d] * Kp + res[W + r - 1]]);
-              else if (emit == 1) sc = R::add(sc, esc[res[W + r - d]]);
-              else if (emit == 2) sc = R::add(sc, esc[res[W + r - 1]]);
-              return sc;
-            };
-            auto finish = [&](int r, int d, T val, bool in) {
-              const int jp = jp0 + r;
-              if (in) {
-                if (want_vsc && jp >= own_jp) { const float f = R::score(val); vbest = vbest > f ? vbest : f; }
-                if (has_begin && d >= rdn && d <= (jp < rdxW ? jp : rdxW)) {
-                  const T cc = R::add(val, beg);
-                  const int ai = (r - 1) * accw + d - rdn;
-                  if (cc >= acc[ai]) { acc[ai] = cc; bestr[ai] = v; }
+            // Column-fixed walk: a thread owns one column d of [lo, hi] and
+            // every rs-th row, so the band tests, the local-end term and the
+            // local-begin test are per column, and each child's address and
+            // the emission indices advance by a constant per cell.
+            const ColWalk cw = col_walk(hi - lo + 1, tid, nt);
+            auto cells = [&](auto cn_, auto em_) {
+              constexpr int CN = decltype(cn_)::value, EM = decltype(em_)::value;
+              for (int c = cw.c0; c < hi - lo + 1; c += cw.cstep) {
+                const int d = lo + c;
+                const T padv = d == 0 ? i0v : imp;
+                int oo = buf + cw.r0 * stride + c;
+                if (d < dn || d > dxW) {
+                  for (int r = cw.r0; r <= nrows; r += cw.rs, oo += cw.rs * stride) {
+                    sm[oo] = padv;
+                    if (r == TT) cout[carry + c] = padv;
+                  }
+                  continue;
+                }
+                const T initv = INIT(d - sd);
+                const int rin = d - jp0;       // rows r >= rin hold band cells (d <= jp)
+                const int rvs = own_jp - jp0;  // rows r >= rvs are owned by the window
+                const bool bcol = has_begin && d >= rdn && d <= rdxW;
+                int ao = (cw.r0 - 1) * accw + d - rdn;
+                int co[CMGB_MAXC];
+#pragma unroll
+                for (int o = 0; o < CMGB_MAXC; o++) co[o] = cb[o] + (cw.r0 - rdo) * cs[o] + d;
+                int il = W + cw.r0 - d, ir = W + cw.r0 - 1;   // residues i = j-d+1 and j
+                int cst[CMGB_MAXC];
+#pragma unroll
+                for (int o = 0; o < CMGB_MAXC; o++) cst[o] = cw.rs * cs[o];
+                const int ost = cw.rs * stride, ast = cw.rs * accw;
+                for (int r = cw.r0; r <= nrows; r += CMGB_RB * cw.rs) {
+                  T cv[CMGB_RB][CMGB_MAXC], av[CMGB_RB];
+#pragma unroll
+                  for (int k = 0; k < CMGB_RB; k++) {
+                    const bool lv = r + k * cw.rs <= nrows;
+#pragma unroll
+                    for (int o = 0; o < CMGB_MAXC; o++) if (o < CN) cv[k][o] = lv ? sm[co[o] + k * cst[o]] : imp;
+                    av[k] = (lv && bcol) ? acc[ao + k * ast] : imp;
+                  }
+#pragma unroll
+                  for (int k = 0; k < CMGB_RB; k++) {
+                    const int rk = r + k * cw.rs;
+                    if (rk <= nrows) {
+                      T val = fold_children<R, CN, true>(cv[k], tv, initv, tbl);
+                      const int ilk = il + k * cw.rs, irk = ir + k * cw.rs;
+                      if (EM == 3) val = R::add(val, esc[res[ilk] * Kp + res[irk]]);
+                      else if (EM == 1) val = R::add(val, esc[res[ilk]]);
+                      else if (EM == 2) val = R::add(val, esc[res[irk]]);
+                      if (rk < rin) val = padv;
+                      else {
+                        if (want_vsc && rk >= rvs) { const float f = R::score(val); vbest = vbest > f ? vbest : f; }
+                        if (bcol) {
+                          const T cc = R::add(val, beg);
+                          if (cc >= av[k]) { acc[ao + k * ast] = cc; bestr[ao + k * ast] = v; }
+                        }
+                      }
+                      sm[oo + k * ost] = val;
+                      if (rk == TT) cout[carry + c] = val;
+                    }
+                  }
+                  oo += CMGB_RB * ost; ao += CMGB_RB * ast; il += CMGB_RB * cw.rs; ir += CMGB_RB * cw.rs;
+#pragma unroll
+                  for (int o = 0; o < CMGB_MAXC; o++) co[o] += CMGB_RB * cst[o];
                 }
               }
-              sm[buf + r * stride + d - lo] = val;
-              if (r == TT) cout[carry + d - lo] = val;
             };
-            const bool band_ok = dn <= dxW;   // uniform: an empty band has only pad cells
-            CellWalk c(tid, lo, hi, wpa, sra, sdda, inva);
-            while (c.r <= nrows) {
-              CellWalk c2 = c; c2.next();
-              const bool two = c2.r <= nrows;
-              const int r1 = c.r, d1 = c.d, r2 = two ? c2.r : c.r, d2 = two ? c2.d : c.d;
-              const int dx1 = jp0 + r1 < dxW ? jp0 + r1 : dxW, dx2 = jp0 + r2 < dxW ? jp0 + r2 : dxW;
-              const bool in1 = d1 >= dn && d1 <= dx1, in2 = d2 >= dn && d2 <= dx2;
-              T v1 = d1 == 0 ? i0v : imp, v2 = d2 == 0 ? i0v : imp;
-              if (band_ok) {
-                const int e1 = d1 < dn ? dn : (d1 > dxW ? dxW : d1), e2 = d2 < dn ? dn : (d2 > dxW ? dxW : d2);
-                const T g1 = gval(r1, e1), g2 = gval(r2, e2);
-                if (in1) v1 = g1;
-                if (in2) v2 = g2;
-              }
-              finish(r1, d1, v1, in1);
-              if (two) finish(r2, d2, v2, in2);
-              c = c2;
-              if (two) c.next();
+#define CMGB_EMIT_CASES(CNV) \
+            switch (emit) { \
+              case 0: cells(std::integral_constant<int, CNV>(), std::integral_constant<int, 0>()); break; \
+              case 1: cells(std::integral_constant<int, CNV>(), std::integral_constant<int, 1>()); break; \
+              case 2: cells(std::integral_constant<int, CNV>(), std::integral_constant<int, 2>()); break; \
+              default: cells(std::integral_constant<int, CNV>(), std::integral_constant<int, 3>()); break; \
             }
-          } else
-          for (CellWalk c(tid, lo, hi, wpa, sra, sdda, inva); c.r <= nrows; c.next()) {
+            switch (cnum) {
+              case 2: CMGB_EMIT_CASES(2) break;
+              case 3: CMGB_EMIT_CASES(3) break;
+              case 4: CMGB_EMIT_CASES(4) break;
+              case 5: CMGB_EMIT_CASES(5) break;
+              default: CMGB_EMIT_CASES(6) break;
+            }
+#undef CMGB_EMIT_CASES
+          } else {
+          const int banded = si.banded, dn_y = si.dn_y, dx_y = si.dx_y, dn_w = si.dn_w, dx_w = si.dx_w;
+          for (CellWalk c(tid, lo, hi, si.wp_all, si.sr_all, si.sdd_all, si.inv_all); c.r <= nrows; c.next()) {
             const int r = c.r, d = c.d, jp = jp0 + r;
             const int dx = jp < dxW ? jp : dxW;
             int rrow = ringj + r; if (rrow >= RR) rrow -= RR;   // ring row of this jp
@@ -606,29 +755,10 @@ CMGB_DEV void qdb_scan_body(const KParams &p0, float *smf, int tid, int nt, int 
                   val = R::comb(val, R::add(wring[rr * wstr - kk], yrow[kk]), tbl);
                   rr = rr == 0 ? RR - 1 : rr - 1;
                 }
-              } else if (begl) {
+              } else {   // BEGL_S
                 val = INIT(d);
 #pragma unroll
                 for (int o = 0; o < CMGB_MAXC; o++) if (o < cnum) val = R::comb(val, R::add(sm[cb[o] + r * cs[o] + d], tv[o]), tbl);
-              } else {
-                const int crow = r - rdo;
-                T sc;
-                switch (cnum) {
-#define CH(o) R::add(sm[cb[o] + crow * cs[o] + d], tv[o])
-                case 2: sc = R::comb(CH(1), INIT(d - sd), tbl); sc = R::comb(sc, CH(0), tbl); break;
-                case 3: sc = R::comb(CH(2), CH(1), tbl); sc = R::comb(sc, INIT(d - sd), tbl); sc = R::comb(sc, CH(0), tbl); break;
-                case 4: sc = R::comb(CH(3), CH(2), tbl); sc = R::comb(sc, INIT(d - sd), tbl); sc = R::comb(sc, CH(1), tbl);
-                        sc = R::comb(sc, CH(0), tbl); break;
-                case 5: sc = R::comb(CH(4), CH(3), tbl); sc = R::comb(sc, INIT(d - sd), tbl); sc = R::comb(sc, CH(1), tbl);
-                        sc = R::comb(sc, CH(2), tbl); sc = R::comb(sc, CH(0), tbl); break;
-                default: sc = R::comb(CH(5), INIT(d - sd), tbl); sc = R::comb(sc, CH(4), tbl); sc = R::comb(sc, CH(3), tbl);
-                         sc = R::comb(sc, CH(2), tbl); sc = R::comb(sc, CH(1), tbl); sc = R::comb(sc, CH(0), tbl); break;
-#undef CH
-                }
-                if (emit == 3)      sc = R::add(sc, esc[res[W + r - d] * Kp + res[W + r - 1]]);
-                else if (emit == 1) sc = R::add(sc, esc[res[W + r - d]]);
-                else if (emit == 2) sc = R::add(sc, esc[res[W + r - 1]]);
-                val = sc;
               }
               if (want_vsc && jp >= own_jp) { const float f = R::score(val); vbest = vbest > f ? vbest : f; }
               if (has_begin && d >= rdn && d <= (jp < rdxW ? jp : rdxW)) {
@@ -643,8 +773,10 @@ CMGB_DEV void qdb_scan_body(const KParams &p0, float *smf, int tid, int nt, int 
               if (r == TT) cout[carry + d - lo] = val;
             }
           }
+          }
         }
 #undef INIT
+#undef CMGB_CARRY_IN
         if (want_vsc && vbest > CMGB_IMP) CMGB_ATOMIC_MAXU(p.vsc + v, cmgb_f2u(vbest));
         if (tid == 0) {   // next phase's record, issued at the top of this phase
           const int ns = slot ^ 1;
@@ -666,11 +798,11 @@ CMGB_DEV void qdb_scan_body(const KParams &p0, float *smf, int tid, int nt, int 
 }
 
 #ifndef CMGB_HOST_EMULATION
-// CYK fits 64 registers without spilling, so two 512-thread CTAs (or four of
-// 256) share an SM and hide each other's barrier and dependency stalls; the
-// Inside kernels keep 128 registers (they spill below that).
+// One 512-thread CTA per SM with up to 128 registers: the generic-cell loops
+// keep four rows of child values in flight per thread, which a 64-register
+// budget (two CTAs per SM) would spill.
 template <int ALG, bool GL, bool MULTI>
-__global__ void __launch_bounds__(512, (ALG == 0 && !MULTI) ? 2 : 1) qdb_scan_kernel(KParams p)
+__global__ void __launch_bounds__(512, 1) qdb_scan_kernel(KParams p)
 {
   extern __shared__ __align__(128) float smem_dyn[];
   qdb_scan_body<ALG, GL, MULTI>(p, smem_dyn, threadIdx.x, blockDim.x, blockIdx.x);

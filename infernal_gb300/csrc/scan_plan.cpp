@@ -188,13 +188,20 @@ bool build_plan(const cmgb_model_desc *m, int qdbidx, int T, int nthreads, bool 
   P.acc_w = std::max(1, S[0].dxW - S[0].dn + 1);
   P.acc_off = off; off += T * P.acc_w;
   P.bestr_off = off; off += T * P.acc_w;
-  P.tmp_off = off; P.tmp_stride = tmp_stride; off += (T + 1) * tmp_stride;
+  P.tmp_stride = tmp_stride;
+  const int tmp_elems = (T + 1) * tmp_stride;
+  // the insert scratch is read back by the self-loop chains right after it is
+  // written; with a global arena it still goes to shared memory when it fits
+  // next to a second CTA on the SM
+  P.tmp_smem = !arena_global || tmp_elems * 4 <= 96 * 1024;
+  if (!P.tmp_smem) { P.tmp_off = off; off += tmp_elems; }
   off = (off + 3) & ~3;
   P.arena_global = arena_global ? 1 : 0;
   if (arena_global) {            // everything above goes to global memory; shared memory restarts at 0
     P.arena_elems = off;
     off = 0;
   } else P.arena_elems = 0;
+  if (P.tmp_smem) { P.tmp_off = off; off += tmp_elems; off = (off + 3) & ~3; }
   P.desc_words = (int) (sizeof(StateInfo) / 4);
   P.rec_max_bytes = (int) sizeof(StateInfo) + ((m->Kp * m->Kp * 4 + 15) & ~15);
   P.desc_off = off; off += 2 * (P.rec_max_bytes / 4);     // two record slots, 16-byte aligned
@@ -231,6 +238,11 @@ bool build_plan(const cmgb_model_desc *m, int qdbidx, int T, int nthreads, bool 
     q.inv_all = 1.0f / (float) q.wp_all; q.inv_band = 1.0f / (float) q.wp_band;
   }
   for (int v = M - 1; v >= 0; v--) if (S[v].kind != SK_E) { out->phases.push_back(S[v]); P.nphase++; }
+  for (size_t k = 0; k < out->phases.size(); k++) {
+    const bool nx = k + 1 < out->phases.size() && out->phases[k + 1].carry >= 0;
+    out->phases[k].next_carry = nx ? out->phases[k + 1].carry : -1;
+    out->phases[k].next_cw = nx ? out->phases[k + 1].hi - out->phases[k + 1].lo + 1 : 0;
+  }
   out->plan = P;
   out->states = std::move(S);
   return true;
@@ -454,6 +466,7 @@ bool build_tr_plan(const cmgb_model_desc *m, int qdbidx, int T, int nthreads, bo
   }
   for (int v = M - 1; v >= 0; v--)
     if (S[v].s.kind != SK_E && S[v].s.kind != SK_DET) { out->phases.push_back(S[v]); P.nphase++; }
+  for (auto &ph : out->phases) { ph.s.next_carry = -1; ph.s.next_cw = 0; }
   out->plan = P;
   out->states = std::move(S);
   return true;

@@ -38,7 +38,8 @@ struct StateInfo {
   // and band [dn,dxW]: width, step in rows / columns per nt cells
   int     wp_all, sr_all, sdd_all, wp_band, sr_band, sdd_band;
   float   inv_all, inv_band;    // 1/width, for the first row/column split
-  int     pad3_[2];
+  int     next_carry, next_cw;  // carry row (offset, width) of the next phase in sweep order, -1: none;
+                                // the kernel prefetches it one phase ahead
   int     lo, hi;    // padded d range of the buffer
   int     dn, dxW;   // own band for j >= W (dx shrinks to jp for small jp)
   int     buf;       // shared-memory element offset of row 0 (E: constant row)
@@ -95,7 +96,8 @@ struct ScanPlan {
   int rec_max_bytes;      // largest phase record (descriptor + emission row)
   int rec0_bytes;         // size of phase 0's record
   int esc_off;            // element offset of the two prefetched emission rows (Kp*Kp each)
-  int tmp_off;            // element offset of the insert-state scratch [(T+1) x tmp_stride]
+  int tmp_off;            // element offset of the insert-state scratch [(T+1) x tmp_stride], in the
+                          // tile arena or, when tmp_smem, in shared memory
   int tmp_stride;
   int acc_w;              // root accumulator width (root band)
   int ltbl_off;           // element offset of the uint16 ILogsum table (integer Inside plans only)
@@ -122,6 +124,7 @@ struct ScanPlan {
   // truncated scans only
   int imp_row;            // element offset of an all-IMPOSSIBLE constant row (detached states)
   int rmax_off;           // element offset of the root's running maxima [4 modes][2 parities][acc_w]
+  int tmp_smem;           // standard scans: the insert scratch lives in shared memory
 };
 
 #ifndef CMGB_NO_HOST_PLAN
