@@ -370,6 +370,7 @@ def run_pipeline(args, rank, world):
         "e2e": {"value": round(res * world / t_e2e / 1e6, 3), "unit": "Mres/s",
                 "h2d_bytes_per_step": int(h2d / args.steps), "d2h_bytes_per_step": int(d2h / args.steps)},
         "kernel_ms_per_step": {k: round(v / args.steps, 3) for k, v in kms.items()},
+        "stage_wall_ms_per_step": {k: round(sum(st["wall_ms"][k] for st in sts) / args.steps, 3) for k in ("filter", "cyk", "inside")},
         "fraction_scanned": round(sum(st["kept"] for st in sts) / res, 4),
         "gpu_launches": launches,
         "tuned_shapes": {k: {"tile_rows": v[0], "arena": "global" if v[1] == 2 else "shared"} for k, v in tuned.items()},

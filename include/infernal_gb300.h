@@ -162,7 +162,7 @@ void cmgb_logsum_init(void);
 int  cmgb_ctx_create(int device, cmgb_ctx **ret_ctx, char *errbuf);
 void cmgb_ctx_destroy(cmgb_ctx *ctx);
 /* Kernel launch shape override; 0 keeps the default of each field.
- * tile_rows: end positions per tile (the rolling-row depth, <= 64);
+ * tile_rows: end positions per tile (the rolling-row depth, <= 128);
  * window_len: owned end positions per CTA work item; ctas_per_sm: resident
  * CTAs per SM (0: as many as fit); threads: threads per CTA (64..512);
  * arena: where the DP tiles live (0 automatic, 1 shared memory, 2 a per-CTA

@@ -303,7 +303,7 @@ extern "C" int cmgb_ctx_set_shape(cmgb_ctx *c, int tile_rows, int window_len, in
   if (!c) return CMGB_EINVAL;
   if (arena < 0 || arena > 2) return CMGB_EINVAL;
   c->arena = arena;
-  if (tile_rows < 0 || tile_rows > 64 || window_len < 0 || ctas_per_sm < 0 || ctas_per_sm > 8) return CMGB_EINVAL;
+  if (tile_rows < 0 || tile_rows > 128 || window_len < 0 || ctas_per_sm < 0 || ctas_per_sm > 8) return CMGB_EINVAL;
   if (threads != 0 && (threads < 64 || threads > 512 || threads % 32)) return CMGB_EINVAL;
   c->tile_rows = tile_rows;
   c->window_len = window_len;
@@ -344,9 +344,17 @@ extern "C" int cmgb_model_create(cmgb_ctx *c, const cmgb_model_desc *d, cmgb_mod
   m->tsc.assign(d->tsc, d->tsc + 6 * M); m->itsc.assign(d->itsc, d->itsc + 6 * M);
   m->endsc.assign(d->endsc, d->endsc + M); m->beginsc.assign(d->beginsc, d->beginsc + M);
   m->iendsc.assign(d->iendsc, d->iendsc + M); m->ibeginsc.assign(d->ibeginsc, d->ibeginsc + M);
-  m->el_selfsc = d->el_selfsc; m->iel_selfsc = d->iel_selfsc;
+  m->el_selfsc = d->el_selfsc == 0.0f ? 0.0f : d->el_selfsc; m->iel_selfsc = d->iel_selfsc;
   m->oesc.assign(d->oesc, d->oesc + (size_t) M * KK);
   m->ioesc.assign(d->ioesc, d->ioesc + (size_t) M * KK);
+  // The CYK kernels take maxima with the max instruction, which orders -0.0
+  // below +0.0 where ESL_MAX keeps its second operand; DP values can be -0.0
+  // only through -0.0 table entries, so those (configured log2-odds tables
+  // hold none) are stored as +0.0: the same values, and the kernels' maxima
+  // then equal ESL_MAX bit for bit
+  auto no_neg_zero = [](std::vector<float> &v) { for (float &x : v) if (x == 0.0f) x = 0.0f; };
+  no_neg_zero(m->tsc); no_neg_zero(m->endsc); no_neg_zero(m->beginsc); no_neg_zero(m->oesc);
+  const float el_sc = d->el_selfsc == 0.0f ? 0.0f : d->el_selfsc;
   std::memset(&m->desc, 0, sizeof(m->desc));
   cmgb_model_desc &D = m->desc;
   D.M = M; D.W = d->W; D.K = d->K; D.Kp = d->Kp; D.flags = d->flags;
@@ -355,14 +363,14 @@ extern "C" int cmgb_model_create(cmgb_ctx *c, const cmgb_model_desc *d, cmgb_mod
   D.dmin2 = m->dmin2.empty() ? nullptr : m->dmin2.data(); D.dmax2 = m->dmax2.empty() ? nullptr : m->dmax2.data();
   D.tsc = m->tsc.data(); D.itsc = m->itsc.data(); D.endsc = m->endsc.data(); D.beginsc = m->beginsc.data();
   D.iendsc = m->iendsc.data(); D.ibeginsc = m->ibeginsc.data();
-  D.el_selfsc = d->el_selfsc; D.iel_selfsc = d->iel_selfsc;
+  D.el_selfsc = el_sc; D.iel_selfsc = d->iel_selfsc;
   D.null = m->null.data(); D.null3_omega = d->null3_omega;
   D.oesc = m->oesc.data(); D.ioesc = m->ioesc.data();
   if (cudaSetDevice(c->device) != cudaSuccess) ERRF(CMGB_ENODEV, "cudaSetDevice failed");
   if (cudaMalloc(&m->d_oesc, sizeof(float) * (size_t) M * KK) != cudaSuccess ||
       cudaMalloc(&m->d_ioesc, sizeof(int) * (size_t) M * KK) != cudaSuccess)
     ERRF(CMGB_EMEM, "out of device memory for emission tables");
-  CUDA_TRY(cudaMemcpy(m->d_oesc, d->oesc, sizeof(float) * (size_t) M * KK, cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(m->d_oesc, m->oesc.data(), sizeof(float) * (size_t) M * KK, cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMemcpy(m->d_ioesc, d->ioesc, sizeof(int) * (size_t) M * KK, cudaMemcpyHostToDevice));
   // truncated scanning tables (cm->lmesc/rmesc, cm->trp, cm->emap), when given
   if (d->lmesc && d->rmesc && d->ilmesc && d->irmesc && d->tr_g_pty && d->tr_l_pty && d->tr_ig_pty && d->tr_il_pty &&
@@ -371,6 +379,7 @@ extern "C" int cmgb_model_create(cmgb_ctx *c, const cmgb_model_desc *d, cmgb_mod
     m->lmesc.assign(d->lmesc, d->lmesc + MK); m->rmesc.assign(d->rmesc, d->rmesc + MK);
     m->ilmesc.assign(d->ilmesc, d->ilmesc + MK); m->irmesc.assign(d->irmesc, d->irmesc + MK);
     m->tr_g.assign(d->tr_g_pty, d->tr_g_pty + 3 * M); m->tr_l.assign(d->tr_l_pty, d->tr_l_pty + 3 * M);
+    no_neg_zero(m->lmesc); no_neg_zero(m->rmesc); no_neg_zero(m->tr_g); no_neg_zero(m->tr_l);
     m->tr_ig.assign(d->tr_ig_pty, d->tr_ig_pty + 3 * M); m->tr_il.assign(d->tr_il_pty, d->tr_il_pty + 3 * M);
     m->ndidx.assign(d->ndidx, d->ndidx + M);
     m->nodes = d->nodes; m->clen = d->clen;
@@ -383,8 +392,8 @@ extern "C" int cmgb_model_create(cmgb_ctx *c, const cmgb_model_desc *d, cmgb_mod
     if (cudaMalloc(&m->d_lmesc, sizeof(float) * MK) != cudaSuccess || cudaMalloc(&m->d_rmesc, sizeof(float) * MK) != cudaSuccess ||
         cudaMalloc(&m->d_ilmesc, sizeof(int) * MK) != cudaSuccess || cudaMalloc(&m->d_irmesc, sizeof(int) * MK) != cudaSuccess)
       ERRF(CMGB_EMEM, "out of device memory for marginal emission tables");
-    CUDA_TRY(cudaMemcpy(m->d_lmesc, d->lmesc, sizeof(float) * MK, cudaMemcpyHostToDevice));
-    CUDA_TRY(cudaMemcpy(m->d_rmesc, d->rmesc, sizeof(float) * MK, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(m->d_lmesc, m->lmesc.data(), sizeof(float) * MK, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(m->d_rmesc, m->rmesc.data(), sizeof(float) * MK, cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(m->d_ilmesc, d->ilmesc, sizeof(int) * MK, cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemcpy(m->d_irmesc, d->irmesc, sizeof(int) * MK, cudaMemcpyHostToDevice));
     m->has_tr = true;
@@ -423,8 +432,9 @@ static int get_plan(cmgb_model *m, int qdbidx, int alg, DevPlan **ret, char *err
   if ((qdbidx == 1 && m->dmin1.empty()) || (qdbidx == 2 && m->dmin2.empty()))
     ERRF(CMGB_EINCOMPAT, "the model was created without band set %d (qdbidx %d)", qdbidx, qdbidx);
   DevPlan &dp = m->plans[qdbidx][alg];
-  // shape: the context's explicit choice, else the autotuner's, else 16 rows in shared memory
-  const int wantT = c->tile_rows ? c->tile_rows : (m->tuned_T[qdbidx][alg] ? m->tuned_T[qdbidx][alg] : 16);
+  // shape: the context's explicit choice, else the autotuner's, else 96 rows
+  // (in global memory unless the context asks for shared)
+  const int wantT = c->tile_rows ? c->tile_rows : (m->tuned_T[qdbidx][alg] ? m->tuned_T[qdbidx][alg] : 96);
   const int wantA = c->tile_rows ? c->arena : (m->tuned_T[qdbidx][alg] ? m->tuned_arena[qdbidx][alg] : c->arena);
   if (dp.built && dp.T == wantT && dp.nt == c->threads && dp.arena == wantA) { *ret = &dp; return CMGB_OK; }
   if (dp.d_states) { cudaFree(dp.d_states); dp.d_states = nullptr; }
@@ -1208,25 +1218,33 @@ static int scan_batch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo, int qd
     }
   }
   const uint8_t *hseq = d_seqs ? (hres.empty() ? nullptr : hres.data()) : seqs;
+  // the sequences' hit lists are independent: resolve them on host threads,
+  // then append them in sequence order
+  std::vector<std::vector<cmgb_hit>> outq(hitlist ? nseq : 0);
+  if (hitlist) {
+    logsum_tables(nullptr, nullptr);
+    TruncFilter tf;
+    if (tr) {
+      tf.pass_idx = pass_idx; tf.local = (m->flags & CMGB_LOCAL_BEGIN) ? 1 : 0; tf.clen = m->clen;
+      tf.ndidx = m->ndidx.data(); tf.ndtype = m->ndtype.data(); tf.lpos = m->emap_lpos.data(); tf.rpos = m->emap_rpos.data();
+    }
+    parallel_for(nseq, [&](int q) {
+      if (per[q].empty()) return;
+      const int64_t off = offsets[q];
+      ResolveArgs ra;
+      ra.null = m->null.data(); ra.K = m->K; ra.null3_omega = m->null3_omega; ra.do_null3 = do_null3;
+      ra.greedy = greedy ? 1 : 0; ra.cutoff = cutoff; ra.i0 = off + 1; ra.j0 = off + lengths[q]; ra.dsq = hseq;
+      if (tr) ra.tr = &tf;
+      resolve_hits(per[q], ra, outq[q]);
+      for (cmgb_hit &h : outq[q]) { h.start -= off; h.stop -= off; }
+    });
+  }
   for (int q = 0; q < nseq; q++) {
     const int64_t off = offsets[q];
     if (ret_envi) ret_envi[q] = envj[q] < off + 1 ? -1 : envi[q] - off;
     if (ret_envj) ret_envj[q] = envj[q] < off + 1 ? -1 : envj[q] - off;
-    int64_t before = hitlist ? (int64_t) hitlist->h.size() : 0;
-    if (hitlist && !per[q].empty()) {
-      TruncFilter tf;
-      ResolveArgs ra;
-      ra.null = m->null.data(); ra.K = m->K; ra.null3_omega = m->null3_omega; ra.do_null3 = do_null3;
-      ra.greedy = greedy ? 1 : 0; ra.cutoff = cutoff; ra.i0 = off + 1; ra.j0 = off + lengths[q]; ra.dsq = hseq;
-      if (tr) {
-        tf.pass_idx = pass_idx; tf.local = (m->flags & CMGB_LOCAL_BEGIN) ? 1 : 0; tf.clen = m->clen;
-        tf.ndidx = m->ndidx.data(); tf.ndtype = m->ndtype.data(); tf.lpos = m->emap_lpos.data(); tf.rpos = m->emap_rpos.data();
-        ra.tr = &tf;
-      }
-      resolve_hits(per[q], ra, hitlist->h);
-      for (size_t k = (size_t) before; k < hitlist->h.size(); k++) { hitlist->h[k].start -= off; hitlist->h[k].stop -= off; }
-    }
-    if (ret_nhits) ret_nhits[q] = hitlist ? (int64_t) hitlist->h.size() - before : 0;
+    if (hitlist) hitlist->h.insert(hitlist->h.end(), outq[q].begin(), outq[q].end());
+    if (ret_nhits) ret_nhits[q] = hitlist ? (int64_t) outq[q].size() : 0;
   }
   return CMGB_OK;
 }
@@ -1501,23 +1519,32 @@ static int scan_multi(cmgb_ctx *c, cmgb_model *const *models, int nmodels, const
   c->last_launches = launches;
   c->last_h2d = h2d; c->last_d2h = d2h;
   auto u2f = [](unsigned u) { if (u == 0) return CMGB_IMPOSSIBLE; unsigned b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u; float f; std::memcpy(&f, &b, 4); return f; };
+  // the jobs' hit lists are independent: resolve them on host threads, then
+  // append them in job order
+  std::vector<std::vector<cmgb_hit>> outk(hitlist ? njobs : 0);
+  if (hitlist) {
+    logsum_tables(nullptr, nullptr);
+    parallel_for(njobs, [&](int k) {
+      if (per[k].empty()) return;
+      const int q = job_seq[k];
+      cmgb_model *mk = models[job_model[k]];
+      const int64_t off = offsets[q];
+      ResolveArgs ra;
+      ra.null = mk->null.data(); ra.K = mk->K; ra.null3_omega = mk->null3_omega; ra.do_null3 = do_null3;
+      ra.greedy = (mk->flags & CMGB_NOTGREEDY) ? 0 : 1; ra.cutoff = cutoffs[job_model[k]];
+      ra.i0 = off + 1; ra.j0 = off + lengths[q]; ra.dsq = hseq;
+      resolve_hits(per[k], ra, outk[k]);
+      for (cmgb_hit &h : outk[k]) { h.start -= off; h.stop -= off; }
+    });
+  }
   for (int k = 0; k < njobs; k++) {
     const int q = job_seq[k];
-    cmgb_model *m = models[job_model[k]];
     const int64_t off = offsets[q];
     if (ret_sc) ret_sc[k] = u2f(bestj[k]);
     if (ret_envi) ret_envi[k] = envj[k] < off + 1 ? -1 : envi[k] - off;
     if (ret_envj) ret_envj[k] = envj[k] < off + 1 ? -1 : envj[k] - off;
-    const int64_t before = hitlist ? (int64_t) hitlist->h.size() : 0;
-    if (hitlist && !per[k].empty()) {
-      ResolveArgs ra;
-      ra.null = m->null.data(); ra.K = m->K; ra.null3_omega = m->null3_omega; ra.do_null3 = do_null3;
-      ra.greedy = (m->flags & CMGB_NOTGREEDY) ? 0 : 1; ra.cutoff = cutoffs[job_model[k]];
-      ra.i0 = off + 1; ra.j0 = off + lengths[q]; ra.dsq = hseq;
-      resolve_hits(per[k], ra, hitlist->h);
-      for (size_t x = (size_t) before; x < hitlist->h.size(); x++) { hitlist->h[x].start -= off; hitlist->h[x].stop -= off; }
-    }
-    if (ret_nhits) ret_nhits[k] = hitlist ? (int64_t) hitlist->h.size() - before : 0;
+    if (hitlist) hitlist->h.insert(hitlist->h.end(), outk[k].begin(), outk[k].end());
+    if (ret_nhits) ret_nhits[k] = hitlist ? (int64_t) outk[k].size() : 0;
   }
   return CMGB_OK;
 }
@@ -1540,7 +1567,7 @@ extern "C" int cmgb_autotune(cmgb_ctx *c, cmgb_model *m, int qdbidx, int algo, i
     dsq[i] = u < 30 ? 0 : u < 50 ? 1 : u < 70 ? 2 : 3;
   }
   dsq[0] = dsq[sample_len + 1] = 255;
-  static const int cand[][2] = {{16, 1}, {8, 1}, {32, 2}, {48, 2}, {64, 2}};
+  static const int cand[][2] = {{16, 1}, {32, 2}, {48, 2}, {64, 2}, {96, 2}, {128, 2}};
   const int saveT = c->tile_rows, saveA = c->arena;
   float best_ms = 3.0e38f; int bT = 16, bA = 1;
   int st = CMGB_OK;

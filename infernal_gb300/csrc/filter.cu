@@ -93,16 +93,28 @@ __global__ void filter_layer0(const unsigned char *dsq, long long i0, long long 
 }
 
 // ---- layers 1-5 on tcgen05 ------------------------------------------------
-// One CTA (4 warps) computes a 128-position x 128-channel tile with
-// tcgen05.mma (cta_group::1, kind::f16, BF16 x BF16 -> FP32, M = N = 128,
-// K = 16 per instruction) accumulating in 128 TMEM columns.  Operands sit in
-// shared memory in the K-major, non-swizzled canonical layout: 8-row x
-// 16-byte core matrices, chunk c (8 input channels) of row r at
-// (c * rows + r) * 16 bytes, so a tap's shift by (t * dil) rows is a 16-byte
-// multiple of the start address.  Descriptors: leading (K) byte offset =
-// one chunk plane, stride (M/N) byte offset = 128 bytes between 8-row core
-// matrices.  Thread 0 issues the 8 MMAs of a tap and commits them to an
-// mbarrier; every wait is bounded and sets *err on expiry.
+// One CTA (4 warps) computes up to TPC 128-position tiles of one window
+// against all 128 output channels with tcgen05.mma (cta_group::1, kind::f16,
+// BF16 x BF16 -> FP32, M = N = 128, K = 16 per instruction), one TMEM
+// accumulator of 128 columns per tile.  Operands sit in shared memory in the
+// K-major, non-swizzled canonical layout: 8-row x 16-byte core matrices,
+// chunk c (8 input channels) of row r at (c * rows + r) * 16 bytes, so a tap's
+// shift by (t * dil) rows is a 16-byte multiple of the start address.
+// Descriptors: leading (K) byte offset = one chunk plane, stride (M/N) byte
+// offset = 128 bytes between 8-row core matrices.
+//
+// The input rows of all nine taps are staged once.  The weights are stored
+// pre-packed in the same operand layout ([layer][tap][chunk][out channel][8]),
+// so a tap is one 32 KB bulk copy (cp.async.bulk) into a ring of NSTG stages:
+// thread 0 issues a tap's MMAs (for every tile, sharing the tap's weights) as
+// soon as its copy has landed, and refills a stage with the tap NSTG ahead
+// once the MMAs reading it have completed (tcgen05.commit to an mbarrier).
+// Every wait is bounded and sets *err on expiry.
+constexpr int TPC = 2;                        // tiles per CTA
+constexpr int NSTG = 3;                       // weight stages
+constexpr int TAP_BYTES = CH * CH * 2;        // one tap's packed weights
+__host__ __device__ constexpr size_t conv_smem(int dil) { return (size_t) 16 * (TPC * TILE + 8 * dil) * 16 + (size_t) NSTG * TAP_BYTES + 128; }
+
 __device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned) __cvta_generic_to_shared(p); }
 __device__ __forceinline__ unsigned long long umma_desc(unsigned saddr, unsigned lbo, unsigned sbo)
 {
@@ -119,6 +131,13 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *mb, unsign
   }
   return false;
 }
+// one tap's packed weights: global -> shared stage, completing on mb
+__device__ __forceinline__ void tap_copy(void *dst, const void *src, unsigned long long *mb)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(smem_u32(mb)), "r"(TAP_BYTES) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               :: "r"(smem_u32(dst)), "l"(src), "r"(TAP_BYTES), "r"(smem_u32(mb)) : "memory");
+}
 
 // mask == NULL: out = bf16(relu(acc + bias)) (a forward layer).  mask != NULL:
 // out = bf16(acc) where mask > 0, else 0, no bias (the input gradient of a
@@ -128,22 +147,26 @@ __global__ void __launch_bounds__(128, 1) filter_conv_tc(const unsigned short *i
                                                          const unsigned short *mask)
 {
   extern __shared__ __align__(1024) unsigned char tsm[];
-  const int rows = TILE + 8 * dil;
+  const int rows = TPC * TILE + 8 * dil;
   unsigned char *sA = tsm;                                    // [16 chunks][rows][16 B]
-  unsigned char *sB = tsm + (size_t) 16 * rows * 16;          // [16 chunks][128][16 B]
-  unsigned long long *mbar = reinterpret_cast<unsigned long long *>(sB + 16 * CH * 16);
-  unsigned *tslot = reinterpret_cast<unsigned *>(mbar + 1);
-  const int tile = blockIdx.x, win = blockIdx.y;
+  unsigned char *sB = tsm + (size_t) 16 * rows * 16;          // [NSTG][16 chunks][128][16 B]
+  unsigned long long *mbW = reinterpret_cast<unsigned long long *>(sB + (size_t) NSTG * TAP_BYTES);   // stage's copy landed
+  unsigned long long *mbM = mbW + NSTG;                                                              // stage's MMAs done
+  unsigned *tslot = reinterpret_cast<unsigned *>(mbM + NSTG);
+  const int tile0 = blockIdx.x * TPC, win = blockIdx.y;
+  const int ntile = LP / TILE - tile0 < TPC ? LP / TILE - tile0 : TPC;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" :: "r"(smem_u32(tslot)), "r"(128) : "memory");
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" :: "r"(smem_u32(tslot)), "r"(TPC * 128) : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
+  int issued[NSTG] = {0}, landed[NSTG] = {0};   // thread 0: copies issued / waited for, per stage
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(mbar)), "r"(1) : "memory");
+    for (int q = 0; q < 2 * NSTG; q++) asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(mbW + q)), "r"(1) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    for (int t = 0; t < NSTG && t < KT; t++) { tap_copy(sB + (size_t) t * TAP_BYTES, wt + (size_t) t * CH * CH, mbW + t); issued[t]++; }
   }
-  const int p0 = tile * TILE - 4 * dil;
+  const int p0 = tile0 * TILE - 4 * dil;
   const unsigned short *inw = in + (size_t) win * LP * CH;
   for (int x = tid; x < rows * 16; x += blockDim.x) {
     const int r = x >> 4, c = x & 15;
@@ -152,70 +175,105 @@ __global__ void __launch_bounds__(128, 1) filter_conv_tc(const unsigned short *i
     if (p >= 0 && p < LP) v = *reinterpret_cast<const uint4 *>(inw + (size_t) p * CH + c * 8);
     *reinterpret_cast<uint4 *>(sA + ((size_t) c * rows + r) * 16) = v;
   }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // generic-proxy stores -> tensor-core reads
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const unsigned taddr = *tslot;
   // instruction descriptor: D f32, A/B bf16, both K-major, N = 128, M = 128
   const unsigned idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned) (CH >> 3) << 17) | ((unsigned) (TILE >> 4) << 24);
-  bool ok = true;
-  for (int t = 0; t < KT && ok; t++) {
-    const unsigned short *wtt = wt + (size_t) t * CH * CH;
-    for (int x = tid; x < CH * 16; x += blockDim.x) {
-      const int co = x >> 4, c = x & 15;
-      *reinterpret_cast<uint4 *>(sB + ((size_t) c * CH + co) * 16) = *reinterpret_cast<const uint4 *>(wtt + (size_t) co * CH + c * 8);
-    }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // generic-proxy stores -> tensor-core reads
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    if (tid == 0) {
+  __shared__ int s_ok;
+  if (tid == 0) {
+    bool ok = true;
+    int committed = 0;   // taps whose MMAs were committed
+    for (int t = 0; t < KT && ok; t++) {
+      const int st = t % NSTG;
+      ok = mbar_wait_bounded(mbW + st, (unsigned) ((t / NSTG) & 1));
+      if (!ok) break;
+      landed[st]++;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      for (int kb = 0; kb < CH / 16; kb++) {
-        const unsigned long long ad = umma_desc(smem_u32(sA + ((size_t) (2 * kb) * rows + t * dil) * 16), rows * 16, 128);
-        const unsigned long long bd = umma_desc(smem_u32(sB + (size_t) (2 * kb) * CH * 16), CH * 16, 128);
-        const unsigned acc = (t > 0 || kb > 0) ? 1u : 0u;
-        asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
-                     :: "r"(taddr), "l"(ad), "l"(bd), "r"(idesc), "r"(acc) : "memory");
+      const unsigned char *stg = sB + (size_t) st * TAP_BYTES;
+      for (int u = 0; u < ntile; u++)
+        for (int kb = 0; kb < CH / 16; kb++) {
+          const unsigned long long ad = umma_desc(smem_u32(sA + ((size_t) (2 * kb) * rows + u * TILE + t * dil) * 16), rows * 16, 128);
+          const unsigned long long bd = umma_desc(smem_u32(stg + (size_t) (2 * kb) * CH * 16), CH * 16, 128);
+          const unsigned acc = (t > 0 || kb > 0) ? 1u : 0u;
+          asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
+                       :: "r"(taddr + (unsigned) (u * 128)), "l"(ad), "l"(bd), "r"(idesc), "r"(acc) : "memory");
+        }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(smem_u32(mbM + st)) : "memory");
+      committed = t + 1;
+      // refill the previous tap's stage with the tap NSTG after it, once its MMAs are done
+      if (t >= 1 && t - 1 + NSTG < KT) {
+        const int sp = (t - 1) % NSTG;
+        ok = mbar_wait_bounded(mbM + sp, (unsigned) (((t - 1) / NSTG) & 1));
+        if (!ok) break;
+        tap_copy(sB + (size_t) sp * TAP_BYTES, wt + (size_t) (t - 1 + NSTG) * CH * CH, mbW + sp);
+        issued[sp]++;
       }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(smem_u32(mbar)) : "memory");
     }
-    // the tap's MMAs must finish reading sB before it is overwritten
-    if (!mbar_wait_bounded(mbar, (unsigned) (t & 1))) { ok = false; if (tid == 0) atomicOr(err, 1); }
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  }
-  // epilogue: warp w holds tile rows 32 w .. 32 w + 31 (TMEM lanes), 16 columns per load
-  unsigned short *outw = out + (size_t) win * LP * CH;
-  const int row = tile * TILE + 32 * warp + lane;
-  for (int cb = 0; cb < CH / 16; cb++) {
-    unsigned r[16];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-                 : "r"(taddr + ((unsigned) (32 * warp) << 16) + (unsigned) (cb * 16)));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-    unsigned pk[8];
-#pragma unroll
-    for (int j = 0; j < 8; j++) {
-      const int co = cb * 16 + 2 * j;
-      float v0, v1;
-      if (mask) {
-        const unsigned mk = *reinterpret_cast<const unsigned *>(mask + (size_t) win * LP * CH + (size_t) row * CH + co);
-        v0 = (mk & 0xFFFFu) != 0 ? __uint_as_float(r[2 * j]) : 0.f;      // activations are >= 0: nonzero bits <=> > 0
-        v1 = (mk >> 16) != 0 ? __uint_as_float(r[2 * j + 1]) : 0.f;
-      } else {
-        v0 = __uint_as_float(r[2 * j]) + bias[co]; v1 = __uint_as_float(r[2 * j + 1]) + bias[co + 1];
-        v0 = v0 > 0.f ? v0 : 0.f; v1 = v1 > 0.f ? v1 : 0.f;
-      }
-      if (row >= W2 || !ok) v0 = v1 = 0.f;
-      pk[j] = (unsigned) f2bf(v0) | ((unsigned) f2bf(v1) << 16);
+    // the MMAs complete in order: the last tap's commit means all are done
+    if (ok) ok = mbar_wait_bounded(mbM + (KT - 1) % NSTG, (unsigned) (((KT - 1) / NSTG) & 1));
+    if (!ok) {
+      atomicOr(err, 1);
+      // let the committed MMAs finish (they complete in order) and every
+      // weight copy still in flight land before TMEM is freed and the CTA exits
+      if (committed > 0) mbar_wait_bounded(mbM + (committed - 1) % NSTG, (unsigned) (((committed - 1) / NSTG) & 1));
+      for (int q = 0; q < NSTG; q++)
+        while (landed[q] < issued[q]) { mbar_wait_bounded(mbW + q, (unsigned) (landed[q] & 1)); landed[q]++; }
     }
-    uint4 *dst = reinterpret_cast<uint4 *>(outw + (size_t) row * CH + cb * 16);
-    dst[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-    dst[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+    s_ok = ok ? 1 : 0;
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(taddr), "r"(128) : "memory");
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const bool ok = s_ok != 0;
+  // epilogue: warp w holds tile rows 32 w .. 32 w + 31 (TMEM lanes), 16 columns per load
+  unsigned short *outw = out + (size_t) win * LP * CH;
+  for (int u = 0; u < ntile; u++) {
+    const int row = (tile0 + u) * TILE + 32 * warp + lane;
+    for (int cb = 0; cb < CH / 16; cb++) {
+      unsigned r[16];
+      asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                   : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                     "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                   : "r"(taddr + ((unsigned) (32 * warp) << 16) + (unsigned) (u * 128 + cb * 16)));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      unsigned pk[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const int co = cb * 16 + 2 * j;
+        float v0, v1;
+        if (mask) {
+          const unsigned mk = *reinterpret_cast<const unsigned *>(mask + (size_t) win * LP * CH + (size_t) row * CH + co);
+          v0 = (mk & 0xFFFFu) != 0 ? __uint_as_float(r[2 * j]) : 0.f;      // activations are >= 0: nonzero bits <=> > 0
+          v1 = (mk >> 16) != 0 ? __uint_as_float(r[2 * j + 1]) : 0.f;
+        } else {
+          v0 = __uint_as_float(r[2 * j]) + bias[co]; v1 = __uint_as_float(r[2 * j + 1]) + bias[co + 1];
+          v0 = v0 > 0.f ? v0 : 0.f; v1 = v1 > 0.f ? v1 : 0.f;
+        }
+        if (row >= W2 || !ok) v0 = v1 = 0.f;
+        pk[j] = (unsigned) f2bf(v0) | ((unsigned) f2bf(v1) << 16);
+      }
+      uint4 *dst = reinterpret_cast<uint4 *>(outw + (size_t) row * CH + cb * 16);
+      dst[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      dst[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(taddr), "r"(TPC * 128) : "memory");
+}
+
+// Packs dilated-layer weights [l][t][co][ci] (bf16 bits) into the operand
+// layout [l][t][ci / 8][co][ci % 8] that one bulk copy per tap stages.
+static void pack_conv_weights(const uint16_t *w, std::vector<uint16_t> &pk)
+{
+  pk.assign((size_t) 5 * KT * CH * CH, 0);
+  for (int lt = 0; lt < 5 * KT; lt++)
+    for (int co = 0; co < CH; co++)
+      for (int ci = 0; ci < CH; ci++)
+        pk[(((size_t) lt * 16 + ci / 8) * CH + co) * 8 + ci % 8] = w[((size_t) lt * CH + co) * CH + ci];
 }
 
 // Read-out: max over the window's positions per channel, then each head's
@@ -257,13 +315,16 @@ extern "C" int cmgb_filter_create_heads(cmgb_ctx *ctx, int W, int nheads, const 
   FCUDA(cudaMalloc(&f->d_b, sizeof(float) * NL * CH));
   FCUDA(cudaMalloc(&f->d_out, sizeof(float) * (CH + 1) * nheads));
   FCUDA(cudaMemcpy(f->d_w0, w0, sizeof(float) * KT * 4 * CH, cudaMemcpyHostToDevice));
-  FCUDA(cudaMemcpy(f->d_w, w, sizeof(unsigned short) * 5 * KT * CH * CH, cudaMemcpyHostToDevice));
+  {
+    std::vector<uint16_t> pk;
+    pack_conv_weights(w, pk);
+    FCUDA(cudaMemcpy(f->d_w, pk.data(), sizeof(unsigned short) * 5 * KT * CH * CH, cudaMemcpyHostToDevice));
+  }
   FCUDA(cudaMemcpy(f->d_b, bias, sizeof(float) * NL * CH, cudaMemcpyHostToDevice));
   FCUDA(cudaMemcpy(f->d_out, wout, sizeof(float) * (CH + 1) * nheads, cudaMemcpyHostToDevice));
   FCUDA(cudaMalloc(&f->d_err, sizeof(int)));
   FCUDA(cudaMemset(f->d_err, 0, sizeof(int)));
-  const int maxsm = 16 * (TILE + 8 * DIL[NL - 1]) * 16 + 16 * CH * 16 + 64;
-  FCUDA(cudaFuncSetAttribute(filter_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm));
+  FCUDA(cudaFuncSetAttribute(filter_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) conv_smem(DIL[NL - 1])));
   *ret = f.release();
   return CMGB_OK;
 #endif
@@ -320,8 +381,7 @@ extern "C" int cmgb_filter_windows(cmgb_ctx *ctx, cmgb_filter *f, const uint8_t 
   int cur = 0;
   for (int l = 1; l < NL; l++) {
     const int d = DIL[l];
-    const size_t sm = (size_t) 16 * (TILE + 8 * d) * 16 + (size_t) 16 * CH * 16 + 64;
-    filter_conv_tc<<<dim3(f->LP / TILE, nwin), 128, sm>>>(f->d_act[cur], f->d_act[cur ^ 1], f->LP, (int) (2 * W), d,
+    filter_conv_tc<<<dim3((f->LP / TILE + TPC - 1) / TPC, nwin), 128, conv_smem(d)>>>(f->d_act[cur], f->d_act[cur ^ 1], f->LP, (int) (2 * W), d,
                                                           f->d_w + (size_t) (l - 1) * KT * CH * CH, f->d_b + l * CH, f->d_err,
                                                           nullptr);
     FCUDA(cudaGetLastError());
@@ -556,16 +616,18 @@ __global__ void train_adamw(float *p, const float *g, float *m1, float *m2, long
   }
 }
 
-// BF16 copies of the dilated layers: forward [l][t][co][ci] and backward
-// [l][t'][ci][co] = w[l][8 - t'][co][ci]
+// BF16 copies of the dilated layers in the convolution's operand layout
+// [l][t][k / 8][n][k % 8] (n: output channel, k: input channel): forward
+// (n, k) = (co, ci) of w[l][t][co][ci]; backward tap t' = 8 - t with
+// (n, k) = (ci, co)
 __global__ void train_pack(const float *w, unsigned short *wbf, unsigned short *wtbf)
 {
   const long long n = (long long) 5 * KT * CH * CH;
   for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
     const int ci = (int) (i % CH), co = (int) ((i / CH) % CH), t = (int) ((i / (CH * CH)) % KT), l = (int) (i / ((long long) KT * CH * CH));
     const unsigned short h = f2bf(w[i]);
-    wbf[i] = h;
-    wtbf[(((size_t) l * KT + (KT - 1 - t)) * CH + ci) * CH + co] = h;
+    wbf[((((size_t) l * KT + t) * 16 + ci / 8) * CH + co) * 8 + ci % 8] = h;
+    wtbf[((((size_t) l * KT + (KT - 1 - t)) * 16 + co / 8) * CH + ci) * 8 + co % 8] = h;
   }
 }
 #endif
@@ -618,8 +680,7 @@ extern "C" int cmgb_filter_trainer_create_heads(cmgb_ctx *ctx, int W, int batch,
   FCUDA(cudaMemcpy(f->p, h.data(), NPARAM * sizeof(float), cudaMemcpyHostToDevice));
   train_pack<<<512, 256>>>(f->p + OFF_W, f->wbf, f->wtbf);
   FCUDA(cudaGetLastError());
-  const int maxsm = 16 * (TILE + 8 * DIL[NL - 1]) * 16 + 16 * CH * 16 + 64;
-  FCUDA(cudaFuncSetAttribute(filter_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm));
+  FCUDA(cudaFuncSetAttribute(filter_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) conv_smem(DIL[NL - 1])));
   FCUDA(cudaDeviceSynchronize());
   *ret = f.release();
   return CMGB_OK;
@@ -691,8 +752,7 @@ extern "C" int cmgb_filter_trainer_step_heads(cmgb_filter_trainer *f, const uint
   filter_layer0<<<dim3(64, B), CH>>>(f->win, 0, (long long) B * W2 - 1, W, W2, B, LP, f->p + OFF_W0, f->p + OFF_B, f->act[0]);
   for (int l = 1; l < NL; l++) {
     const int d = DIL[l];
-    const size_t sm = (size_t) 16 * (TILE + 8 * d) * 16 + (size_t) 16 * CH * 16 + 64;
-    filter_conv_tc<<<dim3(LP / TILE, B), 128, sm>>>(f->act[l - 1], f->act[l], LP, W2, d, f->wbf + (size_t) (l - 1) * KT * CH * CH,
+    filter_conv_tc<<<dim3((LP / TILE + TPC - 1) / TPC, B), 128, conv_smem(d)>>>(f->act[l - 1], f->act[l], LP, W2, d, f->wbf + (size_t) (l - 1) * KT * CH * CH,
                                                     f->p + OFF_B + l * CH, f->err, nullptr);
   }
   train_readout_fwd<<<B, CH>>>(f->act[NL - 1], LP, W2, f->p + OFF_WOUT, H, f->pooled, f->argm, f->logit);
@@ -710,8 +770,7 @@ extern "C" int cmgb_filter_trainer_step_heads(cmgb_filter_trainer *f, const uint
     train_sum_parts<<<1, CH>>>(f->part_b, NB_BIAS, CH, f->g + OFF_B + l * CH);
     train_wgrad<<<dim3(KT, 16, f->zsplit), 256>>>(f->dz[cur], f->act[l - 1], B, LP, W2, d, f->part_w);
     train_sum_parts<<<(unsigned) ((nw + 255) / 256), 256>>>(f->part_w, f->zsplit, nw, f->g + OFF_W + (size_t) (l - 1) * nw);
-    const size_t sm = (size_t) 16 * (TILE + 8 * d) * 16 + (size_t) 16 * CH * 16 + 64;
-    filter_conv_tc<<<dim3(LP / TILE, B), 128, sm>>>(f->dz[cur], f->dz[cur ^ 1], LP, W2, d, f->wtbf + (size_t) (l - 1) * KT * CH * CH,
+    filter_conv_tc<<<dim3((LP / TILE + TPC - 1) / TPC, B), 128, conv_smem(d)>>>(f->dz[cur], f->dz[cur ^ 1], LP, W2, d, f->wtbf + (size_t) (l - 1) * KT * CH * CH,
                                                     nullptr, f->err, f->act[l - 1]);
     cur ^= 1;
   }

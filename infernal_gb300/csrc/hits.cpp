@@ -2,9 +2,12 @@
 #include "hits.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <mutex>
+#include <thread>
 
 namespace cmgb {
 
@@ -14,20 +17,55 @@ static inline double log2d(double x) { return x > 0 ? std::log(x) * 1.44269504 :
 
 static float flog_tbl[23000];
 static int ilog_tbl[23000];
-static bool tables_done = false;
+static std::once_flag tables_once;
 
 void logsum_tables(const float **flog, const int **ilog)
 {
-  if (!tables_done) {
+  std::call_once(tables_once, [] {
     for (int i = 0; i < 23000; i++) {
       double x = log2d(1. + std::exp(((double) -i / 1000.0f) * 0.69314718));
       flog_tbl[i] = (float) x;
       ilog_tbl[i] = (int) std::rint(1000.0f * x);
     }
-    tables_done = true;
-  }
+  });
   if (flog) *flog = flog_tbl;
   if (ilog) *ilog = ilog_tbl;
+}
+
+void parallel_for(int n, const std::function<void(int)> &f)
+{
+  const int nt = std::min<int>(n, std::max(1u, std::min(16u, std::thread::hardware_concurrency())));
+  if (nt <= 1) { for (int i = 0; i < n; i++) f(i); return; }
+  std::atomic<int> next{0};
+  std::vector<std::thread> th;
+  for (int t = 0; t < nt; t++)
+    th.emplace_back([&] { for (int i; (i = next.fetch_add(1)) < n;) f(i); });
+  for (auto &x : th) x.join();
+}
+
+// Candidates in (j, d) order.  The cells are distinct, so two stable
+// counting passes (by d, then by j) give the order a comparison sort gives;
+// they are used when the j range is not much wider than the candidate count.
+static void sort_jd(std::vector<CandHost> &c)
+{
+  if (c.size() < 2) return;
+  long long jmin = c[0].j, jmax = c[0].j;
+  int dmax = 0;
+  for (const CandHost &x : c) { jmin = std::min(jmin, x.j); jmax = std::max(jmax, x.j); dmax = std::max(dmax, x.d); }
+  const long long range = jmax - jmin + 1;
+  if (c.size() < 2048 || range > 8 * (long long) c.size()) {
+    std::sort(c.begin(), c.end(), [](const CandHost &x, const CandHost &y) { return x.j != y.j ? x.j < y.j : x.d < y.d; });
+    return;
+  }
+  std::vector<CandHost> tmp(c.size());
+  std::vector<int64_t> cnt((size_t) dmax + 2, 0);
+  for (const CandHost &x : c) cnt[(size_t) x.d + 1]++;
+  for (size_t k = 1; k < cnt.size(); k++) cnt[k] += cnt[k - 1];
+  for (const CandHost &x : c) tmp[(size_t) cnt[(size_t) x.d]++] = x;
+  std::vector<int64_t> cj((size_t) range + 1, 0);
+  for (const CandHost &x : tmp) cj[(size_t) (x.j - jmin) + 1]++;
+  for (size_t k = 1; k < cj.size(); k++) cj[k] += cj[k - 1];
+  for (const CandHost &x : tmp) c[(size_t) cj[(size_t) (x.j - jmin)]++] = x;
 }
 
 // LogSum2 / FLogsum (src/logsum.c:151-168)
@@ -51,17 +89,32 @@ static inline void count_res(double *ct, uint8_t x, int K)
 
 // Exact residue composition of [i, j]: the reference differences two running
 // sums that start at i0 (act[], src/cm_dpsearch.c:199-231).  When every code
-// in the range has weight 1, 1/2 or 1/4 those sums are exact and a direct
-// count gives the same doubles; three-way codes (H, B, V, D) need the
-// running sums themselves.
+// in the range has weight 1, 1/2 or 1/4 those sums are exact, and so are
+// integer prefix counts in quarter units, which give the same doubles in
+// O(1) per lookup; three-way codes (H, B, V, D) need the running doubles
+// themselves.
 struct Composition {
   const uint8_t *dsq; int64_t i0, j0; int K;
   bool exact_direct = true;
-  std::vector<double> prefix;   // (j0-i0+2) x K running sums, only when needed
+  std::vector<int32_t> qprefix;  // (j0-i0+2) x K running counts in quarter units (exact_direct)
+  std::vector<double> prefix;    // (j0-i0+2) x K running sums (three-way codes)
   Composition(const uint8_t *q, int64_t a, int64_t b, int k) : dsq(q), i0(a), j0(b), K(k) {
     for (int64_t x = i0; x <= j0; x++) { uint8_t c = dsq[x]; if (c >= K && c < 18 && __builtin_popcount(degen_mask[c]) == 3) { exact_direct = false; break; } }
-    if (!exact_direct) {
-      prefix.assign((size_t) (j0 - i0 + 2) * K, 0.);
+    const size_t n = (size_t) (j0 - i0 + 2) * K;
+    if (exact_direct) {
+      qprefix.assign(n, 0);
+      for (int64_t x = i0; x <= j0; x++) {
+        int32_t *cur = &qprefix[(size_t) (x - i0 + 1) * K];
+        std::memcpy(cur, cur - K, sizeof(int32_t) * K);
+        const uint8_t c = dsq[x];
+        if (c < K) cur[c] += 4;
+        else if (c < 18) {
+          const int nb = __builtin_popcount(degen_mask[c]);
+          if (nb) for (int y = 0; y < K; y++) if (degen_mask[c] & (1 << y)) cur[y] += 4 / nb;
+        }
+      }
+    } else {
+      prefix.assign(n, 0.);
       for (int64_t x = i0; x <= j0; x++) {
         double *cur = &prefix[(size_t) (x - i0 + 1) * K];
         std::memcpy(cur, cur - K, sizeof(double) * K);
@@ -71,9 +124,8 @@ struct Composition {
   }
   void get(int64_t i, int64_t j, float *comp) const {
     if (exact_direct) {
-      double ct[8] = {0};
-      for (int64_t x = i; x <= j; x++) count_res(ct, dsq[x], K);
-      for (int a = 0; a < K; a++) comp[a] = (float) ct[a];
+      const int32_t *hi = &qprefix[(size_t) (j - i0 + 1) * K], *lo = &qprefix[(size_t) (i - i0) * K];
+      for (int a = 0; a < K; a++) comp[a] = (float) ((double) (hi[a] - lo[a]) * 0.25);
     } else {
       const double *hi = &prefix[(size_t) (j - i0 + 1) * K], *lo = &prefix[(size_t) (i - i0) * K];
       for (int a = 0; a < K; a++) comp[a] = (float) (hi[a] - lo[a]);
@@ -129,7 +181,7 @@ bool allow_truncation(const TruncFilter &t, int64_t start, int64_t stop, int64_t
 void resolve_hits(std::vector<CandHost> &c, const ResolveArgs &a, std::vector<cmgb_hit> &out)
 {
   logsum_tables(nullptr, nullptr);
-  std::sort(c.begin(), c.end(), [](const CandHost &x, const CandHost &y) { return x.j != y.j ? x.j < y.j : x.d < y.d; });
+  sort_jd(c);
   Composition *cmp = nullptr;
   if (a.do_null3 && !c.empty()) cmp = new Composition(a.dsq, a.i0, a.j0, a.K);
 

@@ -13,6 +13,7 @@
 // tests, so the result is identical to resolving every cell.
 #pragma once
 #include <stdint.h>
+#include <functional>
 #include <vector>
 #include "../../include/infernal_gb300.h"
 
@@ -33,6 +34,10 @@ struct TruncFilter {
   const int *lpos, *rpos;// emit map [nodes]
 };
 bool allow_truncation(const TruncFilter &t, int64_t start, int64_t stop, int64_t i0, int64_t j0, int mode, int b);
+
+// f(0) .. f(n-1) on up to 16 host threads (the resolution of independent
+// sequences of a batch)
+void parallel_for(int n, const std::function<void(int)> &f);
 
 struct ResolveArgs {
   const float *null;     // [K]

@@ -161,7 +161,11 @@ template <> struct Sr<0> {
   typedef float T;
   static CMGB_DEV T imp() { return CMGB_IMP; }
   static CMGB_DEV T add(T a, T b) { return CMGB_FADD(a, b); }
-  static CMGB_DEV T comb(T a, T b, const unsigned short *) { return a > b ? a : b; }   // ESL_MAX(a,b)
+  // ESL_MAX(a,b) = a > b ? a : b.  The max instruction returns the same value
+  // and bits except for a = +0, b = -0 (and NaN, which never occurs); a DP value
+  // is -0.0 only if a model score table holds -0.0, which log2-odds scores do
+  // not (cmgb_model_create checks)
+  static CMGB_DEV T comb(T a, T b, const unsigned short *) { return fmaxf(a, b); }
   static CMGB_DEV T rootfirst(T x) { return CMGB_IMP > x ? CMGB_IMP : x; } // ESL_MAX(IMPOSSIBLE, x)
   static CMGB_DEV float score(T x) { return x; }
   static CMGB_DEV float envval(T x) { return x; }

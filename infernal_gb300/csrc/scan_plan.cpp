@@ -192,8 +192,8 @@ bool build_plan(const cmgb_model_desc *m, int qdbidx, int T, int nthreads, bool 
   const int tmp_elems = (T + 1) * tmp_stride;
   // the insert scratch is read back by the self-loop chains right after it is
   // written; with a global arena it still goes to shared memory when it fits
-  // next to a second CTA on the SM
-  P.tmp_smem = !arena_global || tmp_elems * 4 <= 96 * 1024;
+  // next to the ILogsum table, the residues and the phase records
+  P.tmp_smem = !arena_global || tmp_elems * 4 + (logsum_table ? CMGB_LOGSUM_TBL * 2 : 0) + 4 * (Wm + T) <= 176 * 1024;
   if (!P.tmp_smem) { P.tmp_off = off; off += tmp_elems; }
   off = (off + 3) & ~3;
   P.arena_global = arena_global ? 1 : 0;

@@ -706,8 +706,10 @@ def _ranges_scan(sc: "lib.Scanner", m, d_buf: int, nbuf: int, spans, algo: str, 
     L = (nbuf - 3) // 2
     offs = np.array([s * (L + 1) + a - 1 for s, a, b in spans], np.int64)
     lens = np.array([b - a + 1 for s, a, b in spans], np.int64)
+    t0 = time.perf_counter()
     rs = sc.scan_batch(m, None, algo=algo, qdbidx=qdb, cutoff=cut, env_cutoff=cut, ranges=(None, offs, lens),
                        device_buf=(d_buf, nbuf))
+    stats["wall_ms"][algo] += 1e3 * (time.perf_counter() - t0)
     stats["kernel_ms"][algo] += rs[0].kernel_ms
     stats["launches"] += sc.last_launches()
     stats["calls"][algo] += 1
@@ -718,8 +720,11 @@ def _ranges_scan(sc: "lib.Scanner", m, d_buf: int, nbuf: int, spans, algo: str, 
 
 
 def _new_stats():
-    return {"kernel_ms": {"filter": 0.0, "cyk": 0.0, "inside": 0.0}, "launches": 0, "h2d": 0, "d2h": 0,
-            "lengths": {"cyk": [], "inside": []}, "calls": {"cyk": 0, "inside": 0}, "kept": 0}
+    # kernel_ms: device time of each stage's kernels (CUDA events); wall_ms:
+    # host wall time of each stage's calls (kernels, copies and the host's
+    # hit resolution)
+    return {"kernel_ms": {"filter": 0.0, "cyk": 0.0, "inside": 0.0}, "wall_ms": {"filter": 0.0, "cyk": 0.0, "inside": 0.0},
+            "launches": 0, "h2d": 0, "d2h": 0, "lengths": {"cyk": [], "inside": []}, "calls": {"cyk": 0, "inside": 0}, "kept": 0}
 
 
 def _final_stage(sc, m, d_buf, nbuf, cyk_hits, ins_cut, stats):
@@ -747,11 +752,13 @@ def filtered_scan(sc: "lib.Scanner", filt: "Prefilter", m, d_buf: int, nbuf: int
     st = _new_stats()
     spans = []
     for s in (0, 1):
+        t0 = time.perf_counter()
         logit, ms = filt.logits(d_buf + s * (L + 1), 1, L)
         st["kernel_ms"]["filter"] += ms
         st["launches"] += filt.LAUNCHES
         st["d2h"] += 4 * len(logit)
         spans += [(s, a, b) for a, b in filt.regions(logit, 1, L)]
+        st["wall_ms"]["filter"] += 1e3 * (time.perf_counter() - t0)
     st["kept"] = sum(b - a + 1 for _, a, b in spans)
     cyk = [[], []]
     for (s, a, b), hs in zip(spans, _ranges_scan(sc, m, d_buf, nbuf, spans, "cyk", 1, cyk_cut, st)):
@@ -768,8 +775,10 @@ def plain_scan(sc: "lib.Scanner", m, d_buf: int, nbuf: int, cyk_cut: float, ins_
     st = _new_stats()
     cyk = [[], []]
     for s in (0, 1):
+        t0 = time.perf_counter()
         r = sc.scan(m, None, 1, L, algo="cyk", qdbidx=1, cutoff=cyk_cut, env_cutoff=cyk_cut,
                     device_ptr=d_buf + s * (L + 1))
+        st["wall_ms"]["cyk"] += 1e3 * (time.perf_counter() - t0)
         st["kernel_ms"]["cyk"] += r.kernel_ms
         st["launches"] += sc.last_launches()
         h2d, d2h = sc.last_transfer_bytes()

@@ -2,6 +2,8 @@
 the CPU oracle, through the C ABI.  CYK, integer Inside, hit lists (greedy and
 optimal resolution, NULL3), envelopes, best scores and per-state best scores
 must all be bit-identical."""
+import zlib
+
 import numpy as np
 import pytest
 
@@ -51,7 +53,7 @@ def test_golden_on_gpu(gpu, golden, models, T, arena):
                                            ("Vault", "finside", 2)])
 def test_random_targets_vs_oracle(gpu, models, name, algo, qdb):
     m = models[name]
-    rng = np.random.default_rng(hash((name, algo)) & 0xffff)
+    rng = np.random.default_rng(zlib.crc32(f"{name}{algo}".encode()))
     n = 20000 if algo == "cyk" else 8000
     if name == "Plant_SRP":
         n //= 2
@@ -71,7 +73,7 @@ def test_window_and_tile_invariance(gpu, models):
     dsq = cmfile.digitize("".join(rng.choice(list("ACGU"), n)))
     ref = None
     for T, win, cps, nt, ar in ((16, 0, 0, 0, 1), (8, 1500, 1, 256, 1), (3, 4000, 2, 0, 1), (16, 777, 1, 0, 2),
-                                (64, 2500, 0, 0, 2), (33, 0, 0, 128, 2)):
+                                (64, 2500, 0, 0, 2), (33, 0, 0, 128, 2), (96, 3000, 0, 0, 2), (128, 0, 0, 0, 2)):
         gpu.set_shape(T, win, cps, nt, ar)
         r = gpu.scan(m, dsq, 1, n, algo="cyk", qdbidx=1, cutoff=-1.0, env_cutoff=3.0, want_vsc=True)
         key = (r.hits, r.envi, r.envj, r.sc, r.vsc.tobytes())
@@ -111,6 +113,6 @@ def test_autotune_keeps_results(gpu, models):
     gpu.set_shape(0, 0, 0)
     a = gpu.scan(m, dsq, 1, n, algo="inside", qdbidx=2, cutoff=0.0, env_cutoff=2.0, want_vsc=True)
     T, arena = gpu.autotune(m, 2, "inside", 20000)
-    assert T in (8, 16, 32, 48, 64) and arena in (1, 2)
+    assert T in (16, 32, 48, 64, 96, 128) and arena in (1, 2)
     b = gpu.scan(m, dsq, 1, n, algo="inside", qdbidx=2, cutoff=0.0, env_cutoff=2.0, want_vsc=True)
     assert (a.hits, a.envi, a.envj, a.sc, a.vsc.tobytes()) == (b.hits, b.envi, b.envj, b.sc, b.vsc.tobytes())

@@ -2,6 +2,8 @@
 cmgb_RefITrInsideScan) against the reference's golden vectors and the CPU
 oracle, through the C ABI: hits (with their modes), envelope, best score, the
 best parse's mode and per-state best scores must be bit-identical."""
+import zlib
+
 import numpy as np
 import pytest
 
@@ -69,7 +71,7 @@ def _reads(m, rng, nreads, L=(100, 400)):
                                            ("tRNA", "trinside", 2), ("Vault", "trinside", 2), ("Plant_SRP", "trinside", 2)])
 def test_reads_vs_oracle(gpu, models, name, algo, qdb):
     m = models[name]
-    rng = np.random.default_rng(hash((name, algo, "tr")) & 0xffff)
+    rng = np.random.default_rng(zlib.crc32(f"{name}{algo}tr".encode()))
     gpu.set_shape(0, 0, 0)
     for k, seq in enumerate(_reads(m, rng, 6)):
         dsq = cmfile.digitize(seq)
