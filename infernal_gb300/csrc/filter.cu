@@ -110,10 +110,13 @@ __global__ void filter_layer0(const unsigned char *dsq, long long i0, long long 
 // soon as its copy has landed, and refills a stage with the tap NSTG ahead
 // once the MMAs reading it have completed (tcgen05.commit to an mbarrier).
 // Every wait is bounded and sets *err on expiry.
-constexpr int TPC = 2;                        // tiles per CTA
-constexpr int NSTG = 3;                       // weight stages
 constexpr int TAP_BYTES = CH * CH * 2;        // one tap's packed weights
-__host__ __device__ constexpr size_t conv_smem(int dil) { return (size_t) 16 * (TPC * TILE + 8 * dil) * 16 + (size_t) NSTG * TAP_BYTES + 128; }
+// TPC tiles per CTA, NSTG weight stages
+__host__ __device__ constexpr size_t conv_smem(int tpc, int nstg, int dil) { return (size_t) 16 * (tpc * TILE + 8 * dil) * 16 + (size_t) nstg * TAP_BYTES + 128; }
+// Dilations up to 8 use one tile and two stages per CTA (at most 112 KB, so
+// two CTAs share an SM and one's staging and epilogue overlap the other's
+// MMAs); wider dilations two tiles and three stages (one CTA per SM).
+constexpr bool conv_small(int dil) { return dil <= 8; }
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned) __cvta_generic_to_shared(p); }
 __device__ __forceinline__ unsigned long long umma_desc(unsigned saddr, unsigned lbo, unsigned sbo)
@@ -142,6 +145,7 @@ __device__ __forceinline__ void tap_copy(void *dst, const void *src, unsigned lo
 // mask == NULL: out = bf16(relu(acc + bias)) (a forward layer).  mask != NULL:
 // out = bf16(acc) where mask > 0, else 0, no bias (the input gradient of a
 // layer, with the previous layer's ReLU derivative folded in).
+template <int TPC, int NSTG>
 __global__ void __launch_bounds__(128, 1) filter_conv_tc(const unsigned short *in, unsigned short *out, int LP, int W2, int dil,
                                                          const unsigned short *wt, const float *bias, int *err,
                                                          const unsigned short *mask)
@@ -153,6 +157,7 @@ __global__ void __launch_bounds__(128, 1) filter_conv_tc(const unsigned short *i
   unsigned long long *mbW = reinterpret_cast<unsigned long long *>(sB + (size_t) NSTG * TAP_BYTES);   // stage's copy landed
   unsigned long long *mbM = mbW + NSTG;                                                              // stage's MMAs done
   unsigned *tslot = reinterpret_cast<unsigned *>(mbM + NSTG);
+  int *s_ok = reinterpret_cast<int *>(tslot + 1);   // thread 0's verdict, for the epilogue
   const int tile0 = blockIdx.x * TPC, win = blockIdx.y;
   const int ntile = LP / TILE - tile0 < TPC ? LP / TILE - tile0 : TPC;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -182,7 +187,6 @@ __global__ void __launch_bounds__(128, 1) filter_conv_tc(const unsigned short *i
   const unsigned taddr = *tslot;
   // instruction descriptor: D f32, A/B bf16, both K-major, N = 128, M = 128
   const unsigned idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned) (CH >> 3) << 17) | ((unsigned) (TILE >> 4) << 24);
-  __shared__ int s_ok;
   if (tid == 0) {
     bool ok = true;
     int committed = 0;   // taps whose MMAs were committed
@@ -222,12 +226,12 @@ __global__ void __launch_bounds__(128, 1) filter_conv_tc(const unsigned short *i
       for (int q = 0; q < NSTG; q++)
         while (landed[q] < issued[q]) { mbar_wait_bounded(mbW + q, (unsigned) (landed[q] & 1)); landed[q]++; }
     }
-    s_ok = ok ? 1 : 0;
+    *s_ok = ok ? 1 : 0;
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const bool ok = s_ok != 0;
+  const bool ok = *s_ok != 0;
   // epilogue: warp w holds tile rows 32 w .. 32 w + 31 (TMEM lanes), 16 columns per load
   unsigned short *outw = out + (size_t) win * LP * CH;
   for (int u = 0; u < ntile; u++) {
@@ -263,6 +267,25 @@ __global__ void __launch_bounds__(128, 1) filter_conv_tc(const unsigned short *i
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(taddr), "r"(TPC * 128) : "memory");
+}
+
+// One dilated layer over LP/TILE tiles of nwin windows.
+static cudaError_t conv_launch(const unsigned short *in, unsigned short *out, int LP, int W2, int dil, int nwin,
+                               const unsigned short *wt, const float *bias, int *err, const unsigned short *mask)
+{
+  const int ntile = LP / TILE;
+  if (conv_small(dil))
+    filter_conv_tc<1, 2><<<dim3(ntile, nwin), 128, conv_smem(1, 2, dil)>>>(in, out, LP, W2, dil, wt, bias, err, mask);
+  else
+    filter_conv_tc<2, 3><<<dim3((ntile + 1) / 2, nwin), 128, conv_smem(2, 3, dil)>>>(in, out, LP, W2, dil, wt, bias, err, mask);
+  return cudaGetLastError();
+}
+static cudaError_t conv_prepare()
+{
+  cudaError_t e = cudaFuncSetAttribute(filter_conv_tc<1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) conv_smem(1, 2, 8));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(filter_conv_tc<2, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) conv_smem(2, 3, DIL[NL - 1]));
+  return e;
 }
 
 // Packs dilated-layer weights [l][t][co][ci] (bf16 bits) into the operand
@@ -324,7 +347,7 @@ extern "C" int cmgb_filter_create_heads(cmgb_ctx *ctx, int W, int nheads, const 
   FCUDA(cudaMemcpy(f->d_out, wout, sizeof(float) * (CH + 1) * nheads, cudaMemcpyHostToDevice));
   FCUDA(cudaMalloc(&f->d_err, sizeof(int)));
   FCUDA(cudaMemset(f->d_err, 0, sizeof(int)));
-  FCUDA(cudaFuncSetAttribute(filter_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) conv_smem(DIL[NL - 1])));
+  FCUDA(conv_prepare());
   *ret = f.release();
   return CMGB_OK;
 #endif
@@ -381,9 +404,8 @@ extern "C" int cmgb_filter_windows(cmgb_ctx *ctx, cmgb_filter *f, const uint8_t 
   int cur = 0;
   for (int l = 1; l < NL; l++) {
     const int d = DIL[l];
-    filter_conv_tc<<<dim3((f->LP / TILE + TPC - 1) / TPC, nwin), 128, conv_smem(d)>>>(f->d_act[cur], f->d_act[cur ^ 1], f->LP, (int) (2 * W), d,
-                                                          f->d_w + (size_t) (l - 1) * KT * CH * CH, f->d_b + l * CH, f->d_err,
-                                                          nullptr);
+    FCUDA(conv_launch(f->d_act[cur], f->d_act[cur ^ 1], f->LP, (int) (2 * W), d, nwin, f->d_w + (size_t) (l - 1) * KT * CH * CH,
+                      f->d_b + l * CH, f->d_err, nullptr));
     FCUDA(cudaGetLastError());
     cur ^= 1;
   }
@@ -680,7 +702,7 @@ extern "C" int cmgb_filter_trainer_create_heads(cmgb_ctx *ctx, int W, int batch,
   FCUDA(cudaMemcpy(f->p, h.data(), NPARAM * sizeof(float), cudaMemcpyHostToDevice));
   train_pack<<<512, 256>>>(f->p + OFF_W, f->wbf, f->wtbf);
   FCUDA(cudaGetLastError());
-  FCUDA(cudaFuncSetAttribute(filter_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) conv_smem(DIL[NL - 1])));
+  FCUDA(conv_prepare());
   FCUDA(cudaDeviceSynchronize());
   *ret = f.release();
   return CMGB_OK;
@@ -752,8 +774,7 @@ extern "C" int cmgb_filter_trainer_step_heads(cmgb_filter_trainer *f, const uint
   filter_layer0<<<dim3(64, B), CH>>>(f->win, 0, (long long) B * W2 - 1, W, W2, B, LP, f->p + OFF_W0, f->p + OFF_B, f->act[0]);
   for (int l = 1; l < NL; l++) {
     const int d = DIL[l];
-    filter_conv_tc<<<dim3((LP / TILE + TPC - 1) / TPC, B), 128, conv_smem(d)>>>(f->act[l - 1], f->act[l], LP, W2, d, f->wbf + (size_t) (l - 1) * KT * CH * CH,
-                                                    f->p + OFF_B + l * CH, f->err, nullptr);
+    conv_launch(f->act[l - 1], f->act[l], LP, W2, d, B, f->wbf + (size_t) (l - 1) * KT * CH * CH, f->p + OFF_B + l * CH, f->err, nullptr);
   }
   train_readout_fwd<<<B, CH>>>(f->act[NL - 1], LP, W2, f->p + OFF_WOUT, H, f->pooled, f->argm, f->logit);
   train_loss<<<1, 256>>>(f->logit, f->y, f->posw, B, H, f->dlogit, f->loss);
@@ -770,8 +791,7 @@ extern "C" int cmgb_filter_trainer_step_heads(cmgb_filter_trainer *f, const uint
     train_sum_parts<<<1, CH>>>(f->part_b, NB_BIAS, CH, f->g + OFF_B + l * CH);
     train_wgrad<<<dim3(KT, 16, f->zsplit), 256>>>(f->dz[cur], f->act[l - 1], B, LP, W2, d, f->part_w);
     train_sum_parts<<<(unsigned) ((nw + 255) / 256), 256>>>(f->part_w, f->zsplit, nw, f->g + OFF_W + (size_t) (l - 1) * nw);
-    filter_conv_tc<<<dim3((LP / TILE + TPC - 1) / TPC, B), 128, conv_smem(d)>>>(f->dz[cur], f->dz[cur ^ 1], LP, W2, d, f->wtbf + (size_t) (l - 1) * KT * CH * CH,
-                                                    nullptr, f->err, f->act[l - 1]);
+    conv_launch(f->dz[cur], f->dz[cur ^ 1], LP, W2, d, B, f->wtbf + (size_t) (l - 1) * KT * CH * CH, nullptr, f->err, f->act[l - 1]);
     cur ^= 1;
   }
   train_bias_grad<<<NB_BIAS, CH>>>(f->dz[cur], (long long) B * LP, f->part_b);
