@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <numeric>
 #include <climits>
 #include <cstdio>
 #include <cstring>
@@ -958,6 +959,18 @@ extern "C" int cmgb_RefITrInsideScan_dev(cmgb_ctx *c, cmgb_model *m, char *errbu
 // seqs: host residues (copied to the device per call) or, when d_seqs is
 // given, residues already in device memory (host copies of single sequences
 // are fetched only for the NULL3 composition of sequences with candidates).
+// Owned rows per window of a batched scan: up to max(8 W, 2048), and no more
+// than the batch's rows per resident CTA (at least W), so that a batch of few
+// long sequences still spreads over every SM: a later window starts W-1 rows
+// early, which leaves every cell's value unchanged.
+static int64_t batch_window_len(const cmgb_ctx *c, int W, int64_t rows)
+{
+  const int64_t cap = std::max<int64_t>(8LL * W, 2048);
+  const int64_t ctas = (int64_t) c->nsm * std::max(1, c->ctas_per_sm);
+  const int64_t share = std::max<int64_t>(W, (rows + ctas - 1) / std::max<int64_t>(1, ctas));
+  return std::min(cap, share);
+}
+
 static int scan_batch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo, int qdbidx, int pass_idx,
                       const uint8_t *seqs, const uint8_t *d_seqs, int64_t seqs_len, const int64_t *offsets,
                       const int64_t *lengths, int nseq, float cutoff, cmgb_hitlist *hitlist, int do_null3, float env_cutoff,
@@ -1020,7 +1033,7 @@ static int scan_batch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo, int qd
   // work items: one per sequence for the truncated scanners; the standard
   // scanners cut sequences longer than a window into windows that start W-1
   // rows early (as the single-sequence scan does).  Longest first.
-  const int64_t wlen = std::max<int64_t>(8LL * m->W, 2048);
+  const int64_t wlen = batch_window_len(c, m->W, std::accumulate(lengths, lengths + nseq, (int64_t) 0));
   std::vector<int> wseq;                 // sequence of each window
   std::vector<long long> ws, we, ws0;
   for (int q = 0; q < nseq; q++) {
@@ -1333,10 +1346,12 @@ static int scan_multi(cmgb_ctx *c, cmgb_model *const *models, int nmodels, const
   // windows of every job (as cmgb_ScanBatch cuts a sequence), with their cost
   struct Win { int job; long long s, e, s0; double cost; };
   std::vector<Win> all;
+  int64_t job_rows = 0;
+  for (int k = 0; k < njobs; k++) job_rows += lengths[job_seq[k]];
   for (int k = 0; k < njobs; k++) {
     const int mi = job_model[k], q = job_seq[k];
     const int Wm = models[mi]->W;
-    const int64_t wlen = std::max<int64_t>(8LL * Wm, 2048);
+    const int64_t wlen = batch_window_len(c, Wm, job_rows);
     const int64_t a = offsets[q] + 1, b = offsets[q] + lengths[q];
     for (int64_t s0w = a; s0w <= b; s0w += wlen) {
       Win x; x.job = k; x.s = s0w; x.e = std::min<int64_t>(b, s0w + wlen - 1);

@@ -433,6 +433,17 @@ bool build_tr_plan(const cmgb_model_desc *m, int qdbidx, int T, int nthreads, bo
   off = (off + 3) & ~3;
   P.ltbl_off = off;
   if (logsum_table) off += (CMGB_LOGSUM_TBL * 2 + 3) / 4;
+  // CYK only: the inserts' non-self terms of the two self-loop planes (IL:
+  // J and L, IR: J and R), read back by the self-loop chains; in shared
+  // memory (the order-free max lets the chains fold them last)
+  if (!logsum_table) {
+    int tstr = 1;
+    for (int v = 0; v < M; v++) if (S[v].s.kind == SK_IL || S[v].s.kind == SK_IR) tstr = std::max(tstr, S[v].s.hi - S[v].s.lo + 1);
+    P.tmp_stride = tstr | 1;
+    off = (off + 3) & ~3;
+    P.tmp_off = off; P.tmp_smem = 1;
+    off += 2 * (T + 1) * P.tmp_stride;
+  }
   P.smem_elems = off;
   P.smem_bytes = off * 4 + 32;
   P.carry_elems = carry;

@@ -267,6 +267,106 @@ CMGB_DEV void tr_scan_body(const TrKParams &p, float *smf, int tid, int nt, int 
               own[pm * mst + r * stride + d] = val;
               if (r == TT) cout[carry + pm * stride + d - lo] = val;
             }
+          // (2) the self-loop planes (IL: J and L; IR: J and R)
+          if (ALG == 0) {
+            // CYK: max is order-free, so every term but the self-loop is folded
+            // for all band cells in parallel into the scratch (plane slot 0: J,
+            // slot 1: L for IL, R for IR), and the chains fold the self-loop
+            // last: x = max(t, x + tself) + e
+            T *tmp = reinterpret_cast<T *>(smf) + P.tmp_off;
+            const int tstr = P.tmp_stride, tpl = (TT + 1) * tstr;
+            const int m1 = il ? 1 : 2;                   // second self-loop plane
+            const bool two = il ? (bool) fL : (bool) fR;
+            const int crow0 = il ? 0 : 1;                // children at row r (IL) or r-1 (IR), length d-1
+            for (CellWalk c(tid, 1, dxW, wpb, srb, sddb, invb); c.r <= nrows; c.next()) {
+              const int r = c.r, d = c.d;
+              if (d > jp0 + r) continue;
+              T sJ = INIT(d - 1), s1 = sJ;
+              CMGB_FOR_CHILD(o, 1) {
+                sJ = MAXT(sJ, R::add(CHV(o, 0, r - crow0, d - 1), tv[o]));
+                if (two) s1 = MAXT(s1, R::add(CHV(o, m1, r - crow0, d - 1), tv[o]));
+              }
+              tmp[r * tstr + d - lo] = sJ;
+              if (two) tmp[tpl + r * tstr + d - lo] = s1;
+            }
+            CMGB_SYNC();
+            const T tself = tv[0];
+            if (il) {
+              // IL(r,d) <- IL(r,d-1): one thread per (row, plane), serial in d
+              const int npl = two ? 2 : 1;
+              for (int q = tid; q < npl * nrows; q += nt) {
+                const int mi = q % npl, r = 1 + q / npl, m = mi ? 1 : 0;
+                const int jp = jp0 + r;
+                const int dx = jp < dxW ? jp : dxW;
+                T *row = own + m * mst + r * stride;
+                const T *trow = tmp + mi * tpl + r * tstr - lo;
+                T *crow = r == TT ? cout + carry + m * stride - lo : nullptr;
+                for (int d = lo; d <= hi; d++)
+                  if (d < 1 || d > dx) { const T pv = d == 0 ? (m == 0 ? i0v : imp) : imp; row[d] = pv; if (crow) crow[d] = pv; }
+                T x = m == 0 ? i0v : imp;   // the d = 0 cell
+                for (int d0 = 1; d0 <= dx; d0 += CMGB_CHUNK) {
+                  const int n = dx - d0 + 1;
+                  T tt[CMGB_CHUNK], ee[CMGB_CHUNK];
+#pragma unroll
+                  for (int u = 0; u < CMGB_CHUNK; u++) {
+                    tt[u] = u < n ? trow[d0 + u] : imp;
+                    ee[u] = u < n ? ESC1(res[W + r - d0 - u]) : (T) 0;
+                  }
+#pragma unroll
+                  for (int u = 0; u < CMGB_CHUNK; u++) {
+                    const T nx = (m == 1 && d0 + u == 1) ? ee[u] : R::add(MAXT(tt[u], R::add(x, tself)), ee[u]);
+                    if (u < n) {
+                      x = nx;
+                      row[d0 + u] = x;
+                      if (crow) crow[d0 + u] = x;
+                    }
+                  }
+                }
+              }
+            } else {
+              // IR(r,d) <- IR(r-1,d-1): one thread per (diagonal, plane); a
+              // diagonal's band cells are one run b0..b1 (d <= jp holds on a
+              // whole diagonal or on none of it)
+              const int ndiag = hi - lo + 1 + TT;
+              const int npl = two ? 2 : 1;
+              const int dstep = stride + 1, tstep = tstr + 1;
+              for (int q = tid; q < npl * ndiag; q += nt) {
+                const int mi = q % npl, cdg = lo - TT + q / npl, m = mi ? 2 : 0;
+                const int ra = lo - cdg > 1 ? lo - cdg : 1, rz = hi - cdg < nrows ? hi - cdg : nrows;
+                if (ra > rz) continue;
+                const int b0 = 1 - cdg > ra ? 1 - cdg : ra;
+                const int b1 = cdg > jp0 ? ra - 1 : (dxW - cdg < rz ? dxW - cdg : rz);
+                T *base = own + m * mst;
+                const T pad0 = m == 0 ? i0v : imp;   // a d = 0 cell of this plane
+                T *out = base + ra * stride + cdg + ra;
+                if (b0 > b1) {
+                  for (int r = ra; r <= rz; r++, out += dstep) *out = cdg + r == 0 ? pad0 : imp;
+                } else {
+                  T x = (ra == 1 && cdg >= lo) ? base[cdg] : imp;   // the diagonal's row-0 cell
+                  for (int r = ra; r < b0; r++, out += dstep) { x = cdg + r == 0 ? pad0 : imp; *out = x; }
+                  for (int r = b0; r <= b1; r += CMGB_CHUNK, out += CMGB_CHUNK * dstep) {
+                    const int n = b1 - r + 1;
+                    const T *tp = tmp + mi * tpl + r * tstr + cdg + r - lo;
+                    T tt[CMGB_CHUNK], ee[CMGB_CHUNK];
+#pragma unroll
+                    for (int u = 0; u < CMGB_CHUNK; u++) {
+                      tt[u] = u < n ? tp[u * tstep] : imp;
+                      ee[u] = u < n ? ESC1(res[W + r + u - 1]) : (T) 0;
+                    }
+#pragma unroll
+                    for (int u = 0; u < CMGB_CHUNK; u++) {
+                      const T nx = (m == 2 && cdg + r + u == 1) ? ee[u] : R::add(MAXT(tt[u], R::add(x, tself)), ee[u]);
+                      if (u < n) { x = nx; out[u * dstep] = x; }
+                    }
+                  }
+                  out = base + (b1 + 1) * stride + cdg + b1 + 1;
+                  for (int r = b1 + 1; r <= rz; r++, out += dstep) *out = cdg + r == 0 ? pad0 : imp;
+                }
+                // the diagonal's row-TT cell is the next tile's carry
+                if (TT <= nrows && TT >= ra && TT <= rz) cout[carry + m * stride + cdg + TT - lo] = base[TT * stride + cdg + TT];
+              }
+            }
+          } else {
           CMGB_SYNC();
           // (2) the self-loop chains, children folded in the reference's order
           if (il) {
@@ -345,6 +445,7 @@ CMGB_DEV void tr_scan_body(const TrKParams &p, float *smf, int tid, int nt, int 
                 xJ = vJ; xR = vR;
               }
             }
+          }
           }
           CMGB_SYNC();
           // (3) root accumulators and per-state best over the finished band cells

@@ -19,10 +19,11 @@ def _target(m, seed, bg=20):
     return s[len(s) // 2:] + "".join(rng.choice(list("ACGU"), bg))
 
 
-@pytest.mark.parametrize("algo,pidx,qdb,T,win,arena,ng", [
-    ("trcyk", 4, 1, 8, 0, 1, 0), ("trinside", 3, 2, 8, 16, 2, 0), ("trcyk", 2, 0, 16, 24, 2, 1)])
-def test_emulated_tr_kernel_matches_oracle(emu, models, algo, pidx, qdb, T, win, arena, ng):
-    m = models["tRNA"]
+@pytest.mark.parametrize("name,algo,pidx,qdb,T,win,arena,ng", [
+    ("tRNA", "trcyk", 4, 1, 8, 0, 1, 0), ("tRNA", "trinside", 3, 2, 8, 16, 2, 0), ("tRNA", "trcyk", 2, 0, 16, 24, 2, 1),
+    ("tRNA", "trcyk", 3, 1, 5, 0, 1, 0), ("Vault", "trcyk", 4, 2, 12, 30, 2, 0)])
+def test_emulated_tr_kernel_matches_oracle(emu, models, name, algo, pidx, qdb, T, win, arena, ng):
+    m = models[name]
     seq = _target(m, 7)
     dsq = cmfile.digitize(seq)
     n = len(seq)
