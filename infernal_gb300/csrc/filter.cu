@@ -68,27 +68,53 @@ __device__ __forceinline__ float bf2f(unsigned short h) { return __uint_as_float
 
 // Layer 0: one-hot input -> 128 channels (a gather of nine weight rows).
 // Window win starts at residue i0 + win * wstride (W when scanning, 2W for
-// training batches stored back to back).
-__global__ void filter_layer0(const unsigned char *dsq, long long i0, long long j0, long long W, long long wstride, int nwin,
-                              int LP, const float *w0, const float *b, unsigned short *out)
+// training batches stored back to back).  A block computes one 128-row tile
+// of one window: the tile's residue codes (and four on each side) and the
+// weights sit in shared memory, and each thread produces eight channels of a
+// row (one 16-byte store), summing the taps in order.
+__global__ void __launch_bounds__(256) filter_layer0(const unsigned char *dsq, long long i0, long long j0, long long W,
+                                                     long long wstride, int nwin, int LP, const float *w0, const float *b,
+                                                     unsigned short *out)
 {
-  const int win = blockIdx.y;
-  const int co = threadIdx.x;                  // 128 threads
+  __shared__ float sw[KT * 4 * CH];
+  __shared__ float sb[CH];
+  __shared__ unsigned char sx[TILE + KT - 1];
+  const int tile = blockIdx.x, win = blockIdx.y;
   const long long ws = i0 + (long long) win * wstride;   // first residue of the window
-  for (int i = blockIdx.x; i < LP; i += gridDim.x) {
-    float acc = b[co];
+  for (int k = threadIdx.x; k < KT * 4 * CH; k += blockDim.x) sw[k] = w0[k];
+  for (int k = threadIdx.x; k < CH; k += blockDim.x) sb[k] = b[k];
+  for (int k = threadIdx.x; k < TILE + KT - 1; k += blockDim.x) {
+    const long long q = (long long) tile * TILE + k - 4;   // window position of tap row k
+    unsigned char x = 255;
+    if (q >= 0 && q < 2 * W && ws + q <= j0) { const unsigned char c = dsq[ws + q]; if (c < 4) x = c; }
+    sx[k] = x;
+  }
+  __syncthreads();
+  for (int task = threadIdx.x; task < TILE * (CH / 8); task += blockDim.x) {
+    const int r = task / (CH / 8), cg = task % (CH / 8);
+    const int i = tile * TILE + r;
+    uint4 v = make_uint4(0, 0, 0, 0);
     if (i < 2 * W) {
+      float acc[8];
+#pragma unroll
+      for (int c = 0; c < 8; c++) acc[c] = sb[cg * 8 + c];
       for (int t = 0; t < KT; t++) {
-        const int q = i + t - 4;
-        if (q < 0 || q >= 2 * W) continue;
-        const long long pos = ws + q;
-        if (pos > j0) continue;
-        const int x = dsq[pos];
-        if (x < 4) acc += w0[(t * 4 + x) * CH + co];
+        const unsigned char x = sx[r + t];
+        if (x < 4) {
+          const float *wr = sw + (t * 4 + x) * CH + cg * 8;
+#pragma unroll
+          for (int c = 0; c < 8; c++) acc[c] += wr[c];
+        }
       }
-      acc = acc > 0.f ? acc : 0.f;
-    } else acc = 0.f;
-    out[((size_t) win * LP + i) * CH + co] = f2bf(acc);
+      unsigned pk[4];
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        const float a0 = acc[2 * c] > 0.f ? acc[2 * c] : 0.f, a1 = acc[2 * c + 1] > 0.f ? acc[2 * c + 1] : 0.f;
+        pk[c] = (unsigned) f2bf(a0) | ((unsigned) f2bf(a1) << 16);
+      }
+      v = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    }
+    *reinterpret_cast<uint4 *>(out + ((size_t) win * LP + i) * CH + cg * 8) = v;
   }
 }
 
@@ -399,7 +425,7 @@ extern "C" int cmgb_filter_windows(cmgb_ctx *ctx, cmgb_filter *f, const uint8_t 
   cudaEvent_t e0, e1;
   FCUDA(cudaEventCreate(&e0)); FCUDA(cudaEventCreate(&e1));
   FCUDA(cudaEventRecord(e0));
-  filter_layer0<<<dim3(64, nwin), CH>>>(d_dsq, i0, j0, W, W, nwin, f->LP, f->d_w0, f->d_b, f->d_act[0]);
+  filter_layer0<<<dim3(f->LP / TILE, nwin), 256>>>(d_dsq, i0, j0, W, W, nwin, f->LP, f->d_w0, f->d_b, f->d_act[0]);
   FCUDA(cudaGetLastError());
   int cur = 0;
   for (int l = 1; l < NL; l++) {
@@ -771,7 +797,7 @@ extern "C" int cmgb_filter_trainer_step_heads(cmgb_filter_trainer *f, const uint
   FCUDA(cudaMemcpy(f->posw, pos_weights, sizeof(float) * H, cudaMemcpyHostToDevice));
   FCUDA(cudaEventRecord(e0));
   // forward
-  filter_layer0<<<dim3(64, B), CH>>>(f->win, 0, (long long) B * W2 - 1, W, W2, B, LP, f->p + OFF_W0, f->p + OFF_B, f->act[0]);
+  filter_layer0<<<dim3(LP / TILE, B), 256>>>(f->win, 0, (long long) B * W2 - 1, W, W2, B, LP, f->p + OFF_W0, f->p + OFF_B, f->act[0]);
   for (int l = 1; l < NL; l++) {
     const int d = DIL[l];
     conv_launch(f->act[l - 1], f->act[l], LP, W2, d, B, f->wbf + (size_t) (l - 1) * KT * CH * CH, f->p + OFF_B + l * CH, f->err, nullptr);
