@@ -10,10 +10,17 @@
 // Within a window the end positions advance in tiles of T rows.  For each
 // tile the states are swept v = M-1 .. 0 with one CTA barrier per state; the
 // state's T x band cells are computed in parallel from its children's tiles
-// in shared memory (see scan_plan.h for the layout).  Per state kind:
-//   generic states / BEGL_S / B : one warp per row, lanes over d
-//   IL (self-loop on the same row, serial in d) : one thread per row
-//   IR (self-loop on the previous row, serial along a diagonal) : one thread per diagonal
+// (in shared memory, or in a per-CTA global arena served from L1/L2; see
+// scan_plan.h for the layout).  Per state kind:
+//   generic states : column-fixed walk, a thread owns one column d and every
+//                    rs-th row, four rows of child loads in flight
+//   BEGL_S / B     : flattened walk over all cells
+//   IL (self-loop on the same row, serial in d) : non-self terms in parallel,
+//                    then one thread per row over its band run
+//   IR (self-loop on the previous row, serial along a diagonal) : non-self
+//                    terms in parallel, then one thread per diagonal
+// Each phase's record (descriptor + emission row) arrives by TMA one phase
+// ahead, and each phase prefetches the next phase's carry row into registers.
 // BEGL_S rows go to a per-CTA history ring in global memory, which the
 // bifurcation's k-loop reads (alpha_begl[(j-k)%(W+1)], src/cm_dpsearch.c:253-277).
 // Local begins are folded into a root accumulator while each state's cells

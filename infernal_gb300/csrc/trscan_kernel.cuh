@@ -11,7 +11,9 @@
 // selects which of L, R, T are filled (cm_TrFillFromPassIdx,
 // src/cm_dpsearch_trunc.c:3566).  Inside every cell the scores combine in the
 // reference's order (init score first, then children in yoffset order), so
-// the integer Inside result is bit-identical.
+// the integer Inside result is bit-identical; for CYK, whose max is
+// order-free, the insert self-loop chains fold their other terms in a
+// parallel pass first.
 //
 // Root.  The truncated scanners leave the root through truncated begins only
 // (a penalty into any state), and they never reset the root's cells: a
