@@ -29,7 +29,7 @@ def _check(r, hits, ei, ej, sc, vsc):
         assert np.array_equal(r.vsc.view(np.int32), np.asarray(vsc, np.float32).view(np.int32))
 
 
-@pytest.mark.parametrize("T,arena", [(16, 1), (5, 1), (48, 2)])
+@pytest.mark.parametrize("T,arena", [(16, 1), (5, 1), (48, 2), (128, 2)])
 def test_golden_on_gpu(gpu, golden, models, T, arena):
     """Shared-memory tiles (arena 1) and the global-memory tile arena (arena 2)."""
     meta, arrays = golden

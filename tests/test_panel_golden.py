@@ -2,7 +2,8 @@
 bifurcations, W 89-408) against golden vectors written by the reference's
 own FastCYKScan (QDB1) and FastIInsideScan (QDB2) on seeded 4.4 kb targets
 with emitted sequences embedded (tests/golden/gen_panel_golden.py): the
-oracle on the CPU, the GPU scanners in both tile placements, bit for bit."""
+oracle on the CPU, the kernel source in the host emulation, the GPU scanners
+in both tile placements, bit for bit."""
 import json
 import os
 
@@ -43,8 +44,24 @@ def test_panel_oracle_matches_reference(panel, k):
     _check(*r, c, arrays)
 
 
+@pytest.mark.parametrize("T,arena", [(24, 2), (128, 2)])
+def test_panel_emulated_kernel_matches_reference(panel, emu, T, arena):
+    """The scan kernel's source, run by the host-thread emulation of a CTA,
+    on every panel case: hits, envelope, best score and per-state scores bit
+    for bit against the reference's own output."""
+    meta, arrays, models = panel
+    emu.set_shape(T, 0, 1, 0, arena)
+    try:
+        for c in meta:
+            r = emu.scan(models[c["model"]], arrays["dsq." + c["seq"]], c["i0"], c["j0"], algo=c["algo"], qdbidx=c["qdbidx"],
+                         cutoff=c["cutoff"], do_null3=bool(c["null3"]), env_cutoff=c["env_cutoff"], want_vsc=True)
+            _check(r.hits, r.envi, r.envj, r.sc, r.vsc, c, arrays)
+    finally:
+        emu.set_shape(0, 0, 0)
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("T,arena", [(16, 1), (48, 2)])
+@pytest.mark.parametrize("T,arena", [(16, 1), (48, 2), (128, 2)])
 def test_panel_on_gpu(panel, T, arena):
     meta, arrays, models = panel
     s = L.Scanner(0)
