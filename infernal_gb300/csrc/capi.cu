@@ -746,16 +746,18 @@ static int scan_tr(cmgb_ctx *c, cmgb_model *m, char *errbuf, int qdbidx, int pas
   c->last_h2d = (dev_dsq_in ? 0 : (int64_t) (j0 + 2 - lo)) + (int64_t) sizeof(Control);
 
   const bool gl = P.arena_global != 0;
+  // the kernel's dynamic shared-memory limit is set for every plan (an
+  // explicit CTA count skips only the occupancy query's answer)
   int cps = c->ctas_per_sm;
-  if (cps == 0) {
 #ifndef CMGB_HOST_EMULATION
+  {
     int nb = 1;
     CUDA_TRY(prepare_tr_any(alg, gl, c->threads, P.smem_bytes, &nb));
-    cps = nb < 1 ? 1 : nb;
-#else
-    cps = 1;
-#endif
+    if (cps == 0) cps = nb < 1 ? 1 : nb;
   }
+#else
+  if (cps == 0) cps = 1;
+#endif
   const int grid_max = c->nsm * cps;
   int64_t win = c->window_len;
   if (win <= 0) {
@@ -1075,17 +1077,19 @@ static int scan_batch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo, int qd
   c->last_h2d = (d_seqs ? 0 : seqs_len) + (int64_t) (3 * sizeof(long long) * nw + out_bytes + sizeof(Control));
 
   const bool gl = P->arena_global != 0;
+  // the kernel's dynamic shared-memory limit is set for every plan (an
+  // explicit CTA count skips only the occupancy query's answer)
   int cps = c->ctas_per_sm;
-  if (cps == 0) {
 #ifndef CMGB_HOST_EMULATION
+  {
     int nb = 1;
     if (tr) CUDA_TRY(prepare_tr_any(alg, gl, c->threads, P->smem_bytes, &nb));
     else CUDA_TRY(prepare_any(alg, gl, c->threads, P->smem_bytes, &nb));
-    cps = nb < 1 ? 1 : nb;
-#else
-    cps = 1;
-#endif
+    if (cps == 0) cps = nb < 1 ? 1 : nb;
   }
+#else
+  if (cps == 0) cps = 1;
+#endif
   const int grid = std::min(nw, c->nsm * cps);
   if ((st = grow((void **) &c->d_carry, &c->carry_bytes, sizeof(float) * 2 * (size_t) P->carry_elems * grid, errbuf)) != CMGB_OK) return st;
   if ((st = grow((void **) &c->d_ring, &c->ring_bytes, sizeof(float) * (size_t) P->ring_elems * grid, errbuf)) != CMGB_OK) return st;
@@ -1409,16 +1413,18 @@ static int scan_multi(cmgb_ctx *c, cmgb_model *const *models, int nmodels, const
       long long *env = reinterpret_cast<long long *>(out_init.data());
       for (int w = 0; w < nw; w++) { env[2 * w] = LLONG_MAX; env[2 * w + 1] = -1; }
     }
+    // the kernel's dynamic shared-memory limit is set for every launch (an
+    // explicit CTA count skips only the occupancy query's answer)
     int cps = c->ctas_per_sm;
-    if (cps == 0) {
 #ifndef CMGB_HOST_EMULATION
+    {
       int nb = 1;
       CUDA_TRY(prepare_any(alg, gl, c->threads, smem, &nb, true));
-      cps = nb < 1 ? 1 : nb;
-#else
-      cps = 1;
-#endif
+      if (cps == 0) cps = nb < 1 ? 1 : nb;
     }
+#else
+    if (cps == 0) cps = 1;
+#endif
     const int grid = std::min(nw, c->nsm * cps);
     if ((st = grow((void **) &c->d_carry, &c->carry_bytes, sizeof(float) * 2 * (size_t) max_carry * grid, errbuf)) != CMGB_OK) return st;
     if ((st = grow((void **) &c->d_ring, &c->ring_bytes, sizeof(float) * (size_t) max_ring * grid, errbuf)) != CMGB_OK) return st;

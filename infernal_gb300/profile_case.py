@@ -1,7 +1,7 @@
 """One scan of a stored model on a seeded synthetic target, for profiling.
 
-    python -m infernal_gb300.profile_case <model> <length> <cyk|inside|finside> [tile_rows arena]
-    python -m infernal_gb300.profile_case <model> <nreads> <trcyk|trinside> [tile_rows arena]
+    python -m infernal_gb300.profile_case <model> <length> <cyk|inside|finside> [tile_rows arena [ctas_per_sm]]
+    python -m infernal_gb300.profile_case <model> <nreads> <trcyk|trinside> [tile_rows arena [ctas_per_sm]]
     python -m infernal_gb300.profile_case <model> <length> filter
     python -m infernal_gb300.profile_case <model> <length> learned
 
@@ -37,8 +37,9 @@ def main(argv):
     sc = lib.Scanner(0)
     shape = None
     if len(argv) > 5:
-        sc.set_shape(int(argv[4]), 0, 0, 0, int(argv[5]))
-        shape = (int(argv[4]), int(argv[5]))
+        cps = int(argv[6]) if len(argv) > 6 else 0
+        sc.set_shape(int(argv[4]), 0, cps, 0, int(argv[5]))
+        shape = (int(argv[4]), int(argv[5])) + ((cps,) if cps else ())
     if algo == "learned":
         # the default bench line's step on a <length>-residue target (both
         # strands): filter, CYK on the kept regions, Inside on survivors

@@ -93,3 +93,25 @@ def test_batch_contract_errors(gpu, models):
     st = lib.cmgb_ScanBatch(gpu._ctx, gpu.model(m), err, 0, 1, 0, d.ctypes.data, len(d), offs.ctypes.data,
                             lens.ctypes.data, 1, 0.0, None, 0, 0.0, None, None, None, None, None)
     assert st == 10 and b"outside the buffer" in err.value
+
+
+def test_explicit_ctas_per_sm_with_large_shared_memory(models):
+    """A launch shape with an explicit CTA count still sets each kernel's
+    dynamic shared-memory limit: a truncated batch whose 32-row plan needs
+    about 90 KB of shared memory, at one CTA per SM, equals the default
+    launch."""
+    m = models["Plant_SRP"]
+    rng = np.random.default_rng(zlib.crc32(b"explicit-cps"))
+    reads = [cmfile.digitize("".join(rng.choice(list("ACGU"), int(rng.integers(150, 301))))) for _ in range(24)]
+    reads[3] = cmfile.digitize(emit.sample(m, rng)[40:])
+    s = L.Scanner(0)
+    try:
+        out = []
+        for cps in (0, 1):
+            s.set_shape(32, 0, cps, 0, 2)
+            rs = s.scan_batch(m, reads, algo="trcyk", qdbidx=1, pass_idx=4, cutoff=5.0, env_cutoff=5.0)
+            out.append([(r.hits, r.envi, r.envj, np.float32(r.sc).view(np.uint32)) for r in rs])
+        assert out[0] == out[1]
+        assert any(h for h, _, _, _ in out[0])
+    finally:
+        s.close()
