@@ -1204,12 +1204,26 @@ static int scan_batch(cmgb_ctx *c, cmgb_model *m, char *errbuf, int algo, int qd
       std::vector<int> by_off(nseq);
       for (int q = 0; q < nseq; q++) by_off[q] = q;
       std::sort(by_off.begin(), by_off.end(), [&](int a, int b) { return offsets[a] < offsets[b]; });
-      for (const CandHost &ch : c->h_cand) {
-        int lo = 0, hi = nseq - 1;   // last sequence whose offset is below j
-        while (lo < hi) { const int mid = (lo + hi + 1) / 2; if (offsets[by_off[mid]] < ch.j) lo = mid; else hi = mid - 1; }
-        CandHost x = ch; x.mode = CMGB_TRMODE_J;
-        per[by_off[lo]].push_back(x);
-      }
+      std::vector<long long> soff(nseq);
+      for (int q = 0; q < nseq; q++) soff[q] = offsets[by_off[q]];
+      // each candidate to its sequence (the last whose offset is below j);
+      // contiguous slices of the candidates on host threads, each into its own
+      // per-sequence lists, appended in slice order (the serial order)
+      const size_t ncand = c->h_cand.size();
+      const int nsl = nseq <= 4096 ? (int) std::min<size_t>(16, std::max<size_t>(1, ncand / 65536)) : 1;
+      std::vector<std::vector<std::vector<CandHost>>> part((size_t) nsl, std::vector<std::vector<CandHost>>((size_t) nseq));
+      parallel_for(nsl, [&](int t) {
+        const size_t a = ncand * (size_t) t / (size_t) nsl, b = ncand * (size_t) (t + 1) / (size_t) nsl;
+        for (size_t k = a; k < b; k++) {
+          const CandHost &ch = c->h_cand[k];
+          int lo = 0, hi = nseq - 1;
+          while (lo < hi) { const int mid = (lo + hi + 1) / 2; if (soff[mid] < ch.j) lo = mid; else hi = mid - 1; }
+          CandHost x = ch; x.mode = CMGB_TRMODE_J;
+          part[t][by_off[lo]].push_back(x);
+        }
+      });
+      for (int q = 0; q < nseq; q++)
+        for (int t = 0; t < nsl; t++) per[q].insert(per[q].end(), part[t][q].begin(), part[t][q].end());
     }
     const long long *env = reinterpret_cast<const long long *>(outv.data());
     const unsigned *best = reinterpret_cast<const unsigned *>(outv.data() + sizeof(long long) * 2 * nw);

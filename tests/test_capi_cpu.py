@@ -111,3 +111,23 @@ def test_contract_errors(emu, models):
     with pytest.raises(L.ScanError) as e:
         emu.set_shape(-1, 0, 0)
     assert e.value.status == 11
+
+
+def test_emulated_batch_with_many_candidates_matches_oracle(emu, models):
+    """A batch whose candidate cells (every finite root cell at a very low
+    cutoff, about 200,000 of them) are spread over the sequences by several
+    host threads: every sequence's hits, envelope and best score equal the
+    oracle's scan of that sequence."""
+    m = models["tRNA"]
+    rng = np.random.default_rng(17)
+    seqs = [cmfile.digitize("".join(rng.choice(list("ACGU"), int(n)))) for n in rng.integers(150, 400, size=5)]
+    emu.set_shape(16, 0, 1, 0, 2)
+    try:
+        rs = emu.scan_batch(m, seqs, algo="cyk", qdbidx=1, cutoff=-40.0, env_cutoff=1.0)
+    finally:
+        emu.set_shape(0, 0, 0)
+    assert sum(len(s) - 2 for s in seqs) * 100 > 131072   # enough root cells for more than one slice
+    for dsq, r in zip(seqs, rs):
+        o = oracle.scan(m, dsq, 1, len(dsq) - 2, algo="cyk", qdbidx=1, cutoff=-40.0, env_cutoff=1.0)
+        assert r.hits == o[0]
+        assert (r.envi, r.envj) == (o[1], o[2]) and np.float32(r.sc) == np.float32(o[3])
