@@ -91,43 +91,61 @@ static inline void count_res(double *ct, uint8_t x, int K)
 // sums that start at i0 (act[], src/cm_dpsearch.c:199-231).  When every code
 // in the range has weight 1, 1/2 or 1/4 those sums are exact, and so are
 // integer prefix counts in quarter units, which give the same doubles in
-// O(1) per lookup; three-way codes (H, B, V, D) need the running doubles
-// themselves.
+// O(1) per lookup (ranges longer than kPrefixMaxResidues count each lookup's
+// residues instead, the same doubles without 16 bytes per residue).
+// Three-way codes (H, B, V, D) need the running doubles themselves: they are
+// accumulated in order from i0 as lookups ask for later end positions (the
+// resolvers visit end positions in increasing order), and a ring keeps the
+// last maxd + 1 rows, as the reference's act[jp % (W+1)].
+static const int64_t kPrefixMaxResidues = 16 << 20;
 struct Composition {
   const uint8_t *dsq; int64_t i0, j0; int K;
   bool exact_direct = true;
+  bool counted = false;          // exact_direct over a range too long for prefix counts: count per lookup
   std::vector<int32_t> qprefix;  // (j0-i0+2) x K running counts in quarter units (exact_direct)
-  std::vector<double> prefix;    // (j0-i0+2) x K running sums (three-way codes)
-  Composition(const uint8_t *q, int64_t a, int64_t b, int k) : dsq(q), i0(a), j0(b), K(k) {
+  // three-way codes: running sums of positions i0-1 .. cur in a ring of R rows
+  int R = 0;
+  mutable int64_t cur = 0;
+  mutable std::vector<double> ring;
+  Composition(const uint8_t *q, int64_t a, int64_t b, int k, int maxd) : dsq(q), i0(a), j0(b), K(k) {
     for (int64_t x = i0; x <= j0; x++) { uint8_t c = dsq[x]; if (c >= K && c < 18 && __builtin_popcount(degen_mask[c]) == 3) { exact_direct = false; break; } }
-    const size_t n = (size_t) (j0 - i0 + 2) * K;
-    if (exact_direct) {
-      qprefix.assign(n, 0);
-      for (int64_t x = i0; x <= j0; x++) {
-        int32_t *cur = &qprefix[(size_t) (x - i0 + 1) * K];
-        std::memcpy(cur, cur - K, sizeof(int32_t) * K);
-        const uint8_t c = dsq[x];
-        if (c < K) cur[c] += 4;
-        else if (c < 18) {
-          const int nb = __builtin_popcount(degen_mask[c]);
-          if (nb) for (int y = 0; y < K; y++) if (degen_mask[c] & (1 << y)) cur[y] += 4 / nb;
-        }
-      }
-    } else {
-      prefix.assign(n, 0.);
-      for (int64_t x = i0; x <= j0; x++) {
-        double *cur = &prefix[(size_t) (x - i0 + 1) * K];
-        std::memcpy(cur, cur - K, sizeof(double) * K);
-        count_res(cur, dsq[x], K);
+    if (!exact_direct) {
+      R = maxd + 2;
+      ring.assign((size_t) R * K, 0.);   // row of position i0-1: all zero
+      cur = i0 - 1;
+      return;
+    }
+    if (j0 - i0 + 1 > kPrefixMaxResidues) { counted = true; return; }
+    qprefix.assign((size_t) (j0 - i0 + 2) * K, 0);
+    for (int64_t x = i0; x <= j0; x++) {
+      int32_t *row = &qprefix[(size_t) (x - i0 + 1) * K];
+      std::memcpy(row, row - K, sizeof(int32_t) * K);
+      const uint8_t c = dsq[x];
+      if (c < K) row[c] += 4;
+      else if (c < 18) {
+        const int nb = __builtin_popcount(degen_mask[c]);
+        if (nb) for (int y = 0; y < K; y++) if (degen_mask[c] & (1 << y)) row[y] += 4 / nb;
       }
     }
   }
+  const double *ring_row(int64_t x) const { return &ring[(size_t) ((x - i0 + 1) % R) * K]; }
   void get(int64_t i, int64_t j, float *comp) const {
-    if (exact_direct) {
+    if (counted) {
+      double ct[8] = {0};
+      for (int64_t x = i; x <= j; x++) count_res(ct, dsq[x], K);
+      for (int a = 0; a < K; a++) comp[a] = (float) ct[a];
+    } else if (exact_direct) {
       const int32_t *hi = &qprefix[(size_t) (j - i0 + 1) * K], *lo = &qprefix[(size_t) (i - i0) * K];
       for (int a = 0; a < K; a++) comp[a] = (float) ((double) (hi[a] - lo[a]) * 0.25);
     } else {
-      const double *hi = &prefix[(size_t) (j - i0 + 1) * K], *lo = &prefix[(size_t) (i - i0) * K];
+      while (cur < j) {   // accumulate the running sums up to j
+        const double *prev = ring_row(cur);
+        cur++;
+        double *row = const_cast<double *>(ring_row(cur));
+        if (row != prev) std::memcpy(row, prev, sizeof(double) * K);
+        count_res(row, dsq[cur], K);
+      }
+      const double *hi = ring_row(j), *lo = ring_row(i - 1);
       for (int a = 0; a < K; a++) comp[a] = (float) (hi[a] - lo[a]);
     }
   }
@@ -183,7 +201,11 @@ void resolve_hits(std::vector<CandHost> &c, const ResolveArgs &a, std::vector<cm
   logsum_tables(nullptr, nullptr);
   sort_jd(c);
   Composition *cmp = nullptr;
-  if (a.do_null3 && !c.empty()) cmp = new Composition(a.dsq, a.i0, a.j0, a.K);
+  if (a.do_null3 && !c.empty()) {
+    int maxd = 1;
+    for (const CandHost &x : c) maxd = std::max(maxd, x.d);
+    cmp = new Composition(a.dsq, a.i0, a.j0, a.K, maxd);
+  }
 
   if (a.greedy) {
     // ReportHitsGreedily per j, then greedy overlap removal
