@@ -649,7 +649,12 @@ CMGB_DEV void qdb_scan_body(const KParams &p0, float *smf, int tid, int nt, int 
             // Column-fixed walk: a thread owns one column d of [lo, hi] and
             // every rs-th row, so the band tests, the local-end term and the
             // local-begin test are per column, and each child's address and
-            // the emission indices advance by a constant per cell.
+            // the emission indices advance by a constant per cell.  The child
+            // values (and accumulator cells) of CMGB_RB of the thread's rows
+            // are loaded before any of them is computed and stored; rows
+            // above the band (d > jp, the window's first rows) are evaluated
+            // too (their child reads stay inside the children's buffers) and
+            // then take the pad value.
             const ColWalk cw = col_walk(hi - lo + 1, tid, nt);
             auto cells = [&](auto cn_, auto em_) {
               constexpr int CN = decltype(cn_)::value, EM = decltype(em_)::value;
